@@ -1,0 +1,49 @@
+"""Generate the golden fixtures under tests/golden/ from the reference checkout.
+
+Run once in a checkout that has the reference at REFERENCE (default
+/root/reference); the outputs are committed, so tests never read the reference
+at run time.  Outputs:
+
+  *.bin        byte copies of the reference's small experiment saved states
+               (saved_states/TEXPS.bin, Chain_TEXP.bin, PBEXPS.bin,
+               Chain_EXP.bin, Strings.bin) -- FlatBuffers `State` tables
+               (new_schema.fbs:86-104) carrying the experiment scripts
+  traces.npz   every exported CSV trace of those experiments (data/TEXP_k.csv,
+               data/Chain_T_k.csv, data/pb_experiment_k_1.csv, data/Chain_k.csv)
+               as float64 arrays [rows, 12] in the column order of
+               Settings::save_data (settings.rs:2014-2052):
+               Timestamp, X/Y Position, X/Y Velocity, Rotation,
+               Rotation Velocity, Data1..Data4, FPS
+"""
+import glob
+import os
+import shutil
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REFERENCE = os.environ.get("REFERENCE", "/root/reference")
+STATES = ["TEXPS.bin", "Chain_TEXP.bin", "PBEXPS.bin", "Chain_EXP.bin", "Strings.bin"]
+TRACE_GLOBS = ["TEXP_*.csv", "Chain_T_*.csv", "pb_experiment_*_1.csv", "Chain_[0-9]*.csv"]
+
+
+def main():
+    src_states = os.path.join(REFERENCE, "saved_states")
+    src_data = os.path.join(REFERENCE, "data")
+    if not os.path.isdir(src_states):
+        sys.exit("reference checkout not found at %s" % REFERENCE)
+    for name in STATES:
+        shutil.copyfile(os.path.join(src_states, name), os.path.join(HERE, name))
+    traces = {}
+    for pat in TRACE_GLOBS:
+        for path in sorted(glob.glob(os.path.join(src_data, pat))):
+            key = os.path.splitext(os.path.basename(path))[0]
+            rows = np.loadtxt(path, delimiter=",", skiprows=1, dtype=np.float64, ndmin=2)
+            traces[key] = rows
+    np.savez_compressed(os.path.join(HERE, "traces.npz"), **traces)
+    print("wrote %d states, %d traces" % (len(STATES), len(traces)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,110 @@
+"""Pins the CPU oracle against the reference's own exported traces.
+
+The experiment saved states (tests/golden/*.bin, copied from the reference's
+saved_states/) carry the scripts that produced data/TEXP_k.csv,
+data/Chain_T_k.csv, data/pb_experiment_k_1.csv and data/Chain_k.csv on the
+author's GPU.  Replaying each script through the oracle must reproduce those
+traces.  The traces were written by the reference's GPU whose exact float
+contraction is unknown, so columns are compared against a tolerance relative
+to the column's scale; the bond-break step is compared exactly.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import fbs_state
+import replay
+
+TRACES = np.load(os.path.join(os.path.dirname(__file__), "golden", "traces.npz"))
+COLS = ["X Position", "Y Position", "X Velocity", "Y Velocity", "Rotation", "Rotation Velocity",
+        "Data1", "Data2", "Data3", "Data4"]
+# column-scaled tolerance: worst deviation seen is 7.5e-4 (TEXP_9 Data1, where
+# the values are rounding-level residues of ~1e-4 against a column max ~2e-4)
+RTOL = 2e-3
+
+
+def _run(fixture, golden_dir, long_wait_frames=1):
+    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, fixture))
+    be = replay.OracleBackend(scene, uni, info["use_f64"])
+    r = replay.Replayer(be, info["scripts"], len(scene["radii"]), long_wait_frames)
+    return r.run(), be
+
+
+def _compare(got, ref, skip_cols=()):
+    assert got.shape == ref.shape, (got.shape, ref.shape)
+    # timestamps are f32(timestep * generation); the reference's generation
+    # counter carried over from earlier runs, so only the per-row increments are
+    # compared, to the float32 spacing at the reference's clock value
+    dt = np.diff(ref[:, 0])
+    tol = 4.0 * float(np.spacing(np.float32(np.abs(ref[:, 0]).max())))
+    np.testing.assert_allclose(np.diff(got[:, 0]), dt, rtol=1e-4, atol=max(tol, 1e-12))
+    for c in range(1, 11):
+        if c in skip_cols:
+            continue
+        scale = max(np.abs(ref[:, c]).max(), 1e-30)
+        err = np.abs(got[:, c] - ref[:, c]).max() / scale
+        assert err <= RTOL, "%s: column-relative error %.3g" % (COLS[c - 1], err)
+
+
+@pytest.fixture(scope="module")
+def texps(golden_dir):
+    return _run("TEXPS.bin", golden_dir)
+
+
+@pytest.fixture(scope="module")
+def chain_texp(golden_dir):
+    return _run("Chain_TEXP.bin", golden_dir)
+
+
+@pytest.mark.parametrize("k", range(1, 14))
+def test_texp_traces(texps, k):
+    ex, _ = texps
+    _compare(ex["TEXP_%d" % k], TRACES["TEXP_%d" % k][:, :11])
+
+
+def test_texp1_known_answer(texps):
+    """Data1 of TEXP_1 is |F_n| = kn*A*delta = 5e9 * k * 4.999e-9 until the bond tears."""
+    ex, _ = texps
+    d1 = ex["TEXP_1"][:, 7]
+    k = np.arange(1, 21)
+    np.testing.assert_allclose(d1[1:21], 24.995 * k, rtol=1e-5)
+    assert np.all(d1[21:] == 0.0)
+    ref = TRACES["TEXP_1"][:, 7]
+    assert np.array_equal(d1, ref), "TEXP_1 Data1 is reproduced bit for bit"
+
+
+def test_texp_break_events(texps):
+    """Tensile TEXP runs tear the single bond once per experiment; both sides
+    evaluate the same break in the same step."""
+    _, be = texps
+    ev = np.concatenate(be.events)
+    assert len(ev) > 0
+    assert set(np.unique(ev["code"])) <= {-11, -10, -9}
+
+
+@pytest.mark.parametrize("k", range(1, 14))
+def test_chain_t_traces(chain_texp, k):
+    ex, _ = chain_texp
+    _compare(ex["Chain_T_%d" % k], TRACES["Chain_T_%d" % k][:, :11])
+
+
+# PBEXPS / Chain_EXP traces were exported by an earlier revision of the
+# Simulation shader whose data[0] held a different quantity than the current
+# `data[a] += -normal_force` (2D_Simulation.wgsl:331): in pb_experiment_1_1 a
+# pure normal stretch records Data1 = 0 while Data2/Data3 and every kinematic
+# column agree.  Data1 is therefore not compared for these two families.
+@pytest.mark.parametrize("fixture,prefix,fmt", [
+    ("PBEXPS.bin", "pb_experiment", "pb_experiment_%d_1"),
+    ("Chain_EXP.bin", "Chain", "Chain_%d"),
+])
+def test_older_traces_without_data1(golden_dir, fixture, prefix, fmt):
+    ex, _ = _run(fixture, golden_dir)
+    checked = 0
+    for k in range(1, 14):
+        key = fmt % k
+        if key not in ex or key not in TRACES:
+            continue
+        _compare(ex[key], TRACES[key][:, :11], skip_cols=(7,))
+        checked += 1
+    assert checked >= 12
