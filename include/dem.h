@@ -1,0 +1,199 @@
+/*
+ * dem.h -- C ABI of libdemgb.so, the GB300-native per-step DEM pipeline.
+ *
+ * Drop-in for the compute side of gusjengis/Physics-Sim's WGPUComputeProg
+ * (src/wgpu_prog.rs): the scene travels in the reference's host layouts
+ * (src/state.rs:69-93), the settings in the 29-word uniform of
+ * Settings::collision_settings (src/settings.rs:2086-2119), and one call of
+ * dem_step(ctx, n) advances n steps of LOM + Simulation exactly like
+ * WGPUComputeProg::compute with gen_per_frame = n (src/wgpu_prog.rs:1420-1473).
+ *
+ * Conventions: plain pointers and sizes; the caller owns host memory, the
+ * library owns device memory; every call returns 0 or a negative DEM_E_* code
+ * and never aborts; dem_last_error() describes the last failure.  A context is
+ * used by one host thread at a time.
+ */
+#ifndef DEM_H
+#define DEM_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DEM_ABI_VERSION 1
+#define DEM_MAX_CONTACTS 14   /* settings.setup.max_contacts = max_bonds + 8 (settings.rs:263, 310) */
+#define DEM_DATA_SIZE 7       /* DATA_SIZE (state.rs:67) */
+#define DEM_PROPS_WORDS 28    /* Settings::properties (settings.rs:2158-2189) */
+
+enum {
+    DEM_OK = 0,
+    DEM_E_INVALID = -1,      /* bad argument or inconsistent scene */
+    DEM_E_OOM = -2,          /* device or host allocation failed */
+    DEM_E_CUDA = -3,         /* CUDA runtime error */
+    DEM_E_TIMEOUT = -4,      /* a bounded device wait gave up */
+    DEM_E_STATE = -5,        /* device reported an inconsistent state */
+    DEM_E_UNSUPPORTED = -6,  /* feature not available */
+    DEM_E_CAPACITY = -7      /* a bounded buffer overflowed (see dem_last_error) */
+};
+
+/* The Settings uniform, 29 words in the order of collision_settings()
+ * (settings.rs:2086-2119) and of `struct Settings` in 2D_LOM.wgsl:26-56 /
+ * 2D_Simulation.wgsl:34-64.  Binary-identical to that Vec<f32>. */
+typedef struct dem_params {
+    int32_t walls;
+    float hor_bound;
+    float vert_bound;
+    int32_t round_bounds;
+    float bound_radius;
+    float wall_friction;
+    int32_t gravity;
+    int32_t planet_mode;
+    int32_t bonds;
+    int32_t collisions;
+    float friction_coefficient;
+    float gravity_acc;
+    float bond_normal_stiffness;
+    int32_t bonds_tear;
+    float bond_normal_strength;
+    float contact_damping;
+    float bond_damping;
+    float drag;
+    float bond_shear_strength;
+    float dT;
+    float bond_shear_stiffness;
+    float gravity_x;
+    float gravity_y;
+    int32_t mouse_gravity;
+    float moment_contribution_factor;
+    int32_t collision_interval;
+    int32_t local_damping;
+    float local_damping_alpha;
+    int32_t particles;
+} dem_params;
+
+/* GridInfo as uploaded to grid_info_buffer (wgpu_prog.rs:653-675); computed by
+ * grid_capacity (wgpu_prog.rs:698-717) or dem_grid_capacity() below. */
+typedef struct dem_grid_info {
+    float cell_size;
+    int32_t cell_cap;
+    int32_t w;
+    int32_t h;
+} dem_grid_info;
+
+/* Extensions.  Zero-initialise, then set bond_lambda = 0.5f and
+ * diagnostics = 1 for exact reference behaviour (dem_ext_defaults). */
+typedef struct dem_ext {
+    int32_t use_f64;                  /* F64 distance branch (2D_Simulation.wgsl:264-284; shader_gen.rs:84) */
+    float bond_lambda;                /* parallel-bond radius factor; reference 0.5 (2D_Simulation.wgsl:290) */
+    const float *bond_normal_strength;/* optional per-bond strengths [n_bonds]; NULL = global setting */
+    const float *bond_shear_strength;
+    int32_t diagnostics;              /* 1: maintain data[7n] every step as the reference does */
+    int32_t reorder_interval;         /* steps between particle reorders by cell; 0 = library default */
+    int32_t block_size;               /* threads per block for particle kernels; 0 = default */
+    float search_cell_factor;         /* search-grid cell / (2 r_max); 0 = default 1.0 (minimum) */
+    int32_t event_capacity;           /* break-event ring size; 0 = default */
+    int32_t reserved[7];
+} dem_ext;
+
+/* One scene in the reference's host layouts (state.rs:69-93).  Arrays hold
+ * n_particles entries (times the per-particle width). */
+typedef struct dem_scene {
+    int32_t n_particles;       /* p_count */
+    int32_t n_bonds;           /* bond records (bonds holds 3*n_bonds words) */
+    int32_t n_materials;       /* material records (materials holds 6*n_materials floats) */
+    float *pos;                /* [2n] */
+    float *radii;              /* [n] */
+    float *vel;                /* [2n] */
+    float *acc;                /* [2n]  binding 1 of group 1, "accelerations" */
+    float *rot;                /* [n] */
+    float *rot_vel;            /* [n] */
+    float *rot_acc;            /* [n] */
+    float *forces;             /* [6n]  {x, y, rot, delX, delY, delRot} */
+    int32_t *fixity;           /* [6n]  {x_vel, y_vel, rot_vel, x_vel_2, y_vel_2, rot_vel_2} */
+    float *del_pos;            /* [2n] */
+    float *del_rot;            /* [n] */
+    int32_t *bonds;            /* [3*n_bonds] {index, angle bits, length bits} */
+    int32_t *contacts;         /* [6*14*n] {a, b, tangent_force, bond_tangent_force, theta_b, bonded} bits */
+    int32_t *material_pointers;/* [n] */
+    float *materials;          /* [6*n_materials] {red, green, blue, density, normal_stiffness, shear_stiffness} */
+    float *data;               /* [7n] or NULL */
+    int32_t coll_cont[4];      /* {detect flag, interval counter, tick, positions-set flag} */
+    dem_grid_info grid;
+} dem_scene;
+
+/* One bond break, in evaluation order of the step that produced it. */
+typedef struct dem_break_event {
+    int32_t scene;   /* scene index within a batch (0 for a single-scene context) */
+    int32_t step;    /* step counter value of the step that broke the bond */
+    int32_t bond;    /* bond record index within the scene */
+    int32_t code;    /* -10 + sign(normal displacement) (2D_Simulation.wgsl:323, 403, 426) */
+    int32_t a;       /* particle evaluating the break */
+    int32_t b;       /* its partner */
+} dem_break_event;
+
+typedef struct dem_stats {
+    int64_t steps;              /* steps executed */
+    int64_t capped;             /* narrow phases that reached 14 contacts */
+    int64_t events;             /* bond breaks recorded */
+    int64_t events_dropped;     /* breaks beyond the event ring */
+    int64_t reorders;           /* particle reorders performed */
+    int32_t device_error;       /* sticky device error bits, 0 = none */
+    int32_t reserved;
+} dem_stats;
+
+typedef struct dem_ctx dem_ctx;
+
+int dem_abi_version(void);
+void dem_ext_defaults(dem_ext *ext);
+/* Last error message of ctx, or of the calling thread's last failed create when ctx is NULL. */
+const char *dem_last_error(const dem_ctx *ctx);
+
+/* grid_capacity (wgpu_prog.rs:698-717) over the given radii (State::load
+ * takes min/max over the whole radii vector, state.rs:684-698). */
+int dem_grid_capacity(const dem_params *p, const float *radii, int32_t n_radii, int32_t particles,
+                      dem_grid_info *out);
+
+/* WGPUComputeProg::new + restore: copy a scene to the device.  device < 0
+ * keeps the current CUDA device. */
+int dem_create(const dem_scene *scene, const dem_params *params, const dem_ext *ext, int device,
+               dem_ctx **out);
+void dem_destroy(dem_ctx *ctx);
+
+/* WGPUComputeProg::restore (wgpu_prog.rs:1235-1262): replace the whole state.
+ * The control words coll_cont persist across restore, as the device buffer does
+ * in the reference; scene->coll_cont is ignored here (see dem_set_control). */
+int dem_upload(dem_ctx *ctx, const dem_scene *scene);
+/* Uniform::updateUniform of the settings (client.rs:1128-1135). */
+int dem_set_params(dem_ctx *ctx, const dem_params *params);
+/* Material buffer update (6 floats per material). */
+int dem_set_materials(dem_ctx *ctx, const float *materials, int32_t n_materials);
+int dem_set_control(dem_ctx *ctx, const int32_t coll_cont[4]);
+int dem_get_control(dem_ctx *ctx, int32_t coll_cont[4]);
+
+/* WGPUComputeProg::compute: enqueue n_steps of LOM + Simulation on the
+ * context's stream and return without waiting, like queue.submit. */
+int dem_step(dem_ctx *ctx, int32_t n_steps);
+int dem_synchronize(dem_ctx *ctx);
+
+/* State::update_state (state.rs:264-289): synchronous copy of the whole state
+ * into caller-owned arrays of `out` (NULL arrays are skipped). */
+int dem_download(dem_ctx *ctx, dem_scene *out);
+
+/* Set_Properties event (Set_Properties.wgsl:68-90): props are the 28 words of
+ * Settings::properties; selections [n] is read, and written back with 2 where
+ * a fixity was set (Set_Properties.wgsl:87-89). */
+int dem_set_properties(dem_ctx *ctx, int32_t *selections, const int32_t props[DEM_PROPS_WORDS]);
+
+/* Drain up to cap break events (oldest first); *n receives the count copied. */
+int dem_break_events(dem_ctx *ctx, dem_break_event *buf, int32_t cap, int32_t *n);
+int dem_get_stats(dem_ctx *ctx, dem_stats *out);
+
+/* The CUDA stream the context enqueues on (a cudaStream_t), for callers that
+ * order their own work against the steps. */
+void *dem_stream(dem_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

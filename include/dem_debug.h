@@ -1,0 +1,33 @@
+/*
+ * dem_debug.h -- introspection entry points of libdemgb.so used by the parity
+ * tests.  They have no counterpart in the reference's compute dispatch: they
+ * expose the broad phase's intermediate tables so that cell keys and the
+ * sorted order can be checked bit for bit.
+ */
+#ifndef DEM_DEBUG_H
+#define DEM_DEBUG_H
+#include <stdint.h>
+
+#include "dem.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Run the broad phase on the current positions (no integration) and return,
+ * per scene-local particle, its search-cell key; the particle indices in
+ * stable cell order; the cell start table (n_cells + 1 entries).  Any pointer
+ * may be NULL; *n_cells receives the scene's cell count (incl. its cell for
+ * zero-radius particles). */
+int dem_debug_broad_phase(dem_ctx *ctx, int32_t *keys, int32_t *order, int32_t *cell_start,
+                          int32_t *n_cells);
+
+/* Geometry of the search grid: cell (cx, cy) of a position is
+ * floor((x - x0) * inv), floor((y - y0) * inv) clamped to [0, gw-1] x [0, gh-1];
+ * key = cy * gw + cx. */
+int dem_debug_search_grid(dem_ctx *ctx, float *x0, float *y0, float *inv, int32_t *gw, int32_t *gh);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,811 @@
+// dem_kernels.cu -- sm_103a kernels of one DEM step.
+//
+// Step = integrate (LOM) -> broad phase (keys, counting sort, cell tables,
+// in-cell ordering, periodic reorder) -> interact (narrow phase, contact
+// slots, forces, half kick) -> end of step (apply bond breaks).
+//
+// Arithmetic follows the reference's WGSL expression by expression
+// (src/shaders/physics/2D_LOM.wgsl, 2D_Simulation.wgsl).  This file is
+// compiled with -fmad=false: no multiply-add is contracted, '/' and sqrtf are
+// IEEE round-to-nearest, so every float result is the one the expression
+// denotes, identical to a CPU evaluating the same expression.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dem_world.cuh"
+
+namespace demgb {
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ float len2f(float x, float y) { return sqrtf(x * x + y * y); }
+
+// cell range of the particle's AABB in the reference grid (2D_LOM.wgsl:167-178);
+// i32() is truncation toward zero, saturating (cvt.rzi).
+__device__ __forceinline__ void ref_range(const ScenePar &P, float px, float py, float r, int &x0,
+                                          int &x1, int &y0, int &y1) {
+    float left = px - r, right = px + r, bottom = py - r, top = py + r;
+    int a = __float2int_rz((left - P.ref_base_x) / P.ref_cs);
+    int b = __float2int_rz((right - P.ref_base_x) / P.ref_cs);
+    int c = __float2int_rz((P.ref_base_y - top) / P.ref_cs);
+    int d = __float2int_rz((P.ref_base_y - bottom) / P.ref_cs);
+    x0 = a > 0 ? a : 0;
+    x1 = b < P.ref_w - 1 ? b : P.ref_w - 1;
+    y0 = c > 0 ? c : 0;
+    y1 = d < P.ref_h - 1 ? d : P.ref_h - 1;
+}
+
+// search-grid cell of a position (floor, clamped to the grid)
+__device__ __forceinline__ void search_xy(const ScenePar &P, float x, float y, int &cx, int &cy) {
+    int a = __float2int_rd((x - P.g_x0) * P.g_inv);
+    int b = __float2int_rd((y - P.g_y0) * P.g_inv);
+    cx = a < 0 ? 0 : (a > P.g_w - 1 ? P.g_w - 1 : a);
+    cy = b < 0 ? 0 : (b > P.g_h - 1 ? P.g_h - 1 : b);
+}
+
+struct F3 {
+    float x, y, z;
+};
+
+// distance2 (2D_Simulation.wgsl:273-284): |pa-pb| - length, F64 branch optional
+__device__ __forceinline__ float distance2(int use_f64, float4 pa, float4 pb, float length) {
+    if (use_f64) {
+        double dx = (double)pa.x - (double)pb.x, dy = (double)pa.y - (double)pb.y;
+        return (float)(sqrt(dx * dx + dy * dy) - (double)length);
+    }
+    float dx = pa.x - pb.x, dy = pa.y - pb.y;
+    return len2f(dx, dy) - length;
+}
+// distance (2D_Simulation.wgsl:264-271): the F64 branch sums the radii in double
+__device__ __forceinline__ float distance1(int use_f64, float4 pa, float4 pb) {
+    if (use_f64) {
+        double dx = (double)pa.x - (double)pb.x, dy = (double)pa.y - (double)pb.y;
+        return (float)(sqrt(dx * dx + dy * dy) - ((double)pa.z + (double)pb.z));
+    }
+    float dx = pa.x - pb.x, dy = pa.y - pb.y;
+    return len2f(dx, dy) - (pa.z + pb.z);
+}
+
+struct Acc3 {
+    float d0, d1, d2;
+};
+
+// linear_model (2D_Simulation.wgsl:338-373)
+__device__ __forceinline__ F3 linear_model(const ScenePar &P, const Mat &A, const Mat &B, float4 pa,
+                                           float4 da, float4 pb, float4 db, float length, float &tf,
+                                           Acc3 &acc) {
+    F3 out = {0.0f, 0.0f, 0.0f};
+    float d2 = distance2(P.use_f64, pa, pb, length);
+    float nd = d2 < 0.0f ? d2 : 0.0f;
+    if (nd == 0.0f) return out;
+    float kn = 1.0f / (1.0f / A.kn + 1.0f / B.kn);
+    float ks = 1.0f / (1.0f / A.ks + 1.0f / B.ks);
+    float Fn = (-nd) * kn;
+    float vx = pa.x - pb.x, vy = pa.y - pb.y;
+    float L = len2f(vx, vy);
+    float nx = vx / L, ny = vy / L;
+    float tx = -ny, ty = nx;
+    float dra = da.z * pa.z;
+    float drb = db.z * pb.z;
+    float rx = db.x - da.x, ry = db.y - da.y;
+    float rr = drb + dra;
+    float rt = (rx * tx + ry * ty) + rr;
+    float fl = (Fn < 0.0f ? -Fn : Fn) * P.p.friction_coefficient;
+    float t = tf + rt * ks;
+    t = t > -fl ? t : -fl;
+    t = t < fl ? t : fl;
+    tf = t;
+    float M = (-pa.z) * tf;
+    out.x = nx * Fn + tx * tf;
+    out.y = ny * Fn + ty * tf;
+    out.z = M;
+    acc.d0 = acc.d0 + Fn;
+    acc.d1 = acc.d1 + tf;
+    acc.d2 = acc.d2 + M;
+    return out;
+}
+
+__device__ __forceinline__ int sign_i32(float x) { return x > 0.0f ? 1 : (x < 0.0f ? -1 : 0); }
+
+__device__ __forceinline__ void record_break(const DevWorld &w, const ScenePar &P, int scene,
+                                             long long step, int bond_global, int code, int a_int,
+                                             int b_int) {
+    uint32_t p = atomicAdd(w.pend_count, 1u);
+    if (p < w.pend_cap) {
+        w.pend[p].bond = bond_global;
+        w.pend[p].code = code;
+    } else {
+        atomicAdd(&w.stats[3], 1ull);
+    }
+    unsigned long long e = atomicAdd(w.ev_count, 1ull);
+    if (e < w.ev_cap) {
+        Event ev;
+        ev.scene = scene;
+        ev.step = (int32_t)step;
+        ev.bond = bond_global - P.bond_base;
+        ev.code = code;
+        ev.a = w.orig[a_int];
+        ev.b = w.orig[b_int];
+        w.ev[e] = ev;
+    } else {
+        atomicAdd(&w.stats[2], 1ull);
+    }
+    atomicAdd(&w.stats[1], 1ull);
+}
+
+// ------------------------------------------------------------ LOM kernel
+// 2D_LOM.wgsl:80-152 per particle; then the particle's search-cell key and
+// the histogram count for the counting sort (replaces the atomic bucket
+// insertion of 2D_LOM.wgsl:165-199).
+__global__ void __launch_bounds__(256) k_lom(DevWorld w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.N) return;
+    uint32_t m = w.meta[i];
+    int s = (int)meta_scene(m);
+    const ScenePar &P = w.par[s];
+    float4 p = w.pr[i];
+    if (!P.active) return;
+    if (p.z == 0.0f) {                                            // :83
+        w.keys[i] = (uint32_t)P.dead_cell;
+        atomicAdd(&w.cell_count[P.dead_cell], 1);
+        return;
+    }
+    const float dT = P.p.dT;
+    float4 v = w.vw[i];
+    float4 a = w.ac[i];
+    float ivx = v.x, ivy = v.y, iw = v.z;
+    if (m & M_KICK_X) ivx = ivx + (a.x * dT) * 0.5f;               // :88
+    if (m & M_KICK_Y) ivy = ivy + (a.y * dT) * 0.5f;               // :89
+    if (m & M_KICK_R) iw = iw + (a.z * dT) * 0.5f;                 // :90
+    w.d4[i] = make_float4(ivx, ivy, iw, 0.0f);                     // :92-94
+    float4 d;
+    bool ext = w.cc3[s] != 0;
+    if (!ext) {                                                    // :96-99
+        d = make_float4(ivx * dT, ivy * dT, iw * dT, 0.0f);
+    } else {
+        d = w.dp[i];
+    }
+    float r = p.z;
+    float npx = p.x + d.x, npy = p.y + d.y;                        // :103
+    if (P.p.round_bounds == 0) {                                   // :104-129
+        float yH = P.yH, xW = P.xW;
+        if (!(m & M_FIX_Y)) {
+            if (npy - r < -yH) {
+                ivy = (-ivy) * 0.5f;
+                p.y = p.y + ((-yH) - (npy - r));
+            } else if (npy + r > yH) {
+                ivy = (-ivy) * 0.5f;
+                p.y = p.y - ((npy + r) - yH);
+            }
+        }
+        if (!(m & M_FIX_X)) {
+            if (npx - r < -xW) {
+                ivx = (-ivx) * 0.5f;
+                p.x = p.x + ((-xW) - (npx - r));
+            } else if (npx + r > xW) {
+                ivx = (-ivx) * 0.5f;
+                p.x = p.x - ((npx + r) - xW);
+            }
+        }
+    } else if (len2f(npx, npy) + r > P.p.bound_radius) {          // :130-145
+        float L = len2f(npx, npy);
+        float nx = npx / L, ny = npy / L;
+        float dd = d.x * nx + d.y * ny;
+        float dcx = dd * nx, dcy = dd * ny;
+        float vv = ivx * nx + ivy * ny;
+        float cvx = vv * nx, cvy = vv * ny;
+        float Rb = P.p.bound_radius;
+        if (!(m & M_FIX_X)) {
+            p.x = (nx * (Rb - r)) - dcx;
+            ivx = (-cvx) * 0.5f;
+        }
+        if (!(m & M_FIX_Y)) {
+            p.y = (ny * (Rb - r)) - dcy;
+            ivy = (-cvy) * 0.5f;
+        }
+    }
+    p.x = p.x + d.x;                                               // :148
+    p.y = p.y + d.y;
+    p.w = p.w + d.z;                                               // :149
+    w.pr[i] = p;
+    w.vw[i] = make_float4(ivx, ivy, iw, v.w);                      // :151-152
+    if (!ext) w.dp[i] = d;
+    int cx, cy;
+    search_xy(P, p.x, p.y, cx, cy);
+    uint32_t key = (uint32_t)(P.cell_base + cy * P.g_w + cx);
+    w.keys[i] = key;
+    atomicAdd(&w.cell_count[key], 1);
+}
+
+// keys of the current positions without integrating (standalone broad phase,
+// the role of the unused 2D_Broad_Phase.wgsl:78-111)
+__global__ void __launch_bounds__(256) k_keys(DevWorld w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.N) return;
+    uint32_t m = w.meta[i];
+    const ScenePar &P = w.par[meta_scene(m)];
+    if (!P.active) return;
+    float4 p = w.pr[i];
+    uint32_t key;
+    if (p.z == 0.0f) {
+        key = (uint32_t)P.dead_cell;
+    } else {
+        int cx, cy;
+        search_xy(P, p.x, p.y, cx, cy);
+        key = (uint32_t)(P.cell_base + cy * P.g_w + cx);
+    }
+    w.keys[i] = key;
+    atomicAdd(&w.cell_count[key], 1);
+}
+
+void launch_keys(const DevWorld &w, int block, cudaStream_t st) {
+    if (w.N == 0) return;
+    k_keys<<<(w.N + block - 1) / block, block, 0, st>>>(w);
+}
+
+void launch_lom(const DevWorld &w, int block, cudaStream_t st) {
+    if (w.N == 0) return;
+    k_lom<<<(w.N + block - 1) / block, block, 0, st>>>(w);
+}
+
+// ---------------------------------------------------------- broad phase
+// Exclusive scan of the per-cell counts with warp-shuffle scans: each block
+// scans SCAN_TILE counts, a single block scans the tile sums, a third pass
+// adds the tile offsets.
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_PER_THREAD = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER_THREAD;
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+    int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// block-wide exclusive scan of one value per thread; returns the block total in *total
+__device__ __forceinline__ int block_excl_scan(int v, int *total) {
+    __shared__ int wsum[SCAN_THREADS / 32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int inc = warp_incl_scan(v);
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int x = lane < SCAN_THREADS / 32 ? wsum[lane] : 0;
+        int y = warp_incl_scan(x);
+        if (lane < SCAN_THREADS / 32) wsum[lane] = y - x;
+        if (lane == SCAN_THREADS / 32 - 1) *total = y;
+    }
+    __syncthreads();
+    int r = inc - v + wsum[wid];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(const int32_t *__restrict__ in,
+                                                             int32_t *__restrict__ out, int n,
+                                                             int32_t *__restrict__ tile_sums) {
+    __shared__ int total;
+    int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+    int v[SCAN_PER_THREAD];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+        int idx = base + k;
+        v[k] = idx < n ? in[idx] : 0;
+        sum += v[k];
+    }
+    int off = block_excl_scan(sum, &total);
+#pragma unroll
+    for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+        int idx = base + k;
+        if (idx < n) out[idx] = off;
+        off += v[k];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// single block: exclusive scan of the tile sums in place; writes the grand total to out[n]
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(int32_t *tile_sums, int ntiles,
+                                                            int32_t *out, int n) {
+    __shared__ int total;
+    int carry = 0;
+    for (int base = 0; base < ntiles; base += SCAN_THREADS) {
+        int idx = base + threadIdx.x;
+        int v = idx < ntiles ? tile_sums[idx] : 0;
+        int off = block_excl_scan(v, &total);
+        if (idx < ntiles) tile_sums[idx] = carry + off;
+        carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_add(int32_t *out, int n,
+                                                           const int32_t *tile_sums) {
+    int add = tile_sums[blockIdx.x];
+    int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+        int idx = base + k;
+        if (idx < n) out[idx] += add;
+    }
+}
+
+int scan_tmp_size(int n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
+
+// scatter: slot = start + (count-1) taken by an atomic decrement, which also
+// returns every count to zero for the next step's histogram
+__global__ void __launch_bounds__(256) k_scatter(DevWorld w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.N) return;
+    uint32_t m = w.meta[i];
+    if (!w.par[meta_scene(m)].active) return;
+    uint32_t key = w.keys[i];
+    int slot = w.cell_start[key] + atomicSub(&w.cell_count[key], 1) - 1;
+    w.sorted[slot] = i;
+}
+
+// in-cell ordering: each cell's members sorted by scene-local particle index,
+// so the cell lists equal a stable sort of the particles by cell key
+__global__ void __launch_bounds__(256) k_cell_order(DevWorld w) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= w.C) return;
+    int beg = w.cell_start[c], end = w.cell_start[c + 1];
+    if (end - beg < 2) return;
+    for (int a = beg + 1; a < end; ++a) {
+        int v = w.sorted[a];
+        int ov = w.orig[v];
+        int b = a - 1;
+        while (b >= beg) {
+            int u = w.sorted[b];
+            if (w.orig[u] <= ov) break;
+            w.sorted[b + 1] = u;
+            --b;
+        }
+        w.sorted[b + 1] = v;
+    }
+}
+
+int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st) {
+    if (w.N == 0) return 0;
+    int ntiles = (w.C + SCAN_TILE - 1) / SCAN_TILE;
+    k_scan_tiles<<<ntiles, SCAN_THREADS, 0, st>>>(w.cell_count, w.cell_start, w.C, w.scan_tmp);
+    k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(w.scan_tmp, ntiles, w.cell_start, w.C);
+    k_scan_add<<<ntiles, SCAN_THREADS, 0, st>>>(w.cell_start, w.C, w.scan_tmp);
+    k_scatter<<<(w.N + block - 1) / block, block, 0, st>>>(w);
+    k_cell_order<<<(w.C + 255) / 256, 256, 0, st>>>(w);
+    return 0;
+}
+
+// --------------------------------------------------------------- reorder
+// Permute every per-particle array into cell order (new i <- old sorted[i])
+// and remap partner indices; the cell lists become the identity.
+__global__ void __launch_bounds__(256) k_inverse(DevWorld w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.N) return;
+    w.inv[w.sorted[i]] = i;
+}
+
+__global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.N) return;
+    int src = w.sorted[i];
+    o.pr[i] = w.pr[src];
+    o.vw[i] = w.vw[src];
+    o.ac[i] = w.ac[src];
+    o.dp[i] = w.dp[src];
+    o.fx[i] = w.fx[src];
+    o.d4[i] = w.d4[src];
+    o.dF[i] = w.dF[src];
+    o.meta[i] = w.meta[src];
+    o.orig[i] = w.orig[src];
+    o.smask[i] = w.smask[src];
+    const int N = w.N;
+#pragma unroll 2
+    for (int j = 0; j < K; ++j) {
+        int b = w.s_b[j * N + src];
+        o.s_b[j * N + i] = (b >= 0 && b < N) ? w.inv[b] : b;
+        o.s_bonded[j * N + i] = w.s_bonded[j * N + src];
+        o.s_tf[j * N + i] = w.s_tf[j * N + src];
+        o.s_btf[j * N + i] = w.s_btf[j * N + src];
+        o.s_thb[j * N + i] = w.s_thb[j * N + src];
+    }
+    w.sorted[i] = i;  // safe: every thread read its own sorted[i] above; inv is read for b
+}
+
+void launch_reorder(DevWorld &w, DevWorld &spare, int block, cudaStream_t st) {
+    if (w.N == 0) return;
+    int g = (w.N + block - 1) / block;
+    k_inverse<<<g, block, 0, st>>>(w);
+    k_gather<<<g, block, 0, st>>>(w, spare);
+}
+
+// -------------------------------------------------------------- interact
+// 2D_Simulation.wgsl:108-262 per particle.
+//
+// Narrow phase: the reference accepts partner b when b's AABB shares a bucket
+// with the particle's AABB (both inserted into every bucket their AABB covers,
+// 2D_LOM.wgsl:180-199) and |p_b - p_a| < r_b + r_a; it stops at 14 and keeps
+// them in bucket-scan order (rows top to bottom, columns left to right,
+// bucket members in insertion order).  Here candidates come from the 3x3
+// search cells around the particle, the same acceptance test is evaluated
+// exactly, and accepted partners are ordered by (first shared bucket in scan
+// order, particle index) -- the bucket-scan order with insertion in index
+// order -- keeping the first 14.
+__device__ __forceinline__ void top14_insert(unsigned long long key, int idx, unsigned long long *ck,
+                                             int *ci, int &cnt) {
+    if (cnt == K && key >= ck[K - 1]) return;
+    int pos = cnt < K ? cnt : K - 1;
+    while (pos > 0 && ck[pos - 1] > key) {
+        ck[pos] = ck[pos - 1];
+        ci[pos] = ci[pos - 1];
+        --pos;
+    }
+    ck[pos] = key;
+    ci[pos] = idx;
+    if (cnt < K) ++cnt;
+}
+
+__global__ void __launch_bounds__(128) k_interact(DevWorld w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.N) return;
+    const uint32_t m = w.meta[i];
+    const int s = (int)meta_scene(m);
+    const ScenePar &P = w.par[s];
+    if (!P.active) return;
+    const float4 pa = w.pr[i];
+    if (pa.z == 0.0f) {                                            // :113-118
+        w.dF[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    const long long step = *w.step;
+    const int N = w.N;
+    const float4 da = w.dp[i];
+    const Mat MA = w.mats[P.mat_base + meta_mat(m)];
+    uint32_t mask = w.smask[i];
+    int sb[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) sb[j] = (mask >> j) & 1u ? w.s_b[j * N + i] : -1;
+
+    const bool detect = P.p.collisions == 1 &&
+                        detect_at(P.p.collision_interval, P.cc1_0, step - P.step0);
+    if (detect) {                                                  // :126-228
+        unsigned long long ck[K];
+        int ci[K];
+        int cnt = 0;
+        int ax0, ax1, ay0, ay1;
+        ref_range(P, pa.x, pa.y, pa.z, ax0, ax1, ay0, ay1);
+        const int awidth = ax1 - ax0 + 1;
+        int gx, gy;
+        search_xy(P, pa.x, pa.y, gx, gy);
+        const int R = P.stencil;
+        const int cy0 = max(gy - R, 0), cy1 = min(gy + R, P.g_h - 1);
+        const int cx0 = max(gx - R, 0), cx1 = min(gx + R, P.g_w - 1);
+        for (int cy = cy0; cy <= cy1; ++cy) {
+            const int row = P.cell_base + cy * P.g_w;
+            const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
+            for (int k = beg; k < end; ++k) {
+                const int b = w.sorted[k];
+                if (b == i) continue;
+                const float4 pb = w.pr[b];
+                const float dx = pb.x - pa.x, dy = pb.y - pa.y;
+                if (!(len2f(dx, dy) < pb.z + pa.z)) continue;      // :159
+                int bx0, bx1, by0, by1;
+                ref_range(P, pb.x, pb.y, pb.z, bx0, bx1, by0, by1);
+                if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) continue;
+                const int fy = by0 > ay0 ? by0 : ay0;
+                const int fx = bx0 > ax0 ? bx0 : ax0;
+                const unsigned rank = (unsigned)((fy - ay0) * awidth + (fx - ax0));
+                const unsigned long long key =
+                    ((unsigned long long)rank << 32) | (unsigned)w.orig[b];
+                        top14_insert(key, b, ck, ci, cnt);
+            }
+        }
+        if (cnt == K) atomicAdd(&w.stats[0], 1ull);
+        // delete contacts that were not found (:185-204)
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            if (sb[j] == -1) continue;
+            bool found = false;
+            for (int q = 0; q < cnt; ++q) found |= (ci[q] == sb[j]);
+            if (found) continue;
+            const int bonded = w.s_bonded[j * N + i];
+            if (bonded < 0 || P.p.bonds == 0) {
+                sb[j] = -1;
+                mask &= ~(1u << j);
+            } else if (bonded > 0 && P.p.bonds <= 1) {
+                w.s_tf[j * N + i] = 0.0f;
+            }
+        }
+        // create new contacts in the last empty slot (:207-227)
+        for (int q = 0; q < cnt; ++q) {
+            const int c = ci[q];
+            bool existing = false;
+#pragma unroll
+            for (int j = 0; j < K; ++j) existing |= (sb[j] == c);
+            if (existing) continue;
+            const uint32_t empty = (~mask) & ((1u << K) - 1u);
+            if (empty == 0u) continue;
+            const int j = 31 - __clz(empty);
+            mask |= 1u << j;
+#pragma unroll
+            for (int jj = 0; jj < K; ++jj)
+                if (jj == j) sb[jj] = c;
+            w.s_b[j * N + i] = c;
+            w.s_tf[j * N + i] = 0.0f;
+        }
+        w.smask[i] = mask;
+    }
+
+    // force loop (:230-255)
+    float nfx = 0.0f, nfy = 0.0f, nm = 0.0f;
+    Acc3 acc = {0.0f, 0.0f, 0.0f};
+    const int bonds_model = P.p.bonds;
+#pragma unroll 1
+    for (int j = 0; j < K; ++j) {
+        const int b = sb[j];
+        if (b == -1) continue;
+        int bonded = w.s_bonded[j * N + i];
+        if (bonded >= 0) {
+            const int st = w.b_status[P.bond_base + bonded];
+            if (st < 0) {                                          // :236-239
+                w.s_bonded[j * N + i] = st;
+                bonded = st;
+            }
+        }
+        const float4 pb = w.pr[b];
+        const float4 db = w.dp[b];
+        const Mat MB = w.mats[P.mat_base + meta_mat(w.meta[b])];
+        F3 f = {0.0f, 0.0f, 0.0f};
+        if (bonded < 0 || bonds_model == 0) {
+            float tf = w.s_tf[j * N + i];
+            f = linear_model(P, MA, MB, pa, da, pb, db, pa.z + pb.z, tf, acc);
+            w.s_tf[j * N + i] = tf;
+        } else {
+            const int bg = P.bond_base + bonded;
+            const float blen = w.b_length[bg];
+            float sn = P.p.bond_normal_strength, ss = P.p.bond_shear_strength;
+            if (P.has_strength) {
+                const float2 str = w.b_str[bg];
+                sn = str.x;
+                ss = str.y;
+            }
+            if (bonds_model == 3) {                                // :286-336
+                const float kn = P.p.bond_normal_stiffness, ks = P.p.bond_shear_stiffness;
+                const float Rr = P.lambda * (pa.z < pb.z ? pa.z : pb.z);
+                const float A = (2.0f * Rr) * 1.0f;
+                const float I = ((2.0f / 3.0f * Rr) * Rr) * Rr;
+                const float nd = distance2(P.use_f64, pa, pb, blen);
+                float Fn = ((-kn) * nd) * A;
+                const float vx = pa.x - pb.x, vy = pa.y - pb.y;
+                const float L = len2f(vx, vy);
+                const float nx = vx / L, ny = vy / L;
+                const float tx = -ny, ty = nx;
+                const float dra = da.z * pa.z, drb = db.z * pb.z;
+                const float rx = db.x - da.x, ry = db.y - da.y;
+                const float rr = drb + dra;
+                const float rt = (rx * tx + ry * ty) + rr;
+                float btf = w.s_btf[j * N + i];
+                float thb = w.s_thb[j * N + i];
+                btf = btf + (rt * ks) * A;
+                const float dtb = da.z - db.z;
+                thb = thb + dtb;
+                float M = (((-kn) * I) * thb) - btf * pa.z;
+                float Fx = nx * Fn + tx * btf;
+                float Fy = ny * Fn + ty * btf;
+                float bend = ((-kn) * I) * thb;
+                bend = bend < 0.0f ? -bend : bend;
+                const float abtf = btf < 0.0f ? -btf : btf;
+                if (P.p.bonds_tear == 1 &&
+                    ((Fn / A) - (P.p.moment_contribution_factor * (bend * Rr)) / I < -sn ||
+                     abtf / A > ss)) {
+                    const int code = -10 + sign_i32(nd);
+                    record_break(w, P, s, step, bg, code, i, b);
+                    w.s_bonded[j * N + i] = code;
+                    Fn = 0.0f;
+                    btf = 0.0f;
+                    Fx = 0.0f;
+                    Fy = 0.0f;
+                    M = 0.0f;
+                }
+                w.s_btf[j * N + i] = btf;
+                w.s_thb[j * N + i] = thb;
+                acc.d0 = acc.d0 + (-Fn);
+                acc.d1 = acc.d1 + btf;
+                acc.d2 = acc.d2 + M;
+                float tf = w.s_tf[j * N + i];
+                const F3 lm = linear_model(P, MA, MB, pa, da, pb, db, blen, tf, acc);
+                w.s_tf[j * N + i] = tf;
+                f.x = Fx + lm.x;
+                f.y = Fy + lm.y;
+                f.z = M + lm.z;
+            } else if (bonds_model == 1) {                         // :419-432
+                const float disp = distance1(P.use_f64, pa, pb);
+                float fx = 0.0f, fy = 0.0f;
+                const float sf = P.p.bond_normal_stiffness * disp;
+                const float vx = pb.x - pa.x, vy = pb.y - pa.y;
+                const float L = len2f(vx, vy);
+                fx = fx + sf * (vx / L);
+                fy = fy + sf * (vy / L);
+                if (P.p.bonds_tear == 1 && sf >= sn) {
+                    const int code = -10 + sign_i32(disp);
+                    record_break(w, P, s, step, bg, code, i, b);
+                    w.s_bonded[j * N + i] = code;
+                    fx = 0.0f;
+                    fy = 0.0f;
+                }
+                float tf = w.s_tf[j * N + i];
+                const F3 lm = linear_model(P, MA, MB, pa, da, pb, db, blen, tf, acc);
+                w.s_tf[j * N + i] = tf;
+                f.x = lm.x + fx;
+                f.y = lm.y + fy;
+                f.z = lm.z + 0.0f;
+            } else if (bonds_model == 2) {                         // :375-417
+                const float nd = distance1(P.use_f64, pa, pb);
+                const float kb = P.p.bond_normal_stiffness, ksb = P.p.bond_shear_stiffness;
+                const float kn = 1.0f / (1.0f / kb + 1.0f / kb);
+                const float ks = 1.0f / (1.0f / ksb + 1.0f / ksb);
+                float Fn = (-nd) * kn;
+                const float vx = pa.x - pb.x, vy = pa.y - pb.y;
+                const float L = len2f(vx, vy);
+                const float nx = vx / L, ny = vy / L;
+                const float tx = -ny, ty = nx;
+                const float dra = da.z * pa.z, drb = db.z * pb.z;
+                const float rx = db.x - da.x, ry = db.y - da.y;
+                const float rr = drb + dra;
+                const float rt = (rx * tx + ry * ty) + rr;
+                float tf = w.s_tf[j * N + i];
+                tf = tf + rt * ks;
+                const float cd = P.p.contact_damping;
+                float Fx = cd * (nx * Fn + tx * tf);
+                float Fy = cd * (ny * Fn + ty * tf);
+                float M = (-pa.z) * tf;
+                const float atf = tf < 0.0f ? -tf : tf;
+                if (P.p.bonds_tear == 1 && (Fn < -sn || atf > ss)) {
+                    const int code = -10 + sign_i32(nd);
+                    record_break(w, P, s, step, bg, code, i, b);
+                    w.s_bonded[j * N + i] = code;
+                    Fn = 0.0f;
+                    w.s_btf[j * N + i] = 0.0f;
+                    Fx = 0.0f;
+                    Fy = 0.0f;
+                    M = 0.0f;
+                }
+                w.s_tf[j * N + i] = tf;
+                acc.d0 = -Fn;
+                acc.d1 = tf;
+                acc.d2 = M;
+                f.x = Fx;
+                f.y = Fy;
+                f.z = M;
+            }
+        }
+        nfx = nfx + f.x;
+        nfy = nfy + f.y;
+        nm = nm + f.z;
+    }
+
+    // store_forces (:434-478)
+    const float r = pa.z;
+    const float mass = ((MA.density * 3.14159274101257324219f) * r) * r;
+    const float rot_inertia = ((0.5f * mass) * r) * r;
+    float4 fe = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (m & M_FEXT) fe = w.fx[i];
+    float fxs = nfx + fe.x;
+    float fys = nfy + fe.y;
+    float moment = nm + fe.z;
+    if (P.p.gravity == 1 && P.p.planet_mode == 1) {
+        float cx = 0.0f, cy = 0.0f;
+        if (P.p.mouse_gravity == 1) {
+            cx = P.p.gravity_x;
+            cy = P.p.gravity_y;
+        }
+        const float dx = cx - pa.x, dy = cy - pa.y;
+        if (dx != 0.0f || dy != 0.0f) {
+            const float L = len2f(dx, dy);
+            fxs = fxs + (((dx / L) * 9.81f) * P.p.gravity_acc) * mass;
+            fys = fys + (((dy / L) * 9.81f) * P.p.gravity_acc) * mass;
+        }
+    } else if (P.p.gravity == 1) {
+        const float ga = 9.81f * P.p.gravity_acc;
+        fxs = fxs + 0.0f;
+        fys = fys + (-ga) * mass;
+    }
+    const float ax = fxs / mass, ay = fys / mass;
+    const float al = moment / rot_inertia;
+    w.ac[i] = make_float4(ax, ay, al, 0.0f);
+    float4 v = w.vw[i];
+    const float dT = P.p.dT;
+    if (m & M_KICK_X) v.x = v.x + (0.5f * ax) * dT;
+    if (m & M_KICK_Y) v.y = v.y + (0.5f * ay) * dT;
+    if (m & M_KICK_R) v.z = v.z + (0.5f * al) * dT;
+    w.vw[i] = v;
+    w.dF[i] = make_float4(acc.d0, acc.d1, acc.d2, 0.0f);
+}
+
+void launch_interact(const DevWorld &w, int block, cudaStream_t st) {
+    if (w.N == 0) return;
+    (void)block;
+    k_interact<<<(w.N + 127) / 128, 128, 0, st>>>(w);
+}
+
+// ------------------------------------------------------------ end of step
+// Breaks of this step become visible (status = min code), the positions-set
+// flags clear (2D_Simulation.wgsl:258-261), the step counter advances.
+__global__ void __launch_bounds__(256) k_end_step(DevWorld w) {
+    uint32_t n = *w.pend_count;
+    if (n > w.pend_cap) n = w.pend_cap;
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        Pending p = w.pend[k];
+        atomicMin(&w.b_status[p.bond], p.code);
+    }
+    for (int s = threadIdx.x; s < w.S; s += blockDim.x) w.cc3[s] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *w.pend_count = 0u;
+        *w.step = *w.step + 1;
+    }
+}
+
+void launch_end_step(const DevWorld &w, cudaStream_t st) { k_end_step<<<1, 256, 0, st>>>(w); }
+
+// ------------------------------------------------------- Set_Properties
+// Set_Properties.wgsl:68-90; selections are indexed by scene-local particle.
+__global__ void __launch_bounds__(256) k_set_properties(DevWorld w, int scene,
+                                                        const int32_t *__restrict__ sel,
+                                                        int32_t *__restrict__ sel_out,
+                                                        const int32_t *__restrict__ in) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.N) return;
+    uint32_t m = w.meta[i];
+    if ((int)meta_scene(m) != scene) return;
+    int o = w.orig[i];
+    if (sel[o] == 0) return;
+    const float *f = reinterpret_cast<const float *>(in);
+    float4 p = w.pr[i], v = w.vw[i], d = w.dp[i], fe = w.fx[i];
+    bool setpos = false;
+    if (in[0] == 1) { d.x = f[14] - p.x; p.x = f[14]; setpos = true; }
+    if (in[1] == 1) { d.y = f[15] - p.y; p.y = f[15]; setpos = true; }
+    if (in[2] == 1) { d.z = f[16] - p.w; p.w = f[16]; }
+    if (in[3] == 1) v.x = f[17];
+    if (in[4] == 1) v.y = f[18];
+    if (in[5] == 1) v.z = f[19];
+    if (in[9] == 1) p.z = f[23];
+    if (in[6] == 1) fe.x = f[20];
+    if (in[7] == 1) fe.y = f[21];
+    if (in[8] == 1) fe.z = f[22];
+    if (in[10] == 1) {
+        m &= ~(M_KICK_X | M_FIX_X);
+        m |= (in[24] == 0 ? M_KICK_X : 0u) | (in[24] == 1 ? M_FIX_X : 0u);
+    }
+    if (in[11] == 1) {
+        m &= ~(M_KICK_Y | M_FIX_Y);
+        m |= (in[25] == 0 ? M_KICK_Y : 0u) | (in[25] == 1 ? M_FIX_Y : 0u);
+    }
+    if (in[12] == 1) {
+        m &= ~(M_KICK_R | M_FIX_R);
+        m |= (in[26] == 0 ? M_KICK_R : 0u) | (in[26] == 1 ? M_FIX_R : 0u);
+    }
+    if (in[13] == 1) m = (m & ~(0xFFu << 8)) | ((uint32_t)(in[27] & 0xFF) << 8);
+    if (fe.x != 0.0f || fe.y != 0.0f || fe.z != 0.0f) m |= M_FEXT;
+    else m &= ~M_FEXT;
+    w.pr[i] = p;
+    w.vw[i] = v;
+    w.dp[i] = d;
+    w.fx[i] = fe;
+    w.meta[i] = m;
+    if (setpos) w.cc3[scene] = 1;
+    if (in[10] == 1 || in[11] == 1 || in[12] == 1) sel_out[o] = 2;
+}
+
+void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
+                           const int32_t *d_props, int block, cudaStream_t st) {
+    if (w.N == 0) return;
+    k_set_properties<<<(w.N + block - 1) / block, block, 0, st>>>(w, scene, d_sel, d_sel_out, d_props);
+}
+
+}  // namespace demgb

@@ -1,0 +1,145 @@
+// dem_world.cuh -- device-resident state of one or more DEM scenes ("world").
+//
+// A world holds S independent scenes back to back in HBM.  Every particle
+// array is in *internal* order: the order of the last reorder by search cell,
+// which keeps neighbours close in memory.  orig[i] maps an internal index to
+// the scene-local index the reference uses (src/state.rs:69-93).
+//
+// Per-particle hot state is packed in float4 records so each load is one
+// 16-byte transaction:
+//   pr  {pos.x, pos.y, radius, rot}
+//   vw  {vel.x, vel.y, rot_vel, -}
+//   ac  {acc.x, acc.y, rot_acc, -}          ("accelerations" / rot_acc bindings)
+//   dp  {del_pos.x, del_pos.y, del_rot, -}
+//   fx  {forces.x, forces.y, forces.rot, -} (external forces, read when M_FEXT)
+//   d4  {v_half.x, v_half.y, w_half, -}     data[4..6] written by the LOM pass
+//   dF  {sum Fn, sum Ft, sum M, -}          data[0..2] written by the Simulation pass
+// Contact slots are SoA [14][N] (slot j of particle i at j*N+i), with a
+// 14-bit occupancy mask per particle so empty slots are never read.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dem.h"
+
+namespace demgb {
+
+constexpr int K = DEM_MAX_CONTACTS;
+
+// meta word: fixity predicates, external-force flag, material, scene
+enum : uint32_t {
+    M_KICK_X = 1u << 0,  // fixity.x_vel == 0  (2D_LOM.wgsl:88, 2D_Simulation.wgsl:471)
+    M_KICK_Y = 1u << 1,
+    M_KICK_R = 1u << 2,
+    M_FIX_X = 1u << 3,   // fixity.x_vel == 1  (walls skip the DOF, 2D_LOM.wgsl:108, 119)
+    M_FIX_Y = 1u << 4,
+    M_FIX_R = 1u << 5,
+    M_FEXT = 1u << 6,    // external force record is not all zero
+};
+__host__ __device__ inline uint32_t meta_mat(uint32_t m) { return (m >> 8) & 0xFFu; }
+__host__ __device__ inline uint32_t meta_scene(uint32_t m) { return m >> 16; }
+constexpr int MAX_SCENES = 65536;
+constexpr int MAX_MATERIALS = 256;
+
+struct Mat {
+    float density, kn, ks, pad;
+};
+
+struct ScenePar {
+    dem_params p;          // the 29-word uniform
+    float xW, yH;          // hor_bound / 2, vert_bound / 2 (2D_LOM.wgsl:105-106)
+    // reference bucket grid: defines which pairs are candidates and in which order
+    float ref_cs, ref_base_x, ref_base_y;
+    int32_t ref_w, ref_h;
+    // search grid (centre-binned, complete for every pair the reference grid can find)
+    float g_x0, g_y0, g_inv, g_cs;
+    int32_t g_w, g_h;
+    int32_t cell_base;     // first search cell of the scene in the global cell arrays
+    int32_t dead_cell;     // global cell of zero-radius particles (never searched)
+    int32_t stencil;       // search reach in cells
+    int32_t particle_base; // first internal index of the scene (scenes are contiguous)
+    int32_t n_particles;
+    int32_t bond_base;     // first bond record of the scene
+    int32_t mat_base;      // first material of the scene
+    int32_t n_mat;
+    int32_t use_f64;
+    float lambda;
+    int32_t has_strength;
+    int32_t active;        // 0 = frozen (skipped by every kernel)
+    int64_t step0;         // world step at which the scene's interval counter was cc1_0
+    int32_t cc1_0;
+    int32_t pad0;
+};
+
+struct Event {
+    int32_t scene, step, bond, code, a, b;
+};
+static_assert(sizeof(Event) == sizeof(dem_break_event), "event record layout");
+
+struct Pending {
+    int32_t bond, code;
+};
+
+struct DevWorld {
+    int32_t N, C, B, S, M;
+    float4 *pr, *vw, *ac, *dp, *fx, *d4, *dF;
+    uint32_t *meta;
+    int32_t *orig;
+    uint32_t *smask;
+    int32_t *s_b, *s_bonded;
+    float *s_tf, *s_btf, *s_thb;
+    int32_t *b_status;
+    float *b_length;
+    float2 *b_str;
+    Mat *mats;
+    ScenePar *par;
+    int32_t *cc3;              // per scene "positions set externally" flag
+    // broad phase
+    uint32_t *keys;
+    int32_t *cell_count, *cell_start, *sorted, *inv, *scan_tmp;
+    // bond breaks of the current step (applied after the Simulation pass)
+    Pending *pend;
+    uint32_t *pend_count;
+    uint32_t pend_cap;
+    // event log
+    Event *ev;
+    unsigned long long *ev_count;
+    uint32_t ev_cap;
+    unsigned long long *stats;  // [0] capped, [1] events, [2] dropped, [3] pending overflow
+    long long *step;            // device step counter
+    int32_t *err;
+};
+
+// ---- stateless detection schedule -----------------------------------------
+// The LOM pass's thread 0 does cc1 += 1; if cc1 >= interval {cc0 = 1; cc1 = 0}
+// else {cc0 = 0} (2D_LOM.wgsl:155-163).  From cc1_0 at step0 the detect steps
+// are j1, j1+P, j1+2P, ... with P = max(interval, 1), j1 = max(0, interval-1-cc1_0).
+__host__ __device__ inline bool detect_at(int32_t interval, int32_t cc1_0, long long j) {
+    long long P = interval > 1 ? interval : 1;
+    long long j1 = (long long)interval - 1 - cc1_0;
+    if (j1 < 0) j1 = 0;
+    return j >= j1 && ((j - j1) % P) == 0;
+}
+// counter value after j steps
+__host__ __device__ inline int32_t cc1_after(int32_t interval, int32_t cc1_0, long long j) {
+    if (j <= 0) return cc1_0;
+    long long P = interval > 1 ? interval : 1;
+    long long j1 = (long long)interval - 1 - cc1_0;
+    if (j1 < 0) j1 = 0;
+    if (j <= j1) return (int32_t)(cc1_0 + j);
+    long long since = (j - 1 - j1) % P;  // steps after the last detect
+    return (int32_t)since;
+}
+
+// host launchers (dem_kernels.cu)
+void launch_lom(const DevWorld &w, int block, cudaStream_t st);
+void launch_keys(const DevWorld &w, int block, cudaStream_t st);
+int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st);
+void launch_reorder(DevWorld &w, DevWorld &spare, int block, cudaStream_t st);
+void launch_interact(const DevWorld &w, int block, cudaStream_t st);
+void launch_end_step(const DevWorld &w, cudaStream_t st);
+void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
+                           const int32_t *d_props, int block, cudaStream_t st);
+int scan_tmp_size(int n);
+
+}  // namespace demgb

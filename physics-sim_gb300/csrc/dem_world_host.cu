@@ -1,0 +1,747 @@
+// dem_world_host.cu -- host owner of the device world (see dem_world_host.h).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+#include "dem_world_host.h"
+
+namespace demgb {
+
+#define CK(call)                                                                      \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess) return fail(DEM_E_CUDA, std::string(#call) + ": " +     \
+                                               cudaGetErrorString(e_));               \
+    } while (0)
+
+static inline int32_t f2bits(float f) {
+    int32_t i;
+    std::memcpy(&i, &f, 4);
+    return i;
+}
+static inline float bits2f(int32_t i) {
+    float f;
+    std::memcpy(&f, &i, 4);
+    return f;
+}
+
+World::~World() { release(); }
+
+int World::fail(int code, const std::string &msg) {
+    err = msg;
+    return code;
+}
+
+void World::release() {
+    for (void *p : owned) cudaFree(p);
+    owned.clear();
+    d = DevWorld{};
+    spare = DevWorld{};
+}
+
+template <class T>
+static T *dalloc(std::vector<void *> &owned, size_t count, bool &ok) {
+    if (!ok) return nullptr;
+    void *p = nullptr;
+    if (count == 0) count = 1;
+    if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
+        ok = false;
+        return nullptr;
+    }
+    owned.push_back(p);
+    return static_cast<T *>(p);
+}
+
+int World::alloc(int N, int C, int B, int S, int M, uint32_t ev_cap) {
+    release();
+    bool ok = true;
+    DevWorld &w = d;
+    w.N = N; w.C = C; w.B = B; w.S = S; w.M = M;
+    auto particle_arrays = [&](DevWorld &x) {
+        x.pr = dalloc<float4>(owned, N, ok);
+        x.vw = dalloc<float4>(owned, N, ok);
+        x.ac = dalloc<float4>(owned, N, ok);
+        x.dp = dalloc<float4>(owned, N, ok);
+        x.fx = dalloc<float4>(owned, N, ok);
+        x.d4 = dalloc<float4>(owned, N, ok);
+        x.dF = dalloc<float4>(owned, N, ok);
+        x.meta = dalloc<uint32_t>(owned, N, ok);
+        x.orig = dalloc<int32_t>(owned, N, ok);
+        x.smask = dalloc<uint32_t>(owned, N, ok);
+        x.s_b = dalloc<int32_t>(owned, (size_t)K * N, ok);
+        x.s_bonded = dalloc<int32_t>(owned, (size_t)K * N, ok);
+        x.s_tf = dalloc<float>(owned, (size_t)K * N, ok);
+        x.s_btf = dalloc<float>(owned, (size_t)K * N, ok);
+        x.s_thb = dalloc<float>(owned, (size_t)K * N, ok);
+    };
+    particle_arrays(w);
+    w.b_status = dalloc<int32_t>(owned, B, ok);
+    w.b_length = dalloc<float>(owned, B, ok);
+    w.b_str = dalloc<float2>(owned, B, ok);
+    w.mats = dalloc<Mat>(owned, M, ok);
+    w.par = dalloc<ScenePar>(owned, S, ok);
+    w.cc3 = dalloc<int32_t>(owned, S, ok);
+    w.keys = dalloc<uint32_t>(owned, N, ok);
+    w.cell_count = dalloc<int32_t>(owned, C, ok);
+    w.cell_start = dalloc<int32_t>(owned, (size_t)C + 1, ok);
+    w.sorted = dalloc<int32_t>(owned, N, ok);
+    w.inv = dalloc<int32_t>(owned, N, ok);
+    w.scan_tmp = dalloc<int32_t>(owned, scan_tmp_size(C), ok);
+    w.pend_cap = (uint32_t)std::max<long long>(2LL * B + 64, 64);
+    w.pend = dalloc<Pending>(owned, w.pend_cap, ok);
+    w.pend_count = dalloc<uint32_t>(owned, 1, ok);
+    w.ev_cap = ev_cap;
+    w.ev = dalloc<Event>(owned, ev_cap, ok);
+    w.ev_count = dalloc<unsigned long long>(owned, 1, ok);
+    w.stats = dalloc<unsigned long long>(owned, 4, ok);
+    w.step = dalloc<long long>(owned, 1, ok);
+    w.err = dalloc<int32_t>(owned, 1, ok);
+    spare = w;
+    particle_arrays(spare);
+    if (!ok) {
+        release();
+        return fail(DEM_E_OOM, "device allocation failed");
+    }
+    CK(cudaMemsetAsync(w.cell_count, 0, sizeof(int32_t) * (size_t)C, stream));
+    CK(cudaMemsetAsync(w.pend_count, 0, sizeof(uint32_t), stream));
+    CK(cudaMemsetAsync(w.ev_count, 0, sizeof(unsigned long long), stream));
+    CK(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), stream));
+    CK(cudaMemsetAsync(w.err, 0, sizeof(int32_t), stream));
+    CK(cudaMemsetAsync(w.cc3, 0, sizeof(int32_t) * (size_t)S, stream));
+    CK(cudaMemcpyAsync(w.step, &host_step, sizeof(long long), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    return DEM_OK;
+}
+
+// ---- scene validation and grid geometry -----------------------------------
+int World::compute_layout(SceneHost &h, const dem_scene *sc) {
+    if (!sc) return fail(DEM_E_INVALID, "scene is NULL");
+    const int n = sc->n_particles;
+    if (n < 0) return fail(DEM_E_INVALID, "n_particles < 0");
+    if (sc->n_bonds < 0) return fail(DEM_E_INVALID, "n_bonds < 0");
+    if (sc->n_materials <= 0 || sc->n_materials > MAX_MATERIALS)
+        return fail(DEM_E_INVALID, "n_materials must be in [1, 256]");
+    if (n > 0 && (!sc->pos || !sc->radii || !sc->vel || !sc->acc || !sc->rot || !sc->rot_vel ||
+                  !sc->rot_acc || !sc->forces || !sc->fixity || !sc->del_pos || !sc->del_rot ||
+                  !sc->contacts || !sc->material_pointers))
+        return fail(DEM_E_INVALID, "a required scene array is NULL");
+    if (!sc->materials) return fail(DEM_E_INVALID, "materials is NULL");
+    if (sc->n_bonds > 0 && !sc->bonds) return fail(DEM_E_INVALID, "bonds is NULL");
+    h.n = n;
+    h.n_bonds = sc->n_bonds;
+    h.n_mat = sc->n_materials;
+    float rmax = 0.0f;
+    float xmin = 0, xmax = 0, ymin = 0, ymax = 0;
+    bool any = false;
+    for (int i = 0; i < n; ++i) {
+        float r = sc->radii[i];
+        if (!(r >= 0.0f) || !std::isfinite(r)) return fail(DEM_E_INVALID, "radius must be finite and >= 0");
+        rmax = std::max(rmax, r);
+        int32_t mp = sc->material_pointers[i];
+        if (mp < 0 || mp >= sc->n_materials) return fail(DEM_E_INVALID, "material pointer out of range");
+        float x = sc->pos[2 * i], y = sc->pos[2 * i + 1];
+        if (std::isfinite(x) && std::isfinite(y) && r > 0.0f) {
+            if (!any) { xmin = xmax = x; ymin = ymax = y; any = true; }
+            xmin = std::min(xmin, x); xmax = std::max(xmax, x);
+            ymin = std::min(ymin, y); ymax = std::max(ymax, y);
+        }
+    }
+    for (long long k = 0; k < (long long)n * K; ++k) {
+        const int32_t *c = sc->contacts + 6 * k;
+        int owner = (int)(k / K);
+        if (c[5] >= sc->n_bonds) return fail(DEM_E_INVALID, "contact bonded index beyond n_bonds");
+        if (c[1] != -1) {
+            if (c[1] < 0 || c[1] >= n) return fail(DEM_E_INVALID, "contact partner out of range");
+            if (c[0] != owner) return fail(DEM_E_INVALID, "contact record's a differs from its owner");
+        }
+    }
+    h.r_max = rmax;
+    // reference bucket grid
+    dem_grid_info g = sc->grid;
+    if (!(g.cell_size > 0.0f) || g.w <= 0 || g.h <= 0) {
+        if (dem_grid_capacity(&h.params, sc->radii, n, n, &g) != 0)
+            return fail(DEM_E_INVALID, "cannot derive the bucket grid");
+    }
+    h.grid = g;
+    // search grid: centre-binned cells of side >= 2 r_max (1 + pad), covering the
+    // walls (or the particles, whichever is smaller in cells)
+    const dem_params &p = h.params;
+    float reach = std::max(2.0f * rmax, 1e-30f) * std::max(h.cell_factor, 1.0f);
+    double ex0, ex1, ey0, ey1;
+    if (p.round_bounds == 0) {
+        ex0 = -0.5 * p.hor_bound; ex1 = 0.5 * p.hor_bound;
+        ey0 = -0.5 * p.vert_bound; ey1 = 0.5 * p.vert_bound;
+    } else {
+        ex0 = ey0 = -(double)p.bound_radius;
+        ex1 = ey1 = (double)p.bound_radius;
+    }
+    if (any) {
+        ex0 = std::min(ex0, (double)xmin); ex1 = std::max(ex1, (double)xmax);
+        ey0 = std::min(ey0, (double)ymin); ey1 = std::max(ey1, (double)ymax);
+    }
+    double cap_cells = std::max(4.0 * n, 65536.0);
+    double span_x = (ex1 - ex0) + 2.0 * reach, span_y = (ey1 - ey0) + 2.0 * reach;
+    if (!(span_x > 0) || !(span_y > 0) || !std::isfinite(span_x) || !std::isfinite(span_y)) {
+        span_x = span_y = 2.0 * reach;
+        ex0 = ey0 = -reach; ex1 = ey1 = reach;
+    }
+    if ((span_x / reach) * (span_y / reach) > cap_cells && any) {
+        ex0 = xmin; ex1 = xmax; ey0 = ymin; ey1 = ymax;
+        span_x = (ex1 - ex0) + 2.0 * reach;
+        span_y = (ey1 - ey0) + 2.0 * reach;
+    }
+    double qmax = std::max(span_x, span_y) / reach + 2.0;
+    double pad = 1e-5 + 8.0 * std::ldexp(1.0, -24) * qmax;
+    float gcs = (float)(reach * (1.0 + pad));
+    int gw = (int)std::ceil(span_x / gcs) + 1;
+    int gh = (int)std::ceil(span_y / gcs) + 1;
+    gw = std::max(gw, 1);
+    gh = std::max(gh, 1);
+    if ((double)gw * gh > 2.0e9) return fail(DEM_E_INVALID, "search grid too large");
+    h.n_cells = gw * gh + 1;
+    ScenePar &P = h.par;
+    std::memset(&P, 0, sizeof P);
+    P.g_cs = gcs;
+    P.g_inv = 1.0f / gcs;
+    P.g_x0 = (float)(ex0 - reach);
+    P.g_y0 = (float)(ey0 - reach);
+    P.g_w = gw;
+    P.g_h = gh;
+    P.stencil = 1;
+    return DEM_OK;
+}
+
+void World::fill_par(SceneHost &h) {
+    ScenePar &P = h.par;
+    P.p = h.params;
+    P.p.particles = h.n;
+    P.xW = h.params.hor_bound / 2.0f;
+    P.yH = h.params.vert_bound / 2.0f;
+    P.ref_cs = h.grid.cell_size;
+    P.ref_w = h.grid.w;
+    P.ref_h = h.grid.h;
+    P.ref_base_x = ((-h.grid.cell_size) * (float)h.grid.w) * 0.5f;
+    P.ref_base_y = (h.grid.cell_size * (float)h.grid.h) * 0.5f;
+    P.cell_base = h.cell_base;
+    P.dead_cell = h.cell_base + h.n_cells - 1;
+    P.particle_base = h.particle_base;
+    P.n_particles = h.n;
+    P.bond_base = h.bond_base;
+    P.mat_base = h.mat_base;
+    P.n_mat = h.n_mat;
+    P.use_f64 = h.use_f64;
+    P.lambda = h.lambda;
+    P.has_strength = h.bond_sn.empty() ? 0 : 1;
+    P.active = h.active ? 1 : 0;
+    P.step0 = h.step0;
+    P.cc1_0 = h.cc1_0;
+}
+
+int World::push_par(int s) {
+    fill_par(sh[s]);
+    CK(cudaMemcpyAsync(d.par + s, &sh[s].par, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
+    return DEM_OK;
+}
+
+// ---- staging: reference layout -> internal layout --------------------------
+int World::stage_scene(int s, const dem_scene *sc) {
+    SceneHost &h = sh[s];
+    const int n = h.n, base = h.particle_base;
+    const int N = d.N;
+    h.fixity.assign(sc->fixity, sc->fixity + 6 * (size_t)n);
+    h.forces.assign(sc->forces, sc->forces + 6 * (size_t)n);
+    h.material_ptr.assign(sc->material_pointers, sc->material_pointers + n);
+    h.materials.assign(sc->materials, sc->materials + 6 * (size_t)h.n_mat);
+    h.data3.assign((size_t)n, 0.0f);
+    if (sc->data)
+        for (int i = 0; i < n; ++i) h.data3[i] = sc->data[7 * (size_t)i + 3];
+    std::vector<float4> pr(n), vw(n), ac(n), dp(n), fx(n), d4(n), dF(n);
+    std::vector<uint32_t> meta(n), mask(n);
+    std::vector<int32_t> orig(n);
+    std::vector<int32_t> sb((size_t)K * n), sbd((size_t)K * n);
+    std::vector<float> stf((size_t)K * n), sbtf((size_t)K * n), sthb((size_t)K * n);
+    for (int i = 0; i < n; ++i) {
+        pr[i] = make_float4(sc->pos[2 * i], sc->pos[2 * i + 1], sc->radii[i], sc->rot[i]);
+        vw[i] = make_float4(sc->vel[2 * i], sc->vel[2 * i + 1], sc->rot_vel[i], 0.0f);
+        ac[i] = make_float4(sc->acc[2 * i], sc->acc[2 * i + 1], sc->rot_acc[i], 0.0f);
+        dp[i] = make_float4(sc->del_pos[2 * i], sc->del_pos[2 * i + 1], sc->del_rot[i], 0.0f);
+        const float *f = sc->forces + 6 * i;
+        fx[i] = make_float4(f[0], f[1], f[2], 0.0f);
+        if (sc->data) {
+            const float *dd = sc->data + 7 * i;
+            d4[i] = make_float4(dd[4], dd[5], dd[6], 0.0f);
+            dF[i] = make_float4(dd[0], dd[1], dd[2], 0.0f);
+        } else {
+            d4[i] = dF[i] = make_float4(0, 0, 0, 0);
+        }
+        const int32_t *fix = sc->fixity + 6 * i;
+        uint32_t m = 0;
+        m |= fix[0] == 0 ? M_KICK_X : 0u;
+        m |= fix[1] == 0 ? M_KICK_Y : 0u;
+        m |= fix[2] == 0 ? M_KICK_R : 0u;
+        m |= fix[0] == 1 ? M_FIX_X : 0u;
+        m |= fix[1] == 1 ? M_FIX_Y : 0u;
+        m |= fix[2] == 1 ? M_FIX_R : 0u;
+        if (f[0] != 0.0f || f[1] != 0.0f || f[2] != 0.0f) m |= M_FEXT;
+        m |= ((uint32_t)sc->material_pointers[i] & 0xFFu) << 8;
+        m |= (uint32_t)s << 16;
+        meta[i] = m;
+        orig[i] = i;
+        uint32_t mk = 0;
+        for (int j = 0; j < K; ++j) {
+            const int32_t *c = sc->contacts + 6 * ((size_t)i * K + j);
+            size_t at = (size_t)j * n + i;
+            if (c[1] != -1) {
+                mk |= 1u << j;
+                sb[at] = base + c[1];
+            } else {
+                sb[at] = -1;
+            }
+            stf[at] = bits2f(c[2]);
+            sbtf[at] = bits2f(c[3]);
+            sthb[at] = bits2f(c[4]);
+            sbd[at] = c[5];
+        }
+        mask[i] = mk;
+    }
+    auto up = [&](auto *dst, const auto &src) -> cudaError_t {
+        if (src.empty()) return cudaSuccess;
+        return cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice,
+                               stream);
+    };
+    CK(up(d.pr + base, pr));
+    CK(up(d.vw + base, vw));
+    CK(up(d.ac + base, ac));
+    CK(up(d.dp + base, dp));
+    CK(up(d.fx + base, fx));
+    CK(up(d.d4 + base, d4));
+    CK(up(d.dF + base, dF));
+    CK(up(d.meta + base, meta));
+    CK(up(d.orig + base, orig));
+    CK(up(d.smask + base, mask));
+    for (int j = 0; j < K && n > 0; ++j) {
+        size_t off = (size_t)j * N + base, src = (size_t)j * n;
+        CK(cudaMemcpyAsync(d.s_b + off, sb.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d.s_bonded + off, sbd.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d.s_tf + off, stf.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d.s_btf + off, sbtf.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d.s_thb + off, sthb.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
+    }
+    // bonds
+    const int nb = h.n_bonds;
+    if (nb > 0) {
+        std::vector<int32_t> st(nb);
+        std::vector<float> len(nb);
+        std::vector<float2> str(nb);
+        h.bond_angle.resize(nb);
+        for (int k = 0; k < nb; ++k) {
+            st[k] = sc->bonds[3 * k];
+            h.bond_angle[k] = sc->bonds[3 * k + 1];
+            len[k] = bits2f(sc->bonds[3 * k + 2]);
+            str[k] = make_float2(h.bond_sn.empty() ? 0.0f : h.bond_sn[k],
+                                 h.bond_ss.empty() ? 0.0f : h.bond_ss[k]);
+        }
+        CK(up(d.b_status + h.bond_base, st));
+        CK(up(d.b_length + h.bond_base, len));
+        CK(up(d.b_str + h.bond_base, str));
+    }
+    // materials
+    std::vector<Mat> mats(h.n_mat);
+    for (int k = 0; k < h.n_mat; ++k) {
+        const float *mm = sc->materials + 6 * k;
+        mats[k] = Mat{mm[3], mm[4], mm[5], 0.0f};
+    }
+    CK(up(d.mats + h.mat_base, mats));
+    CK(cudaStreamSynchronize(stream));
+    return DEM_OK;
+}
+
+int World::build(const std::vector<const dem_scene *> &scenes, const std::vector<dem_params> &params,
+                 const dem_ext &ext) {
+    const int S = (int)scenes.size();
+    if (S <= 0 || S > MAX_SCENES) return fail(DEM_E_INVALID, "scene count out of range");
+    if (ext.block_size) {
+        if (ext.block_size < 32 || ext.block_size > 1024 || (ext.block_size & 31))
+            return fail(DEM_E_INVALID, "block_size must be a multiple of 32 in [32, 1024]");
+        block = ext.block_size;
+    }
+    if (ext.reorder_interval < 0) return fail(DEM_E_INVALID, "reorder_interval < 0");
+    if (ext.reorder_interval > 0) reorder_interval = ext.reorder_interval;
+    if (!(ext.bond_lambda > 0.0f)) return fail(DEM_E_INVALID, "bond_lambda must be > 0");
+    diagnostics = ext.diagnostics != 0;
+    sh.assign(S, SceneHost{});
+    long long N = 0, C = 0, B = 0, M = 0;
+    for (int s = 0; s < S; ++s) {
+        SceneHost &h = sh[s];
+        h.params = params[s];
+        h.use_f64 = ext.use_f64 ? 1 : 0;
+        h.lambda = ext.bond_lambda;
+        h.cell_factor = ext.search_cell_factor > 0.0f ? ext.search_cell_factor : 1.0f;
+        int rc = compute_layout(h, scenes[s]);
+        if (rc) return rc;
+        if (ext.bond_normal_strength && h.n_bonds > 0)
+            h.bond_sn.assign(ext.bond_normal_strength, ext.bond_normal_strength + h.n_bonds);
+        if (ext.bond_shear_strength && h.n_bonds > 0)
+            h.bond_ss.assign(ext.bond_shear_strength, ext.bond_shear_strength + h.n_bonds);
+        if (h.bond_sn.empty() != h.bond_ss.empty()) {
+            if (h.bond_sn.empty()) h.bond_sn.assign(h.n_bonds, params[s].bond_normal_strength);
+            if (h.bond_ss.empty()) h.bond_ss.assign(h.n_bonds, params[s].bond_shear_strength);
+        }
+        h.particle_base = (int)N;
+        h.cell_base = (int)C;
+        h.bond_base = (int)B;
+        h.mat_base = (int)M;
+        h.step0 = host_step;
+        h.cc0_0 = scenes[s]->coll_cont[0];
+        h.cc1_0 = scenes[s]->coll_cont[1];
+        h.cc2_0 = scenes[s]->coll_cont[2];
+        N += h.n;
+        C += h.n_cells;
+        B += h.n_bonds;
+        M += h.n_mat;
+    }
+    if (N > (1LL << 30) || C > (1LL << 31) - 2 || B > (1LL << 30))
+        return fail(DEM_E_INVALID, "world too large");
+    uint32_t ev_cap = ext.event_capacity > 0 ? (uint32_t)ext.event_capacity : 1u << 16;
+    int rc = alloc((int)N, (int)C, (int)B, S, (int)M, ev_cap);
+    if (rc) return rc;
+    for (int s = 0; s < S; ++s) {
+        rc = stage_scene(s, scenes[s]);
+        if (rc) return rc;
+        rc = push_par(s);
+        if (rc) return rc;
+        int32_t c3 = scenes[s]->coll_cont[3];
+        CK(cudaMemcpyAsync(d.cc3 + s, &c3, 4, cudaMemcpyHostToDevice, stream));
+    }
+    CK(cudaStreamSynchronize(stream));
+    steps_since_reorder = 0;
+    return DEM_OK;
+}
+
+int World::upload_scene(int s, const dem_scene *sc) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    SceneHost &h = sh[s];
+    if (!sc || sc->n_particles != h.n || sc->n_bonds != h.n_bonds || sc->n_materials != h.n_mat)
+        return fail(DEM_E_INVALID, "upload must keep particle, bond and material counts");
+    SceneHost probe = h;
+    int rc = compute_layout(probe, sc);
+    if (rc) return rc;
+    if (probe.n_cells > h.n_cells)
+        return fail(DEM_E_UNSUPPORTED, "uploaded scene needs a larger search grid; create a new context");
+    // keep the cell budget; adopt the new geometry inside it
+    probe.n_cells = h.n_cells;
+    h.r_max = probe.r_max;
+    h.grid = probe.grid;
+    h.par.g_cs = probe.par.g_cs;
+    h.par.g_inv = probe.par.g_inv;
+    h.par.g_x0 = probe.par.g_x0;
+    h.par.g_y0 = probe.par.g_y0;
+    h.par.g_w = probe.par.g_w;
+    h.par.g_h = probe.par.g_h;
+    CK(cudaStreamSynchronize(stream));
+    rc = stage_scene(s, sc);
+    if (rc) return rc;
+    return push_par(s);
+}
+
+int World::set_params(int s, const dem_params &p) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    SceneHost &h = sh[s];
+    dem_params old = h.params;
+    // the interval counter restarts its schedule from the current step
+    int32_t cc[4];
+    control(s, cc);
+    h.params = p;
+    bool geometry = old.hor_bound != p.hor_bound || old.vert_bound != p.vert_bound ||
+                    old.round_bounds != p.round_bounds || old.bound_radius != p.bound_radius;
+    if (geometry) {
+        // walls moved: the search grid keeps its allocation and clamps particles to it
+    }
+    h.step0 = host_step;
+    h.cc0_0 = cc[0];
+    h.cc1_0 = cc[1];
+    h.cc2_0 = cc[2];
+    return push_par(s);
+}
+
+int World::set_materials(int s, const float *m, int n) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    SceneHost &h = sh[s];
+    if (!m || n != h.n_mat) return fail(DEM_E_INVALID, "material count must stay the same");
+    h.materials.assign(m, m + 6 * (size_t)n);
+    std::vector<Mat> mats(n);
+    for (int k = 0; k < n; ++k) mats[k] = Mat{m[6 * k + 3], m[6 * k + 4], m[6 * k + 5], 0.0f};
+    CK(cudaMemcpyAsync(d.mats + h.mat_base, mats.data(), n * sizeof(Mat), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    return DEM_OK;
+}
+
+void World::control(int s, int32_t cc[4]) const {
+    const SceneHost &h = sh[s];
+    long long j = host_step - h.step0;
+    int32_t iv = h.params.collision_interval;
+    if (j <= 0) {
+        cc[0] = h.cc0_0;
+        cc[1] = h.cc1_0;
+        cc[2] = h.cc2_0;
+    } else {
+        cc[0] = detect_at(iv, h.cc1_0, j - 1) ? 1 : 0;
+        cc[1] = cc1_after(iv, h.cc1_0, j);
+        cc[2] = (int32_t)(h.cc2_0 + j);
+    }
+    cc[3] = 0;
+}
+
+int World::set_control(int s, const int32_t cc[4]) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    SceneHost &h = sh[s];
+    h.step0 = host_step;
+    h.cc0_0 = cc[0];
+    h.cc1_0 = cc[1];
+    h.cc2_0 = cc[2];
+    int32_t c3 = cc[3];
+    CK(cudaMemcpyAsync(d.cc3 + s, &c3, 4, cudaMemcpyHostToDevice, stream));
+    return push_par(s);
+}
+
+int World::step(int n_steps) {
+    if (n_steps < 0) return fail(DEM_E_INVALID, "n_steps < 0");
+    for (int k = 0; k < n_steps; ++k) {
+        launch_lom(d, block, stream);
+        launch_broad_phase(d, block, stream);
+        if (++steps_since_reorder >= reorder_interval) {
+            launch_reorder(d, spare, block, stream);
+            std::swap(d.pr, spare.pr);
+            std::swap(d.vw, spare.vw);
+            std::swap(d.ac, spare.ac);
+            std::swap(d.dp, spare.dp);
+            std::swap(d.fx, spare.fx);
+            std::swap(d.d4, spare.d4);
+            std::swap(d.dF, spare.dF);
+            std::swap(d.meta, spare.meta);
+            std::swap(d.orig, spare.orig);
+            std::swap(d.smask, spare.smask);
+            std::swap(d.s_b, spare.s_b);
+            std::swap(d.s_bonded, spare.s_bonded);
+            std::swap(d.s_tf, spare.s_tf);
+            std::swap(d.s_btf, spare.s_btf);
+            std::swap(d.s_thb, spare.s_thb);
+            steps_since_reorder = 0;
+            reorders++;
+        }
+        launch_interact(d, block, stream);
+        launch_end_step(d, stream);
+        host_step++;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return DEM_OK;
+}
+
+int World::sync() {
+    CK(cudaStreamSynchronize(stream));
+    int32_t e = 0;
+    CK(cudaMemcpy(&e, d.err, 4, cudaMemcpyDeviceToHost));
+    if (e) return fail(DEM_E_STATE, "device error flags set: " + std::to_string(e));
+    return DEM_OK;
+}
+
+int World::download_scene(int s, dem_scene *out) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    if (!out) return fail(DEM_E_INVALID, "out is NULL");
+    const SceneHost &h = sh[s];
+    const int n = h.n, base = h.particle_base, N = d.N;
+    if (out->n_particles != n) return fail(DEM_E_INVALID, "out->n_particles must match the scene");
+    CK(cudaStreamSynchronize(stream));
+    std::vector<float4> pr(n), vw(n), ac(n), dp(n), d4(n), dF(n);
+    std::vector<uint32_t> mask(n);
+    std::vector<int32_t> orig(n);
+    std::vector<int32_t> sb((size_t)K * n), sbd((size_t)K * n);
+    std::vector<float> stf((size_t)K * n), sbtf((size_t)K * n), sthb((size_t)K * n);
+    auto dn = [&](auto &dst, const auto *src) -> cudaError_t {
+        if (dst.empty()) return cudaSuccess;
+        return cudaMemcpyAsync(dst.data(), src, dst.size() * sizeof(dst[0]), cudaMemcpyDeviceToHost, stream);
+    };
+    CK(dn(pr, d.pr + base));
+    CK(dn(vw, d.vw + base));
+    CK(dn(ac, d.ac + base));
+    CK(dn(dp, d.dp + base));
+    CK(dn(d4, d.d4 + base));
+    CK(dn(dF, d.dF + base));
+    CK(dn(mask, d.smask + base));
+    CK(dn(orig, d.orig + base));
+    for (int j = 0; j < K && n > 0; ++j) {
+        size_t off = (size_t)j * N + base, dst = (size_t)j * n;
+        CK(cudaMemcpyAsync(sb.data() + dst, d.s_b + off, n * 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(sbd.data() + dst, d.s_bonded + off, n * 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(stf.data() + dst, d.s_tf + off, n * 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(sbtf.data() + dst, d.s_btf + off, n * 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(sthb.data() + dst, d.s_thb + off, n * 4, cudaMemcpyDeviceToHost, stream));
+    }
+    std::vector<int32_t> bst(h.n_bonds);
+    if (h.n_bonds > 0) CK(dn(bst, d.b_status + h.bond_base));
+    CK(cudaStreamSynchronize(stream));
+    for (int i = 0; i < n; ++i) {
+        const int o = orig[i];
+        if (o < 0 || o >= n) return fail(DEM_E_STATE, "internal particle map is corrupt");
+        if (out->pos) { out->pos[2 * o] = pr[i].x; out->pos[2 * o + 1] = pr[i].y; }
+        if (out->radii) out->radii[o] = pr[i].z;
+        if (out->rot) out->rot[o] = pr[i].w;
+        if (out->vel) { out->vel[2 * o] = vw[i].x; out->vel[2 * o + 1] = vw[i].y; }
+        if (out->rot_vel) out->rot_vel[o] = vw[i].z;
+        if (out->acc) { out->acc[2 * o] = ac[i].x; out->acc[2 * o + 1] = ac[i].y; }
+        if (out->rot_acc) out->rot_acc[o] = ac[i].z;
+        if (out->del_pos) { out->del_pos[2 * o] = dp[i].x; out->del_pos[2 * o + 1] = dp[i].y; }
+        if (out->del_rot) out->del_rot[o] = dp[i].z;
+        if (out->data) {
+            float *dd = out->data + 7 * (size_t)o;
+            dd[0] = dF[i].x; dd[1] = dF[i].y; dd[2] = dF[i].z; dd[3] = h.data3[o];
+            dd[4] = d4[i].x; dd[5] = d4[i].y; dd[6] = d4[i].z;
+        }
+        if (out->contacts) {
+            for (int j = 0; j < K; ++j) {
+                size_t at = (size_t)j * n + i;
+                int32_t *c = out->contacts + 6 * ((size_t)o * K + j);
+                if ((mask[i] >> j) & 1u) {
+                    int pb = sb[at] - base;
+                    if (pb < 0 || pb >= n) return fail(DEM_E_STATE, "contact partner outside its scene");
+                    c[0] = o;
+                    c[1] = orig[pb];
+                } else {
+                    c[0] = -1;
+                    c[1] = -1;
+                }
+                c[2] = f2bits(stf[at]);
+                c[3] = f2bits(sbtf[at]);
+                c[4] = f2bits(sthb[at]);
+                c[5] = sbd[at];
+            }
+        }
+    }
+    if (out->fixity) std::memcpy(out->fixity, h.fixity.data(), h.fixity.size() * 4);
+    if (out->forces) std::memcpy(out->forces, h.forces.data(), h.forces.size() * 4);
+    if (out->material_pointers) std::memcpy(out->material_pointers, h.material_ptr.data(), h.material_ptr.size() * 4);
+    if (out->materials && out->n_materials == h.n_mat)
+        std::memcpy(out->materials, h.materials.data(), h.materials.size() * 4);
+    if (out->bonds && out->n_bonds == h.n_bonds) {
+        std::vector<float> blen(h.n_bonds);
+        if (h.n_bonds > 0) CK(cudaMemcpy(blen.data(), d.b_length + h.bond_base, h.n_bonds * 4, cudaMemcpyDeviceToHost));
+        for (int k = 0; k < h.n_bonds; ++k) {
+            out->bonds[3 * k] = bst[k];
+            out->bonds[3 * k + 1] = h.bond_angle[k];
+            out->bonds[3 * k + 2] = f2bits(blen[k]);
+        }
+    }
+    control(s, out->coll_cont);
+    out->grid = h.grid;
+    return DEM_OK;
+}
+
+int World::set_properties(int s, int32_t *selections, const int32_t *props) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    if (!selections || !props) return fail(DEM_E_INVALID, "selections/props is NULL");
+    SceneHost &h = sh[s];
+    const int n = h.n;
+    if (props[13] == 1 && (props[27] < 0 || props[27] >= h.n_mat))
+        return fail(DEM_E_INVALID, "material index out of range");
+    float f[28];
+    std::memcpy(f, props, sizeof f);
+    bool any = false;
+    for (int i = 0; i < n; ++i) any |= selections[i] != 0;
+    if (props[9] == 1 && any && !(f[23] >= 0.0f && std::isfinite(f[23])))
+        return fail(DEM_E_INVALID, "radius must be finite and >= 0");
+    if (props[9] == 1 && any && f[23] > h.r_max && f[23] * 2.0f * (1.0f + 1e-3f) > h.par.g_cs)
+        return fail(DEM_E_UNSUPPORTED, "radius beyond the search grid's reach; create a new context");
+    int32_t *dsel = nullptr, *dout = nullptr, *dprops = nullptr;
+    CK(cudaMalloc(&dsel, sizeof(int32_t) * (n > 0 ? n : 1)));
+    CK(cudaMalloc(&dout, sizeof(int32_t) * (n > 0 ? n : 1)));
+    CK(cudaMalloc(&dprops, sizeof(int32_t) * 28));
+    cudaMemcpyAsync(dsel, selections, sizeof(int32_t) * n, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(dout, selections, sizeof(int32_t) * n, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(dprops, props, sizeof(int32_t) * 28, cudaMemcpyHostToDevice, stream);
+    launch_set_properties(d, s, dsel, dout, dprops, block, stream);
+    cudaError_t e = cudaMemcpyAsync(selections, dout, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, stream);
+    cudaError_t e2 = cudaStreamSynchronize(stream);
+    cudaFree(dsel);
+    cudaFree(dout);
+    cudaFree(dprops);
+    if (e != cudaSuccess || e2 != cudaSuccess) return fail(DEM_E_CUDA, "set_properties failed");
+    // mirror on the host copies the step never writes
+    for (int i = 0; i < n; ++i) {
+        if (selections[i] == 0) continue;
+        if (props[6] == 1) h.forces[6 * i] = f[20];
+        if (props[7] == 1) h.forces[6 * i + 1] = f[21];
+        if (props[8] == 1) h.forces[6 * i + 2] = f[22];
+        if (props[10] == 1) { h.fixity[6 * i] = props[24]; h.fixity[6 * i + 3] = props[24]; }
+        if (props[11] == 1) { h.fixity[6 * i + 1] = props[25]; h.fixity[6 * i + 4] = props[25]; }
+        if (props[12] == 1) { h.fixity[6 * i + 2] = props[26]; h.fixity[6 * i + 5] = props[26]; }
+        if (props[13] == 1) h.material_ptr[i] = props[27];
+        if (props[9] == 1) h.r_max = std::max(h.r_max, f[23]);
+    }
+    return DEM_OK;
+}
+
+int World::drain_events(std::vector<dem_break_event> &out) {
+    CK(cudaStreamSynchronize(stream));
+    unsigned long long cnt = 0;
+    CK(cudaMemcpy(&cnt, d.ev_count, sizeof cnt, cudaMemcpyDeviceToHost));
+    size_t k = (size_t)std::min<unsigned long long>(cnt, d.ev_cap);
+    out.resize(k);
+    if (k) CK(cudaMemcpy(out.data(), d.ev, k * sizeof(Event), cudaMemcpyDeviceToHost));
+    CK(cudaMemset(d.ev_count, 0, sizeof(unsigned long long)));
+    std::sort(out.begin(), out.end(), [](const dem_break_event &x, const dem_break_event &y) {
+        if (x.step != y.step) return x.step < y.step;
+        if (x.scene != y.scene) return x.scene < y.scene;
+        if (x.bond != y.bond) return x.bond < y.bond;
+        if (x.a != y.a) return x.a < y.a;
+        return x.b < y.b;
+    });
+    return DEM_OK;
+}
+
+int World::broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *cell_start,
+                                int32_t *n_cells) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    const SceneHost &h = sh[s];
+    if (n_cells) *n_cells = h.n_cells;
+    launch_keys(d, block, stream);
+    launch_broad_phase(d, block, stream);
+    const int n = h.n, base = h.particle_base;
+    std::vector<uint32_t> k(n);
+    std::vector<int32_t> srt(n), orig(n), cs((size_t)h.n_cells + 1);
+    if (n > 0) {
+        CK(cudaMemcpyAsync(k.data(), d.keys + base, n * 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(srt.data(), d.sorted + base, n * 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(orig.data(), d.orig + base, n * 4, cudaMemcpyDeviceToHost, stream));
+    }
+    CK(cudaMemcpyAsync(cs.data(), d.cell_start + h.cell_base, cs.size() * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    for (int i = 0; i < n; ++i) {
+        if (keys) keys[orig[i]] = (int32_t)k[i] - h.cell_base;
+        int src = srt[i] - base;
+        if (src < 0 || src >= n) return fail(DEM_E_STATE, "sorted order leaves its scene");
+        if (order) order[i] = orig[src];
+    }
+    if (cell_start)
+        for (size_t c = 0; c < cs.size(); ++c) cell_start[c] = cs[c] - base;
+    return DEM_OK;
+}
+
+int World::stats(dem_stats *out) {
+    CK(cudaStreamSynchronize(stream));
+    unsigned long long st[4];
+    CK(cudaMemcpy(st, d.stats, sizeof st, cudaMemcpyDeviceToHost));
+    int32_t e = 0;
+    CK(cudaMemcpy(&e, d.err, 4, cudaMemcpyDeviceToHost));
+    std::memset(out, 0, sizeof *out);
+    out->steps = host_step;
+    out->capped = (int64_t)st[0];
+    out->events = (int64_t)st[1];
+    out->events_dropped = (int64_t)st[2];
+    out->reorders = reorders;
+    out->device_error = e | (st[3] ? 1 : 0);
+    return DEM_OK;
+}
+
+}  // namespace demgb

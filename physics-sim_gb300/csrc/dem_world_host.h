@@ -1,0 +1,88 @@
+// dem_world_host.h -- host-side owner of a DevWorld: allocation, scene
+// layout (grid geometry, offsets), conversion between the reference's host
+// layouts and the internal device layout, and step orchestration.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "dem.h"
+#include "dem_world.cuh"
+
+namespace demgb {
+
+struct SceneHost {
+    // reference-layout copies of what the step never writes (kept for download)
+    std::vector<int32_t> fixity;       // [6n]
+    std::vector<float> forces;         // [6n]
+    std::vector<int32_t> material_ptr; // [n]
+    std::vector<float> materials;      // [6m]
+    std::vector<int32_t> bond_angle;   // [B] raw bits
+    std::vector<float> data3;          // [n] data[7i+3], never written by a step
+    std::vector<float> bond_sn, bond_ss;
+    dem_params params;
+    dem_grid_info grid;
+    int n = 0, n_bonds = 0, n_mat = 0;
+    float r_max = 0.0f;
+    int use_f64 = 0;
+    float lambda = 0.5f;
+    float cell_factor = 1.0f;
+    // control words (coll_cont) at step0
+    long long step0 = 0;
+    int32_t cc0_0 = 0, cc1_0 = 0, cc2_0 = 0;
+    bool active = true;
+    // layout in the world
+    int particle_base = 0, cell_base = 0, n_cells = 0, bond_base = 0, mat_base = 0;
+    ScenePar par;
+};
+
+class World {
+  public:
+    World() = default;
+    ~World();
+    World(const World &) = delete;
+    World &operator=(const World &) = delete;
+
+    // Lay out the given scenes (host staging), allocate and upload.  Returns DEM_* code.
+    int build(const std::vector<const dem_scene *> &scenes, const std::vector<dem_params> &params,
+              const dem_ext &ext);
+    // Replace one scene's state in place (same particle/bond/material counts).
+    int upload_scene(int s, const dem_scene *scene);
+    int download_scene(int s, dem_scene *out);
+    int set_params(int s, const dem_params &p);
+    int set_materials(int s, const float *m, int n);
+    int set_properties(int s, int32_t *selections, const int32_t *props);
+    int step(int n_steps);
+    int sync();
+    int drain_events(std::vector<dem_break_event> &out);
+    int stats(dem_stats *out);
+    int broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *cell_start, int32_t *n_cells);
+    void control(int s, int32_t cc[4]) const;
+    int set_control(int s, const int32_t cc[4]);
+
+    std::string err;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int block = 256;
+    int reorder_interval = 20;
+    bool diagnostics = true;
+    long long host_step = 0;
+    long long reorders = 0;
+    std::vector<SceneHost> sh;
+    DevWorld d{};
+
+  private:
+    int fail(int code, const std::string &msg);
+    int alloc(int N, int C, int B, int S, int M, uint32_t ev_cap);
+    void release();
+    int compute_layout(SceneHost &h, const dem_scene *scene);
+    void fill_par(SceneHost &h);
+    int push_par(int s);
+    int stage_scene(int s, const dem_scene *scene);
+    DevWorld spare{};
+    std::vector<void *> owned;
+    int steps_since_reorder = 0;
+};
+
+}  // namespace demgb

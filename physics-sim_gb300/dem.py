@@ -1,0 +1,347 @@
+"""ctypes binding of libdemgb.so (include/dem.h, include/dem_debug.h).
+
+The host-side mirror of the reference's compute program for Python callers:
+`Context` plays WGPUComputeProg (src/wgpu_prog.rs): `step(n)` is `compute`
+with gen_per_frame = n, `upload` is `restore`, `download` is `update_state`,
+`set_properties` is the Set_Properties event.  Scenes are dicts of numpy
+arrays in the reference's host layouts (src/state.rs:69-93):
+
+    pos f32[2n], radii f32[n], vel f32[2n], acc f32[2n], rot f32[n],
+    rot_vel f32[n], rot_acc f32[n], forces f32[6n], fixity i32[6n],
+    del_pos f32[2n], del_rot f32[n], bonds i32[3B], contacts i32[84n],
+    material_pointers i32[n], materials f32[6M], data f32[7n],
+    coll_cont i32[4], grid (cell_size, cell_cap, w, h)
+
+There is no fallback: if the CUDA library cannot be loaded, or no GPU is
+present, the calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdemgb.so")
+
+MAX_CONTACTS = 14
+DATA_SIZE = 7
+
+DEM_E = {0: "OK", -1: "INVALID", -2: "OOM", -3: "CUDA", -4: "TIMEOUT", -5: "STATE",
+         -6: "UNSUPPORTED", -7: "CAPACITY"}
+
+PARAM_FIELDS = [
+    ("walls", C.c_int32), ("hor_bound", C.c_float), ("vert_bound", C.c_float),
+    ("round_bounds", C.c_int32), ("bound_radius", C.c_float), ("wall_friction", C.c_float),
+    ("gravity", C.c_int32), ("planet_mode", C.c_int32), ("bonds", C.c_int32),
+    ("collisions", C.c_int32), ("friction_coefficient", C.c_float), ("gravity_acc", C.c_float),
+    ("bond_normal_stiffness", C.c_float), ("bonds_tear", C.c_int32),
+    ("bond_normal_strength", C.c_float), ("contact_damping", C.c_float),
+    ("bond_damping", C.c_float), ("drag", C.c_float), ("bond_shear_strength", C.c_float),
+    ("dT", C.c_float), ("bond_shear_stiffness", C.c_float), ("gravity_x", C.c_float),
+    ("gravity_y", C.c_float), ("mouse_gravity", C.c_int32),
+    ("moment_contribution_factor", C.c_float), ("collision_interval", C.c_int32),
+    ("local_damping", C.c_int32), ("local_damping_alpha", C.c_float), ("particles", C.c_int32),
+]
+
+_FP = C.POINTER(C.c_float)
+_IP = C.POINTER(C.c_int32)
+
+
+class Params(C.Structure):
+    _fields_ = PARAM_FIELDS
+
+
+class GridInfo(C.Structure):
+    _fields_ = [("cell_size", C.c_float), ("cell_cap", C.c_int32), ("w", C.c_int32), ("h", C.c_int32)]
+
+
+class Ext(C.Structure):
+    _fields_ = [("use_f64", C.c_int32), ("bond_lambda", C.c_float),
+                ("bond_normal_strength", _FP), ("bond_shear_strength", _FP),
+                ("diagnostics", C.c_int32), ("reorder_interval", C.c_int32),
+                ("block_size", C.c_int32), ("search_cell_factor", C.c_float),
+                ("event_capacity", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class Scene(C.Structure):
+    _fields_ = [("n_particles", C.c_int32), ("n_bonds", C.c_int32), ("n_materials", C.c_int32),
+                ("pos", _FP), ("radii", _FP), ("vel", _FP), ("acc", _FP), ("rot", _FP),
+                ("rot_vel", _FP), ("rot_acc", _FP), ("forces", _FP), ("fixity", _IP),
+                ("del_pos", _FP), ("del_rot", _FP), ("bonds", _IP), ("contacts", _IP),
+                ("material_pointers", _IP), ("materials", _FP), ("data", _FP),
+                ("coll_cont", C.c_int32 * 4), ("grid", GridInfo)]
+
+
+class BreakEvent(C.Structure):
+    _fields_ = [("scene", C.c_int32), ("step", C.c_int32), ("bond", C.c_int32),
+                ("code", C.c_int32), ("a", C.c_int32), ("b", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("capped", C.c_int64), ("events", C.c_int64),
+                ("events_dropped", C.c_int64), ("reorders", C.c_int64),
+                ("device_error", C.c_int32), ("reserved", C.c_int32)]
+
+
+BREAK_DTYPE = np.dtype([("scene", "<i4"), ("step", "<i4"), ("bond", "<i4"), ("code", "<i4"),
+                        ("a", "<i4"), ("b", "<i4")])
+
+# exported symbols of include/dem.h and include/dem_debug.h
+SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_capacity",
+           "dem_create", "dem_destroy", "dem_upload", "dem_set_params", "dem_set_materials",
+           "dem_set_control", "dem_get_control", "dem_step", "dem_synchronize", "dem_download",
+           "dem_set_properties", "dem_break_events", "dem_get_stats", "dem_stream",
+           "dem_debug_broad_phase", "dem_debug_search_grid"]
+
+_lib = None
+
+
+class DemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("dem error %d (%s): %s" % (code, DEM_E.get(code, "?"), msg))
+        self.code = code
+
+
+def lib(path=None):
+    """Load libdemgb.so (built by build_lib.py); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise OSError("libdemgb.so not built at %s (run __graft_entry__.build())" % path)
+    L = C.CDLL(path)
+    L.dem_abi_version.restype = C.c_int
+    L.dem_ext_defaults.argtypes = [C.POINTER(Ext)]
+    L.dem_last_error.argtypes = [C.c_void_p]
+    L.dem_last_error.restype = C.c_char_p
+    L.dem_grid_capacity.argtypes = [C.POINTER(Params), _FP, C.c_int32, C.c_int32, C.POINTER(GridInfo)]
+    L.dem_create.argtypes = [C.POINTER(Scene), C.POINTER(Params), C.POINTER(Ext), C.c_int,
+                             C.POINTER(C.c_void_p)]
+    L.dem_destroy.argtypes = [C.c_void_p]
+    L.dem_destroy.restype = None
+    L.dem_upload.argtypes = [C.c_void_p, C.POINTER(Scene)]
+    L.dem_set_params.argtypes = [C.c_void_p, C.POINTER(Params)]
+    L.dem_set_materials.argtypes = [C.c_void_p, _FP, C.c_int32]
+    L.dem_set_control.argtypes = [C.c_void_p, _IP]
+    L.dem_get_control.argtypes = [C.c_void_p, _IP]
+    L.dem_step.argtypes = [C.c_void_p, C.c_int32]
+    L.dem_synchronize.argtypes = [C.c_void_p]
+    L.dem_download.argtypes = [C.c_void_p, C.POINTER(Scene)]
+    L.dem_set_properties.argtypes = [C.c_void_p, _IP, _IP]
+    L.dem_break_events.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
+    L.dem_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    L.dem_stream.argtypes = [C.c_void_p]
+    L.dem_stream.restype = C.c_void_p
+    L.dem_debug_broad_phase.argtypes = [C.c_void_p, _IP, _IP, _IP, C.POINTER(C.c_int32)]
+    L.dem_debug_search_grid.argtypes = [C.c_void_p, _FP, _FP, _FP, _IP, _IP]
+    for name in SYMBOLS:
+        if name not in ("dem_destroy", "dem_ext_defaults", "dem_last_error", "dem_stream",
+                        "dem_abi_version"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def make_params(d):
+    p = Params()
+    for k, _ in PARAM_FIELDS:
+        setattr(p, k, d[k])
+    return p
+
+
+def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnostics=True,
+             reorder_interval=0, block_size=0, search_cell_factor=0.0, event_capacity=0, keep=None):
+    e = Ext()
+    lib().dem_ext_defaults(C.byref(e))
+    e.use_f64 = 1 if use_f64 else 0
+    e.bond_lambda = bond_lambda
+    e.diagnostics = 1 if diagnostics else 0
+    e.reorder_interval = reorder_interval
+    e.block_size = block_size
+    e.search_cell_factor = search_cell_factor
+    e.event_capacity = event_capacity
+    for attr, arr in (("bond_normal_strength", bond_sn), ("bond_shear_strength", bond_ss)):
+        if arr is not None:
+            a = np.ascontiguousarray(arr, dtype=np.float32)
+            setattr(e, attr, a.ctypes.data_as(_FP))
+            if keep is not None:
+                keep.append(a)
+    return e
+
+
+F32_KEYS = ("pos", "radii", "vel", "acc", "rot", "rot_vel", "rot_acc", "forces", "del_pos",
+            "del_rot", "materials", "data")
+I32_KEYS = ("fixity", "bonds", "contacts", "material_pointers")
+
+
+def make_scene(sc):
+    """Scene struct pointing into the numpy arrays of dict `sc` (kept alive by the caller)."""
+    for k in F32_KEYS:
+        a = sc[k]
+        if a.dtype != np.float32 or not a.flags.c_contiguous:
+            raise TypeError("%s must be contiguous float32" % k)
+    for k in I32_KEYS:
+        a = sc[k]
+        if a.dtype != np.int32 or not a.flags.c_contiguous:
+            raise TypeError("%s must be contiguous int32" % k)
+    s = Scene()
+    n = int(sc["radii"].shape[0])
+    s.n_particles = n
+    s.n_bonds = int(sc["bonds"].shape[0] // 3)
+    s.n_materials = int(sc["materials"].shape[0] // 6)
+    for k in F32_KEYS:
+        setattr(s, k, sc[k].ctypes.data_as(_FP))
+    for k in I32_KEYS:
+        setattr(s, k, sc[k].ctypes.data_as(_IP))
+    for i in range(4):
+        s.coll_cont[i] = int(sc["coll_cont"][i])
+    cs, cap, w, h = sc["grid"]
+    s.grid.cell_size = float(cs)
+    s.grid.cell_cap = int(cap)
+    s.grid.w = int(w)
+    s.grid.h = int(h)
+    return s
+
+
+def empty_like_scene(sc):
+    out = {k: np.zeros_like(sc[k]) for k in F32_KEYS + I32_KEYS}
+    out["coll_cont"] = np.zeros(4, dtype=np.int32)
+    out["grid"] = sc["grid"]
+    return out
+
+
+def _check(L, ctx, rc):
+    if rc != 0:
+        raise DemError(rc, (L.dem_last_error(ctx) or b"").decode())
+
+
+class Context:
+    """One scene resident on one GPU (WGPUComputeProg's compute side)."""
+
+    def __init__(self, scene, params, *, device=-1, **ext_kw):
+        L = lib()
+        self._keep = []
+        self.params = dict(params)
+        ext = make_ext(keep=self._keep, **ext_kw)
+        self._template = {k: (v.copy() if hasattr(v, "copy") else v) for k, v in scene.items()}
+        st = make_scene(scene)
+        p = make_params(self.params)
+        h = C.c_void_p()
+        rc = L.dem_create(C.byref(st), C.byref(p), C.byref(ext), device, C.byref(h))
+        if rc != 0:
+            raise DemError(rc, (L.dem_last_error(None) or b"").decode())
+        self.h = h
+        self.n = int(scene["radii"].shape[0])
+        self.dt = np.float32(self.params["dT"])
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().dem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def step(self, n=1):
+        L = lib()
+        _check(L, self.h, L.dem_step(self.h, int(n)))
+
+    def synchronize(self):
+        L = lib()
+        _check(L, self.h, L.dem_synchronize(self.h))
+
+    def download(self):
+        L = lib()
+        out = empty_like_scene(self._template)
+        st = make_scene(out)
+        _check(L, self.h, L.dem_download(self.h, C.byref(st)))
+        out["coll_cont"] = np.array(st.coll_cont[:], dtype=np.int32)
+        return out
+
+    def upload(self, scene):
+        L = lib()
+        st = make_scene(scene)
+        _check(L, self.h, L.dem_upload(self.h, C.byref(st)))
+
+    def set_params(self, params):
+        L = lib()
+        self.params = dict(params)
+        p = make_params(self.params)
+        _check(L, self.h, L.dem_set_params(self.h, C.byref(p)))
+
+    def set_properties(self, selections, words):
+        L = lib()
+        sel = np.ascontiguousarray(selections, dtype=np.int32).copy()
+        w = np.ascontiguousarray(words, dtype=np.int32)
+        _check(L, self.h, L.dem_set_properties(self.h, sel.ctypes.data_as(_IP), w.ctypes.data_as(_IP)))
+        return sel
+
+    def control(self):
+        L = lib()
+        cc = np.zeros(4, dtype=np.int32)
+        _check(L, self.h, L.dem_get_control(self.h, cc.ctypes.data_as(_IP)))
+        return cc
+
+    def set_control(self, cc):
+        L = lib()
+        cc = np.ascontiguousarray(cc, dtype=np.int32)
+        _check(L, self.h, L.dem_set_control(self.h, cc.ctypes.data_as(_IP)))
+
+    def break_events(self, cap=1 << 16):
+        L = lib()
+        buf = np.zeros(cap, dtype=BREAK_DTYPE)
+        n = C.c_int32(0)
+        _check(L, self.h, L.dem_break_events(self.h, buf.ctypes.data, cap, C.byref(n)))
+        return buf[: n.value].copy()
+
+    def stats(self):
+        L = lib()
+        s = Stats()
+        _check(L, self.h, L.dem_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in Stats._fields_ if k != "reserved"}
+
+    def stream(self):
+        return lib().dem_stream(self.h)
+
+    def broad_phase(self):
+        """(keys per particle, particle order, cell_start) of the current positions."""
+        L = lib()
+        nc = C.c_int32(0)
+        _check(L, self.h, L.dem_debug_broad_phase(self.h, None, None, None, C.byref(nc)))
+        keys = np.zeros(self.n, dtype=np.int32)
+        order = np.zeros(self.n, dtype=np.int32)
+        cs = np.zeros(nc.value + 1, dtype=np.int32)
+        _check(L, self.h, L.dem_debug_broad_phase(self.h, keys.ctypes.data_as(_IP),
+                                                  order.ctypes.data_as(_IP), cs.ctypes.data_as(_IP),
+                                                  C.byref(nc)))
+        return keys, order, cs
+
+    def search_grid(self):
+        L = lib()
+        x0, y0, inv = C.c_float(), C.c_float(), C.c_float()
+        gw, gh = C.c_int32(), C.c_int32()
+        _check(L, self.h, L.dem_debug_search_grid(self.h, C.byref(x0), C.byref(y0), C.byref(inv),
+                                                  C.byref(gw), C.byref(gh)))
+        return x0.value, y0.value, inv.value, gw.value, gh.value
+
+
+def grid_capacity(params, radii, particles):
+    L = lib()
+    r = np.ascontiguousarray(radii, dtype=np.float32)
+    g = GridInfo()
+    p = make_params(params)
+    rc = L.dem_grid_capacity(C.byref(p), r.ctypes.data_as(_FP), int(r.shape[0]), int(particles),
+                             C.byref(g))
+    if rc != 0:
+        raise DemError(rc, "grid_capacity")
+    return (g.cell_size, g.cell_cap, g.w, g.h)

@@ -1,0 +1,178 @@
+"""Scene setup for the DEM pipeline (the role of src/setup.rs, src/particle_def.rs
+and the scene-building half of src/state.rs), plus the seeded synthetic
+workloads the benchmark runs.
+
+Every builder returns (scene, params, ext) where `scene` is a dict of numpy
+arrays in the reference's host layouts (see dem.py), `params` the 29-word
+settings dict, and `ext` keyword arguments for dem.Context (extensions such as
+per-bond strengths).  Synthetic inputs stand in for the reference's saved
+scenes: shapes, sizes and value distributions follow the workload definitions
+quoted in each docstring.
+"""
+import numpy as np
+
+MAX_CONTACTS = 14
+
+
+def reference_defaults(particles):
+    """Settings::new (src/settings.rs:257-439) packed as collision_settings()."""
+    vert = np.float32(2.0)
+    return {
+        "walls": 1, "hor_bound": float(vert * np.float32(1.333)), "vert_bound": float(vert),
+        "round_bounds": 0, "bound_radius": 1.0, "wall_friction": 0.0, "gravity": 1,
+        "planet_mode": 1, "bonds": 0, "collisions": 1, "friction_coefficient": 0.5,
+        "gravity_acc": 1.0, "bond_normal_stiffness": 10.0, "bonds_tear": 0,
+        "bond_normal_strength": 0.5, "contact_damping": 0.2, "bond_damping": 0.2, "drag": 1.0,
+        "bond_shear_strength": 0.5, "dT": float(np.float32(1.0 / 12600.0)),
+        "bond_shear_stiffness": 10.0, "gravity_x": 0.0, "gravity_y": 0.0, "mouse_gravity": 0,
+        "moment_contribution_factor": 1.0, "collision_interval": 1, "local_damping": 0,
+        "local_damping_alpha": 0.1, "particles": int(particles),
+    }
+
+
+def empty_scene(n, materials):
+    """A scene with n particles at rest, no contacts and no bonds (state.rs:98-118)."""
+    materials = np.ascontiguousarray(materials, dtype=np.float32).reshape(-1)
+    return {
+        "pos": np.zeros(2 * n, np.float32), "radii": np.zeros(n, np.float32),
+        "vel": np.zeros(2 * n, np.float32), "acc": np.zeros(2 * n, np.float32),
+        "rot": np.zeros(n, np.float32), "rot_vel": np.zeros(n, np.float32),
+        "rot_acc": np.zeros(n, np.float32), "forces": np.zeros(6 * n, np.float32),
+        "fixity": np.zeros(6 * n, np.int32), "del_pos": np.zeros(2 * n, np.float32),
+        "del_rot": np.zeros(n, np.float32), "bonds": np.full(1, -1, np.int32),
+        "contacts": np.full(6 * MAX_CONTACTS * n, -1, np.int32),
+        "material_pointers": np.zeros(n, np.int32), "materials": materials,
+        "data": np.zeros(7 * n, np.float32), "coll_cont": np.zeros(4, np.int32),
+        "grid": (0.0, 0, 0, 0),
+    }
+
+
+def grid_capacity(hor_bound, vert_bound, radii, particles):
+    """grid_capacity (wgpu_prog.rs:698-717) over the radii, float32 arithmetic."""
+    f = np.float32
+    rmax = f(radii.max()) if radii.size else f(0)
+    rmin = f(radii.min()) if radii.size else f(0)
+    variable = rmin != rmax
+    max_rad = rmax * f(2.0)
+    min_rad = rmin if variable else rmax
+    w = int(np.ceil(f(hor_bound) * f(2.0) / max_rad))
+    h = int(np.ceil(f(vert_bound) * f(2.0) / max_rad))
+    with np.errstate(divide="ignore", over="ignore"):
+        q = max_rad / min_rad + f(1.0)
+        capf = np.ceil(q * q)
+    cap = int(min(capf, 2147483647.0)) if np.isfinite(capf) else 2147483647
+    return (float(max_rad), min(cap, int(particles)) + 2, w, h)
+
+
+def _bond_record(dx, dy):
+    """Bond triple of regen_bonds (state.rs:308-314): status 1, atan2 angle, length."""
+    dx = np.float32(dx)
+    dy = np.float32(dy)
+    mag = np.float32(np.power(np.float32(dx * dx + dy * dy), np.float32(0.5)))
+    ang = np.float32(np.arctan2(np.float32(dx / mag), np.float32(dy / mag)))
+    return 1, int(np.array([ang], np.float32).view(np.int32)[0]), int(np.array([mag], np.float32).view(np.int32)[0])
+
+
+def add_chain_bonds(scene, chains):
+    """Bonds and bonded contact slots for particle chains whose consecutive
+    members are within 1.05 (r_i + r_j) and whose other pairs are not: the
+    output of regen_bonds (state.rs:291-367) for such a layout, built in
+    O(n).  `chains` is a list of index arrays in ascending order."""
+    pos = scene["pos"].reshape(-1, 2)
+    contacts = scene["contacts"].reshape(-1, MAX_CONTACTS, 6)
+    pairs = []
+    for ch in chains:
+        ch = np.asarray(ch)
+        pairs.extend(zip(ch[:-1].tolist(), ch[1:].tolist()))
+    pairs.sort()
+    bonds = np.zeros(3 * max(len(pairs), 1), np.int32)
+    nxt = np.zeros(pos.shape[0], np.int64)
+    for k, (i, j) in enumerate(pairs):
+        d = pos[j] - pos[i]
+        bonds[3 * k:3 * k + 3] = _bond_record(d[0], d[1])
+        for a, b in ((i, j), (j, i)):
+            s = nxt[a]
+            contacts[a, s] = [a, b, 0, 0, 0, k]
+            nxt[a] += 1
+    if not pairs:
+        bonds = np.full(1, -1, np.int32)
+    scene["bonds"] = bonds
+    scene["contacts"] = contacts.reshape(-1).copy()
+    return scene
+
+
+def c0_settle(n=4096, seed=0, box=(128.0, 256.0), spacing=None):
+    """Plain granular settle: n disks, radii U[0.8, 1.2] (r0 = 1), a jittered
+    square lattice (jitter U[-0.1, 0.1]) filling a 128 x 256 box with walls,
+    gravity -9.81 (planet mode off, gravity_acc 1), density 1, k_n = 1e5,
+    k_t = 0.5 k_n, friction 0.5, dt = 1e-4.  Wall restitution is the
+    reference's fixed 0.5 (2D_LOM.wgsl:110-126)."""
+    rng = np.random.default_rng(seed)
+    W, H = float(box[0]), float(box[1])
+    if spacing is None:
+        s0 = np.sqrt(W * H / n)
+        cols = int(np.floor(W / s0))
+        rows = int(np.ceil(n / cols))
+        spacing = min((W - 2.6) / cols, (H - 2.6) / rows)
+    else:
+        cols = max(int(np.floor((W - 2.6) / spacing)), 1)
+        rows = int(np.ceil(n / cols))
+    idx = np.arange(n)
+    cx = (idx % cols) - (cols - 1) / 2.0
+    cy = (idx // cols) - (rows - 1) / 2.0
+    pos = np.empty((n, 2), np.float64)
+    pos[:, 0] = cx * spacing + rng.uniform(-0.1, 0.1, n)
+    pos[:, 1] = cy * spacing + rng.uniform(-0.1, 0.1, n)
+    radii = rng.uniform(0.8, 1.2, n).astype(np.float32)
+    mats = [1, 1, 1, 1.0, 1e5, 5e4]
+    sc = empty_scene(n, mats)
+    sc["pos"] = pos.astype(np.float32).reshape(-1)
+    sc["radii"] = radii
+    p = reference_defaults(n)
+    p.update({"hor_bound": W, "vert_bound": H, "planet_mode": 0, "gravity": 1, "gravity_acc": 1.0,
+              "friction_coefficient": 0.5, "dT": 1e-4, "bonds": 0})
+    sc["grid"] = grid_capacity(W, H, radii, n)
+    return sc, p, {}
+
+
+def c1_chains(chains=64, length=256, seed=0, pull_velocity=0.1):
+    """Bonded chain tensile test: `chains` independent chains of `length` disks
+    of radius 1 at spacing 2 (touching), joined by parallel bonds (bond radius
+    factor 0.8, k_n = 1e5, k_s = 0.5 k_n, tensile and shear strengths Weibull
+    shape 8 scale 5e3 per bond); particle 0 of each chain fully fixed, the last
+    one pulled along x at 0.01 per 1e3 steps of dt = 1e-4 (velocity 0.1) with its
+    x DOF fixed; contacts as in c0_settle (no gravity)."""
+    rng = np.random.default_rng(seed)
+    n = chains * length
+    gap = 6.0  # > 2 search cells between chains
+    L = 2.0 * (length - 1)
+    pos = np.zeros((n, 2), np.float32)
+    for c in range(chains):
+        base = c * length
+        pos[base:base + length, 0] = (np.arange(length, dtype=np.float32) * np.float32(2.0)
+                                      - np.float32(L / 2.0))
+        pos[base:base + length, 1] = np.float32((c - (chains - 1) / 2.0) * gap)
+    sc = empty_scene(n, [1, 1, 1, 1.0, 1e5, 5e4])
+    sc["pos"] = pos.reshape(-1)
+    sc["radii"] = np.ones(n, np.float32)
+    add_chain_bonds(sc, [np.arange(c * length, (c + 1) * length) for c in range(chains)])
+    fix = sc["fixity"].reshape(-1, 6)
+    vel = sc["vel"].reshape(-1, 2)
+    for c in range(chains):
+        first, last = c * length, (c + 1) * length - 1
+        fix[first, :] = 1
+        fix[last, 0] = 1
+        fix[last, 3] = 1
+        vel[last, 0] = pull_velocity
+    W = L + 40.0
+    Hb = chains * gap + 20.0
+    nb = sc["bonds"].shape[0] // 3
+    strength = (5e3 * rng.weibull(8.0, size=(2, nb))).astype(np.float32)
+    p = reference_defaults(n)
+    p.update({"hor_bound": float(W), "vert_bound": float(Hb), "gravity": 0, "planet_mode": 0,
+              "bonds": 3, "bonds_tear": 1, "bond_normal_stiffness": 1e5,
+              "bond_shear_stiffness": 5e4, "bond_normal_strength": 5e3,
+              "bond_shear_strength": 5e3, "dT": 1e-4, "friction_coefficient": 0.5})
+    sc["grid"] = grid_capacity(W, Hb, sc["radii"], n)
+    ext = {"bond_lambda": 0.8, "bond_sn": strength[0], "bond_ss": strength[1]}
+    return sc, p, ext

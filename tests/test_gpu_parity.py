@@ -1,0 +1,208 @@
+"""GPU parity: the CUDA path against the CPU oracle on identical inputs.
+
+Both follow the reference's expressions with the same float rounding (no
+contraction on either side), and both resolve the reference's races the same
+way, so whole states are compared bit for bit: positions, velocities,
+accelerations, diagnostics, every contact record (pairs, slot positions,
+tangential histories) and every bond record, plus the bond-break event list.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import dem
+import dem_scenes
+import fbs_state
+import oracle
+import replay
+from gpu_backend import GpuBackend, assert_same_state, contact_pairs, copy_scene, run_both
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import build_lib
+    build_lib.build()
+
+
+def test_texps_replay_equals_oracle_and_golden(golden_dir):
+    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "TEXPS.bin"))
+    gb = GpuBackend(scene, uni, info["use_f64"])
+    gx = replay.Replayer(gb, info["scripts"], len(scene["radii"])).run()
+    ob = replay.OracleBackend(scene, uni, info["use_f64"])
+    ox = replay.Replayer(ob, info["scripts"], len(scene["radii"])).run()
+    traces = np.load(os.path.join(golden_dir, "traces.npz"))
+    assert set(gx) == set(ox)
+    for k in gx:
+        assert np.array_equal(gx[k], ox[k]), k
+    assert np.array_equal(gx["TEXP_1"][:, 7], traces["TEXP_1"][:, 7])
+
+
+def test_chain_texp_replay_equals_oracle(golden_dir):
+    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "Chain_TEXP.bin"))
+    gx = replay.Replayer(GpuBackend(scene, uni, info["use_f64"]), info["scripts"], 3).run()
+    ox = replay.Replayer(replay.OracleBackend(scene, uni, info["use_f64"]), info["scripts"], 3).run()
+    for k in ox:
+        assert np.array_equal(gx[k], ox[k]), k
+
+
+@pytest.mark.parametrize("n,steps", [(600, 400), (2000, 150)])
+def test_dense_settle_bit_exact(n, steps):
+    sc, p, ext = dem_scenes.c0_settle(n=n, seed=1, box=(60, 90), spacing=2.3)
+    g, o, _, _ = run_both(sc, p, steps, chunk=50, reorder_interval=7)
+    assert len(contact_pairs(o)) > n  # the scene is in contact
+    assert_same_state(g, o)
+
+
+def test_c0_default_scene_bit_exact():
+    sc, p, ext = dem_scenes.c0_settle(n=4096, seed=0)
+    g, o, _, _ = run_both(sc, p, 60)
+    assert_same_state(g, o)
+
+
+def test_chains_with_breaks_bit_exact():
+    sc, p, ext = dem_scenes.c1_chains(chains=6, length=40, seed=3, pull_velocity=20.0)
+    g, o, gev, oev = run_both(sc, p, 700, chunk=100, **ext)
+    assert len(oev) > 0, "the pull must break bonds"
+    assert_same_state(g, o)
+    got = sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in gev)
+    ref = sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in oev)
+    assert got == ref
+
+
+@pytest.mark.parametrize("model", [1, 2, 3])
+def test_bond_models_bit_exact(model):
+    sc, p, ext = dem_scenes.c1_chains(chains=3, length=24, seed=5, pull_velocity=8.0)
+    p = dict(p)
+    p["bonds"] = model
+    p["bond_normal_strength"] = 2e3 if model != 1 else 3e3
+    ext = {"bond_lambda": 0.8}
+    g, o, gev, oev = run_both(sc, p, 400, chunk=80, **ext)
+    assert_same_state(g, o)
+    assert len(gev) == len(oev)
+
+
+@pytest.mark.parametrize("variant", ["planet", "round_walls", "interval3", "f64", "fixity_mix"])
+def test_setting_variants_bit_exact(variant):
+    sc, p, ext = dem_scenes.c0_settle(n=500, seed=7, box=(50, 60), spacing=2.3)
+    p = dict(p)
+    kw = {}
+    if variant == "planet":
+        p["planet_mode"] = 1
+    elif variant == "round_walls":
+        p["round_bounds"] = 1
+        p["bound_radius"] = 26.0
+    elif variant == "interval3":
+        p["collision_interval"] = 3
+    elif variant == "f64":
+        kw["use_f64"] = True
+    elif variant == "fixity_mix":
+        fx = sc["fixity"].reshape(-1, 6)
+        fx[::7, 0] = 1
+        fx[::11, 1] = 1
+        fx[::5, 2] = 2
+        sc["vel"].reshape(-1, 2)[::7, 0] = 3.0
+        sc["forces"].reshape(-1, 6)[::13, :3] = [50.0, -20.0, 1.0]
+    g, o, _, _ = run_both(sc, p, 200, chunk=40, **kw)
+    assert_same_state(g, o, variant + ": ")
+
+
+def test_strings_scene_bit_exact(golden_dir):
+    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "Strings.bin"))
+    g, o, gev, oev = run_both(scene, uni, 300, chunk=60, use_f64=info["use_f64"])
+    assert_same_state(g, o)
+    assert len(gev) == len(oev)
+
+
+def test_broad_phase_keys_and_order():
+    sc, p, ext = dem_scenes.c0_settle(n=3000, seed=2, box=(80, 120), spacing=2.3)
+    with dem.Context(sc, p) as ctx:
+        ctx.step(25)
+        st = ctx.download()
+        keys, order, cs = ctx.broad_phase()
+        x0, y0, inv, gw, gh = ctx.search_grid()
+    pos = st["pos"].reshape(-1, 2)
+    f = np.float32
+    qx = np.floor((pos[:, 0] - f(x0)) * f(inv)).astype(np.int64)
+    qy = np.floor((pos[:, 1] - f(y0)) * f(inv)).astype(np.int64)
+    ref_keys = np.clip(qy, 0, gh - 1) * gw + np.clip(qx, 0, gw - 1)
+    ref_keys[st["radii"] == 0] = gw * gh
+    assert np.array_equal(keys, ref_keys)
+    ref_order = np.lexsort((np.arange(len(keys)), ref_keys))
+    assert np.array_equal(order, ref_order)
+    counts = np.bincount(ref_keys, minlength=gw * gh + 1)
+    assert np.array_equal(cs, np.concatenate([[0], np.cumsum(counts)]))
+
+
+def test_upload_download_roundtrip(golden_dir):
+    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "Strings.bin"))
+    with dem.Context(scene, uni, use_f64=info["use_f64"]) as ctx:
+        d = ctx.download()
+        for k in ("pos", "radii", "vel", "acc", "rot", "rot_vel", "rot_acc", "forces", "fixity",
+                  "del_pos", "del_rot", "bonds", "contacts", "material_pointers", "materials"):
+            assert np.array_equal(d[k].view(np.int32), scene[k].view(np.int32)), k
+        ctx.step(40)
+        mid = ctx.download()
+        ctx.upload(scene)
+        back = ctx.download()
+        assert np.array_equal(back["contacts"], scene["contacts"])
+        assert not np.array_equal(mid["pos"], scene["pos"])
+
+
+def test_set_properties_matches_oracle():
+    sc, p, ext = dem_scenes.c0_settle(n=400, seed=4, box=(40, 60), spacing=2.3)
+    o = copy_scene(sc)
+    sel = np.zeros(400, np.int32)
+    sel[10:30] = 1
+    words = np.zeros(28, np.int32)
+    words[[0, 3, 10, 6]] = 1
+    f = words.view(np.float32)
+    f[14] = 3.5
+    f[17] = -1.25
+    f[20] = 40.0
+    words[24] = 1
+    with dem.Context(sc, p) as ctx:
+        ctx.step(10)
+        oracle.step(o, p, 10)
+        gsel = ctx.set_properties(sel, words)
+        osel = oracle.set_properties(o, sel.copy(), words)
+        assert np.array_equal(gsel, osel)
+        ctx.step(30)
+        oracle.step(o, p, 30, step_base=10)
+        g = ctx.download()
+    assert_same_state(g, o)
+    assert np.array_equal(g["fixity"], o["fixity"]) and np.array_equal(g["forces"], o["forces"])
+
+
+def test_fp64_twin_error_is_reported():
+    """Per-particle FP32 accelerations of one step against the FP64 twin of the
+    same step, scaled by the particle's force magnitude (sum |F_n| + m g).  The
+    figure is reported; the bound only guards against gross errors, since FP32
+    positions of magnitude ~30 already carry ~2e-6 absolute rounding, i.e.
+    ~1e-3 of a 1e-3 overlap."""
+    sc, p, ext = dem_scenes.c0_settle(n=1500, seed=9, box=(60, 90), spacing=2.3)
+    with dem.Context(sc, p) as ctx:
+        ctx.step(30)
+        s30 = ctx.download()
+        ctx.step(1)
+        s31 = ctx.download()
+    twin = oracle.step_f64(s30, p, 1)
+    r = s30["radii"].astype(np.float64)
+    mass = np.pi * r * r
+    a32 = s31["acc"].reshape(-1, 2).astype(np.float64)
+    a64 = twin["acc"].reshape(-1, 2)
+    f_abs = np.abs(s31["data"].reshape(-1, 7)[:, 0]).astype(np.float64)
+    scale = (f_abs + mass * 9.81) / mass
+    err = np.linalg.norm(a32 - a64, axis=1) / scale
+    print("fp32 vs fp64 one-step acceleration error: max %.3g median %.3g" % (err.max(), np.median(err)))
+    assert np.median(err) < 1e-4
+    assert err.max() < 5e-2
+
+
+def test_zero_radius_and_empty_slots_edge_cases():
+    sc, p, ext = dem_scenes.c0_settle(n=300, seed=6, box=(40, 50), spacing=2.3)
+    sc["radii"][::17] = 0.0
+    g, o, _, _ = run_both(sc, p, 120, chunk=30)
+    assert_same_state(g, o)
