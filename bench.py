@@ -1,0 +1,376 @@
+"""Benchmark of the GB300 DEM step (prints one JSON line on rank 0).
+
+A bench "step" is one frame of the reference's compute(): `frame` simulation
+steps of LOM + Simulation over the whole scene (WGPUComputeProg::compute with
+gen_per_frame steps, src/wgpu_prog.rs:1420-1473; the reference default is
+105, src/settings.rs:322).  The metric is particle-steps/s = particles x
+simulation steps / device time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload c1_chains|c0_settle|dense_bed] [--frame F]
+
+--impl reference times the reference's algorithm on the host cores: the CPU
+restatement under oracle/ (the reference's own WGSL-through-wgpu step cannot
+run without a graphics stack), with every host thread, on a bounded sample of
+the same workload.  Under torchrun only rank 0 runs it.
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in ("physics-sim_gb300", "oracle"):
+    _q = os.path.join(ROOT, _p)
+    if _q not in sys.path:
+        sys.path.insert(0, _q)
+
+import numpy as np  # noqa: E402
+
+L2_BYTES = 129 * 1024 * 1024
+FLUSH_BYTES = 2 * L2_BYTES
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c1_chains")
+    ap.add_argument("--frame", type=int, default=105)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def build_workload(name):
+    import dem_scenes
+    if name == "c1_chains":
+        sc, p, ext = dem_scenes.c1_chains()
+        desc = {"workload": "c1 bonded chain tensile test", "chains": 64, "chain_length": 256,
+                "particles": 64 * 256, "bond_model": "parallel (bonds=3)", "bond_radius_factor": 0.8,
+                "bond_strengths": "Weibull(8, 5e3) per bond", "dt": 1e-4}
+    elif name == "c0_settle":
+        sc, p, ext = dem_scenes.c0_settle()
+        desc = {"workload": "c0 granular settle", "particles": 4096, "box": [128, 256], "dt": 1e-4}
+    elif name == "dense_bed":
+        n = 1 << 20
+        sc, p, ext = dem_scenes.dense_bed(n=n)
+        desc = {"workload": "dense bed (c0 particle model, packed)", "particles": n, "dt": 1e-4}
+    else:
+        raise SystemExit("unknown workload %s" % name)
+    return sc, p, ext, desc
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        self.p = None
+        self.marks = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def mark(self):
+        self.f.flush()
+        try:
+            self.marks.append(sum(1 for _ in open(self.f.name)))
+        except OSError:
+            self.marks.append(0)
+
+    def stop(self):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        self.f.flush()
+
+    def summary(self):
+        try:
+            lines = [l.strip() for l in open(self.f.name) if l.strip()]
+        except OSError:
+            lines = []
+        if len(self.marks) >= 2 and self.marks[1] > self.marks[0]:
+            window = lines[self.marks[0]:self.marks[1]]
+        else:
+            window = lines
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in window:
+            c = [x.strip() for x in l.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                mx = float(c[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if c[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        try:
+            os.unlink(self.f.name)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(workload):
+    """dram bytes per k_interact launch recorded from an ncu capture under profiles/."""
+    path = os.path.join(ROOT, "profiles", "k_interact_%s.md" % workload)
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+def slot_counts(st):
+    c = st["contacts"].reshape(-1, 6)
+    occ = c[:, 1] != -1
+    bonded = occ & (c[:, 5] >= 0)
+    return int((occ & ~bonded).sum()), int(bonded.sum())
+
+
+def cpu_baseline(sc, p, ext, seconds, frame):
+    """The oracle (reference-mode FP32 CPU restatement) on a bounded sample of
+    the same workload, all host threads."""
+    import oracle
+    okw = {}
+    if "bond_lambda" in ext:
+        okw["bond_lambda"] = ext["bond_lambda"]
+    if "bond_sn" in ext:
+        okw["bond_sn"], okw["bond_ss"] = ext["bond_sn"], ext["bond_ss"]
+    s = {k: (v.copy() if hasattr(v, "copy") else v) for k, v in sc.items()}
+    n = int(s["radii"].shape[0])
+    t0 = time.perf_counter()
+    oracle.step(s, p, 1, **okw)
+    t1 = time.perf_counter()
+    per = max(t1 - t0, 1e-6)
+    k = int(max(1, min(seconds / per, 50 * frame)))
+    t0 = time.perf_counter()
+    oracle.step(s, p, k, step_base=1, **okw)
+    dt = time.perf_counter() - t0
+    cores = os.cpu_count() or 1
+    return {"value": n * k / dt, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d consecutive steps of the %d-particle scene from its initial state "
+                      "(%.1f s, OpenMP over particles)" % (k, n, dt)}, n * k / dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sc, p, ext, desc = build_workload(args.workload)
+    import oracle
+    okw = {}
+    if "bond_lambda" in ext:
+        okw["bond_lambda"] = ext["bond_lambda"]
+    if "bond_sn" in ext:
+        okw["bond_sn"], okw["bond_ss"] = ext["bond_sn"], ext["bond_ss"]
+    n = int(sc["radii"].shape[0])
+    s = {k: (v.copy() if hasattr(v, "copy") else v) for k, v in sc.items()}
+    # bounded sample per bench step: enough simulation steps for ~1 s of CPU work
+    t0 = time.perf_counter()
+    oracle.step(s, p, 1, **okw)
+    per = max(time.perf_counter() - t0, 1e-6)
+    sub = int(max(1, min(args.frame, 1.0 / per)))
+    step_base = 1
+    for _ in range(args.warmup):
+        oracle.step(s, p, sub, step_base=step_base, **okw)
+        step_base += sub
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.step(s, p, sub, step_base=step_base, **okw)
+        step_base += sub
+    dt = time.perf_counter() - t0
+    value = n * sub * args.steps / dt
+    cores = os.cpu_count() or 1
+    cfg = dict(desc)
+    cfg.update({"frame_steps": args.frame, "sample_steps_per_bench_step": sub})
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": "%d steps per bench step, %d bench steps, all host threads" % (sub, args.steps)},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def scene_bytes(sc):
+    keys = ("pos", "radii", "vel", "acc", "rot", "rot_vel", "rot_acc", "forces", "fixity", "del_pos",
+            "del_rot", "bonds", "contacts", "material_pointers", "materials", "data")
+    return int(sum(sc[k].nbytes for k in keys))
+
+
+def run_ours(args):
+    import torch
+    import build_lib
+    import dem
+    build_lib.build()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sc, p, ext, desc = build_workload(args.workload)
+    n = int(sc["radii"].shape[0])
+    F = args.frame
+    ctx = dem.Context(sc, p, device=local, reorder_interval=21, **ext)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        ctx.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        ctx.step(F)
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    launches0 = ctx.stats()["kernel_launches"]
+    sampler.mark()
+    barrier()
+    evs = []
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))          # L2 flush between frames, outside the events
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.step(F)
+        e1.record(stream)
+        evs.append((e0, e1))
+    barrier()
+    wall = time.perf_counter() - wall0
+    sampler.mark()
+    launches = ctx.stats()["kernel_launches"] - launches0
+    sampler.stop()
+    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = n * F * args.steps * ws / (max_ms / 1e3)
+    clocks = sampler.summary()
+
+    # roofline pass: events around every k_interact launch, same stream, plain launches
+    ctx.kernel_timing(True)
+    ctx.step(2 * F)
+    int_ms, int_n = ctx.kernel_time("interact")
+    lom_ms, lom_n = ctx.kernel_time("lom")
+    bp_ms, bp_n = ctx.kernel_time("broad_phase")
+    ctx.kernel_timing(False)
+    st = ctx.download()
+    s_u, s_b = slot_counts(st)
+    alg_bytes = 12 * s_u + 36 * s_b + 56 * n
+    avg_s = (int_ms / max(int_n, 1)) / 1e3
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / avg_s / 1e9
+    traffic = profiled_traffic(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "kernel": "k_interact", "launch_us": avg_s * 1e6,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "slots_unbonded": s_u, "slots_bonded": s_b,
+                "lom_us": lom_ms / max(lom_n, 1) * 1e3, "broad_phase_us": bp_ms / max(bp_n, 1) * 1e3}
+
+    # end to end through the public API: restore from host arrays, one frame, update_state
+    import dem as _dem
+    host = {k: (v.copy() if hasattr(v, "copy") else v) for k, v in st.items()}
+    h2d = scene_bytes(host)
+    d2h = h2d
+    e2e_n = max(1, args.e2e_steps)
+    ctx.upload(host)
+    ctx.step(F)
+    ctx.download()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_n):
+        ctx.upload(host)
+        ctx.step(F)
+        out = ctx.download()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    del out, _dem
+    e2e = {"value": n * F * e2e_n * ws / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h,
+           "note": "dem_upload (restore) of the whole scene + dem_step(frame) + dem_download (update_state)"}
+
+    base = None
+    if rank == 0 and ws == 1:
+        base, _ = cpu_baseline(sc, p, ext, args.cpu_seconds, F)
+    cfg = dict(desc)
+    cfg.update({"frame_steps": F, "parallelism": "replicas" if ws > 1 else "single",
+                "l2": "flushed between frames (write of %d MiB on the stream, untimed)" % (FLUSH_BYTES >> 20),
+                "reorder_interval": 21, "graphs": True})
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg, "clocks": clocks, "roofline": roofline,
+            "e2e": e2e, "gpu_launches": int(launches), "wall_s": wall}
+    if base is not None:
+        line["cpu_baseline"] = base
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

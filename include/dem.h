@@ -140,6 +140,7 @@ typedef struct dem_stats {
     int64_t reorders;           /* particle reorders performed */
     int32_t device_error;       /* sticky device error bits, 0 = none */
     int32_t reserved;
+    int64_t kernel_launches;    /* kernels this library launched on the context's stream */
 } dem_stats;
 
 typedef struct dem_ctx dem_ctx;

@@ -27,6 +27,14 @@ int dem_debug_broad_phase(dem_ctx *ctx, int32_t *keys, int32_t *order, int32_t *
  * key = cy * gw + cx. */
 int dem_debug_search_grid(dem_ctx *ctx, float *x0, float *y0, float *inv, int32_t *gw, int32_t *gh);
 
+/* Kernel timing: while enabled, dem_step launches without CUDA graphs and
+ * brackets every launch of the named kernels with CUDA events on the
+ * context's stream.  dem_debug_kernel_time returns the summed device time
+ * (milliseconds) and launch count of one kernel ("interact", "lom",
+ * "broad_phase", "reorder", "end_step") since timing was enabled. */
+int dem_debug_kernel_timing(dem_ctx *ctx, int32_t enable);
+int dem_debug_kernel_time(dem_ctx *ctx, const char *kernel, double *total_ms, int64_t *launches);
+
 #ifdef __cplusplus
 }
 #endif

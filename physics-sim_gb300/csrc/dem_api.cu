@@ -226,4 +226,25 @@ int dem_debug_search_grid(dem_ctx *ctx, float *x0, float *y0, float *inv, int32_
     return DEM_OK;
 }
 
+int dem_debug_kernel_timing(dem_ctx *ctx, int32_t enable) {
+    CTX_GUARD(ctx);
+    ctx->world.set_timing(enable != 0);
+    return DEM_OK;
+}
+
+int dem_debug_kernel_time(dem_ctx *ctx, const char *kernel, double *total_ms, int64_t *launches) {
+    CTX_GUARD(ctx);
+    if (!kernel) return set_err(ctx, DEM_E_INVALID, "kernel is NULL");
+    static const char *names[5] = {"interact", "lom", "broad_phase", "reorder", "end_step"};
+    for (int k = 0; k < 5; ++k) {
+        if (std::strcmp(kernel, names[k]) == 0) {
+            long long n = 0;
+            int rc = ctx->world.kernel_time(k, total_ms, &n);
+            if (launches) *launches = n;
+            return world_rc(ctx, rc);
+        }
+    }
+    return set_err(ctx, DEM_E_INVALID, "unknown kernel name");
+}
+
 }  // extern "C"

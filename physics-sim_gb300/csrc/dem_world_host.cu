@@ -26,7 +26,12 @@ static inline float bits2f(int32_t i) {
     return f;
 }
 
-World::~World() { release(); }
+World::~World() {
+    set_timing(true);
+    set_timing(false);
+    drop_graphs();
+    release();
+}
 
 int World::fail(int code, const std::string &msg) {
     err = msg;
@@ -34,6 +39,7 @@ int World::fail(int code, const std::string &msg) {
 }
 
 void World::release() {
+    drop_graphs();
     for (void *p : owned) cudaFree(p);
     owned.clear();
     d = DevWorld{};
@@ -505,35 +511,162 @@ int World::set_control(int s, const int32_t cc[4]) {
     return push_par(s);
 }
 
+namespace {
+enum { T_INTERACT = 0, T_LOM = 1, T_BROAD = 2, T_REORDER = 3, T_END = 4 };
+}
+
+// record a start/stop event pair around `fn` when timing is on
+int World::timed(int kind, void (*fn)(World &), bool &ok) {
+    if (!timing) {
+        fn(*this);
+        return 0;
+    }
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        ok = false;
+        fn(*this);
+        return 0;
+    }
+    cudaEventRecord(a, stream);
+    fn(*this);
+    cudaEventRecord(b, stream);
+    timers[kind].ev.push_back(a);
+    timers[kind].ev.push_back(b);
+    return 0;
+}
+
+void World::set_timing(bool on) {
+    if (on && !timing) {
+        for (auto &t : timers) {
+            for (auto e : t.ev) cudaEventDestroy(e);
+            t.ev.clear();
+            t.ms = 0.0;
+            t.n = 0;
+        }
+    }
+    timing = on;
+}
+
+int World::kernel_time(int kind, double *ms, long long *n) {
+    if (kind < 0 || kind >= 5) return fail(DEM_E_INVALID, "unknown kernel");
+    CK(cudaStreamSynchronize(stream));
+    Timer &t = timers[kind];
+    for (size_t k = 0; k + 1 < t.ev.size(); k += 2) {
+        float x = 0.0f;
+        CK(cudaEventElapsedTime(&x, t.ev[k], t.ev[k + 1]));
+        t.ms += x;
+        t.n += 1;
+        cudaEventDestroy(t.ev[k]);
+        cudaEventDestroy(t.ev[k + 1]);
+    }
+    t.ev.clear();
+    if (ms) *ms = t.ms;
+    if (n) *n = t.n;
+    return DEM_OK;
+}
+
+void World::enqueue_step() {
+    bool ok = true;
+    timed(T_LOM, [](World &w) { launch_lom(w.d, w.block, w.stream); }, ok);
+    timed(T_BROAD, [](World &w) { launch_broad_phase(w.d, w.block, w.stream); }, ok);
+    launches += 6;
+    if (++steps_since_reorder >= reorder_interval) {
+        timed(T_REORDER, [](World &w) { launch_reorder(w.d, w.spare, w.block, w.stream); }, ok);
+        launches += 2;
+        std::swap(d.pr, spare.pr);
+        std::swap(d.vw, spare.vw);
+        std::swap(d.ac, spare.ac);
+        std::swap(d.dp, spare.dp);
+        std::swap(d.fx, spare.fx);
+        std::swap(d.d4, spare.d4);
+        std::swap(d.dF, spare.dF);
+        std::swap(d.meta, spare.meta);
+        std::swap(d.orig, spare.orig);
+        std::swap(d.smask, spare.smask);
+        std::swap(d.s_b, spare.s_b);
+        std::swap(d.s_bonded, spare.s_bonded);
+        std::swap(d.s_tf, spare.s_tf);
+        std::swap(d.s_btf, spare.s_btf);
+        std::swap(d.s_thb, spare.s_thb);
+        steps_since_reorder = 0;
+        reorders++;
+        parity ^= 1;
+    }
+    timed(T_INTERACT, [](World &w) { launch_interact(w.d, w.block, w.stream); }, ok);
+    timed(T_END, [](World &w) { launch_end_step(w.d, w.stream); }, ok);
+    launches += 2;
+    host_step++;
+}
+
+void World::drop_graphs() {
+    for (int k = 0; k < 2; ++k) {
+        if (graph[k]) cudaGraphExecDestroy(graph[k]);
+        graph[k] = nullptr;
+        graph_R[k] = 0;
+    }
+}
+
+// Launch one reorder period as a graph (capturing it the first time for the
+// current pointer parity).  Requires steps_since_reorder == 0.
+int World::launch_period() {
+    const int p = parity;
+    const int R = reorder_interval;
+    if (graph[p] && graph_R[p] == R) {
+        CK(cudaGraphLaunch(graph[p], stream));
+        launches += graph_launches[p];
+        // replay the host-side bookkeeping of the captured steps
+        for (int k = 0; k < R; ++k) {
+            if (++steps_since_reorder >= reorder_interval) {
+                std::swap(d.pr, spare.pr); std::swap(d.vw, spare.vw); std::swap(d.ac, spare.ac);
+                std::swap(d.dp, spare.dp); std::swap(d.fx, spare.fx); std::swap(d.d4, spare.d4);
+                std::swap(d.dF, spare.dF); std::swap(d.meta, spare.meta); std::swap(d.orig, spare.orig);
+                std::swap(d.smask, spare.smask); std::swap(d.s_b, spare.s_b);
+                std::swap(d.s_bonded, spare.s_bonded); std::swap(d.s_tf, spare.s_tf);
+                std::swap(d.s_btf, spare.s_btf); std::swap(d.s_thb, spare.s_thb);
+                steps_since_reorder = 0;
+                reorders++;
+                parity ^= 1;
+            }
+            host_step++;
+        }
+        return DEM_OK;
+    }
+    if (graph[p]) {
+        cudaGraphExecDestroy(graph[p]);
+        graph[p] = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    long long l0 = launches;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < R; ++k) enqueue_step();
+    graph_launches[p] = (int)(launches - l0);
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    graph[p] = ex;
+    graph_R[p] = R;
+    CK(cudaGraphLaunch(ex, stream));
+    return DEM_OK;
+}
+
 int World::step(int n_steps) {
     if (n_steps < 0) return fail(DEM_E_INVALID, "n_steps < 0");
-    for (int k = 0; k < n_steps; ++k) {
-        launch_lom(d, block, stream);
-        launch_broad_phase(d, block, stream);
-        if (++steps_since_reorder >= reorder_interval) {
-            launch_reorder(d, spare, block, stream);
-            std::swap(d.pr, spare.pr);
-            std::swap(d.vw, spare.vw);
-            std::swap(d.ac, spare.ac);
-            std::swap(d.dp, spare.dp);
-            std::swap(d.fx, spare.fx);
-            std::swap(d.d4, spare.d4);
-            std::swap(d.dF, spare.dF);
-            std::swap(d.meta, spare.meta);
-            std::swap(d.orig, spare.orig);
-            std::swap(d.smask, spare.smask);
-            std::swap(d.s_b, spare.s_b);
-            std::swap(d.s_bonded, spare.s_bonded);
-            std::swap(d.s_tf, spare.s_tf);
-            std::swap(d.s_btf, spare.s_btf);
-            std::swap(d.s_thb, spare.s_thb);
-            steps_since_reorder = 0;
-            reorders++;
+    int k = 0;
+    if (use_graphs && !timing && n_steps >= reorder_interval) {
+        while (k < n_steps && steps_since_reorder != 0) {
+            enqueue_step();
+            ++k;
         }
-        launch_interact(d, block, stream);
-        launch_end_step(d, stream);
-        host_step++;
+        while (n_steps - k >= reorder_interval) {
+            int rc = launch_period();
+            if (rc) return rc;
+            k += reorder_interval;
+        }
     }
+    for (; k < n_steps; ++k) enqueue_step();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     return DEM_OK;
@@ -740,6 +873,7 @@ int World::stats(dem_stats *out) {
     out->events = (int64_t)st[1];
     out->events_dropped = (int64_t)st[2];
     out->reorders = reorders;
+    out->kernel_launches = launches;
     out->device_error = e | (st[3] ? 1 : 0);
     return DEM_OK;
 }

@@ -83,6 +83,30 @@ class World {
     DevWorld spare{};
     std::vector<void *> owned;
     int steps_since_reorder = 0;
+    // CUDA graphs of one reorder period (R steps ending in a reorder), one per
+    // pointer parity (each reorder swaps the live and spare particle arrays)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_R[2] = {0, 0};
+    int parity = 0;
+    void enqueue_step();
+    void drop_graphs();
+    int launch_period();
+    int graph_launches[2] = {0, 0};
+
+  public:
+    bool use_graphs = true;
+    long long launches = 0;
+    // kernel timing (debug): event pairs per kernel kind, summed on demand
+    bool timing = false;
+    struct Timer {
+        std::vector<cudaEvent_t> ev;  // start/stop pairs
+        double ms = 0.0;
+        long long n = 0;
+    };
+    Timer timers[5];
+    int timed(int kind, void (*fn)(World &), bool &ok);
+    int kernel_time(int kind, double *ms, long long *n);
+    void set_timing(bool on);
 };
 
 }  // namespace demgb

@@ -80,7 +80,8 @@ class BreakEvent(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("capped", C.c_int64), ("events", C.c_int64),
                 ("events_dropped", C.c_int64), ("reorders", C.c_int64),
-                ("device_error", C.c_int32), ("reserved", C.c_int32)]
+                ("device_error", C.c_int32), ("reserved", C.c_int32),
+                ("kernel_launches", C.c_int64)]
 
 
 BREAK_DTYPE = np.dtype([("scene", "<i4"), ("step", "<i4"), ("bond", "<i4"), ("code", "<i4"),
@@ -91,7 +92,8 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_create", "dem_destroy", "dem_upload", "dem_set_params", "dem_set_materials",
            "dem_set_control", "dem_get_control", "dem_step", "dem_synchronize", "dem_download",
            "dem_set_properties", "dem_break_events", "dem_get_stats", "dem_stream",
-           "dem_debug_broad_phase", "dem_debug_search_grid"]
+           "dem_debug_broad_phase", "dem_debug_search_grid", "dem_debug_kernel_timing",
+           "dem_debug_kernel_time"]
 
 _lib = None
 
@@ -135,6 +137,9 @@ def lib(path=None):
     L.dem_stream.restype = C.c_void_p
     L.dem_debug_broad_phase.argtypes = [C.c_void_p, _IP, _IP, _IP, C.POINTER(C.c_int32)]
     L.dem_debug_search_grid.argtypes = [C.c_void_p, _FP, _FP, _FP, _IP, _IP]
+    L.dem_debug_kernel_timing.argtypes = [C.c_void_p, C.c_int32]
+    L.dem_debug_kernel_time.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_int64)]
     for name in SYMBOLS:
         if name not in ("dem_destroy", "dem_ext_defaults", "dem_last_error", "dem_stream",
                         "dem_abi_version"):
@@ -206,6 +211,9 @@ def make_scene(sc):
 
 def empty_like_scene(sc):
     out = {k: np.zeros_like(sc[k]) for k in F32_KEYS + I32_KEYS}
+    # a scene without bonds carries the placeholder record [-1] (state.rs:357-359)
+    if sc["bonds"].shape[0] < 3:
+        out["bonds"] = sc["bonds"].copy()
     out["coll_cont"] = np.zeros(4, dtype=np.int32)
     out["grid"] = sc["grid"]
     return out
@@ -312,6 +320,18 @@ class Context:
 
     def stream(self):
         return lib().dem_stream(self.h)
+
+    def kernel_timing(self, on):
+        L = lib()
+        _check(L, self.h, L.dem_debug_kernel_timing(self.h, 1 if on else 0))
+
+    def kernel_time(self, kernel):
+        """(total device ms, launches) of a kernel since kernel timing was enabled."""
+        L = lib()
+        ms = C.c_double(0.0)
+        n = C.c_int64(0)
+        _check(L, self.h, L.dem_debug_kernel_time(self.h, kernel.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
 
     def broad_phase(self):
         """(keys per particle, particle order, cell_start) of the current positions."""

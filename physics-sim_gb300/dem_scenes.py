@@ -176,3 +176,15 @@ def c1_chains(chains=64, length=256, seed=0, pull_velocity=0.1):
     sc["grid"] = grid_capacity(W, Hb, sc["radii"], n)
     ext = {"bond_lambda": 0.8, "bond_sn": strength[0], "bond_ss": strength[1]}
     return sc, p, ext
+
+
+def dense_bed(n, seed=0, spacing=2.05, aspect=1.0):
+    """A packed bed for contact-heavy runs: the c0_settle particle and material
+    model on a jittered square lattice of the given spacing (radii U[0.8, 1.2],
+    so about half of the lattice neighbours overlap from the first step),
+    walls just outside the lattice."""
+    cols = max(int(np.sqrt(n * aspect)), 1)
+    rows = int(np.ceil(n / cols))
+    W = cols * spacing + 2.6
+    H = rows * spacing + 2.6
+    return c0_settle(n=n, seed=seed, box=(W, H), spacing=spacing)

@@ -50,7 +50,7 @@ def test_chain_texp_replay_equals_oracle(golden_dir):
 
 @pytest.mark.parametrize("n,steps", [(600, 400), (2000, 150)])
 def test_dense_settle_bit_exact(n, steps):
-    sc, p, ext = dem_scenes.c0_settle(n=n, seed=1, box=(60, 90), spacing=2.3)
+    sc, p, ext = dem_scenes.dense_bed(n=n, seed=1)
     g, o, _, _ = run_both(sc, p, steps, chunk=50, reorder_interval=7)
     assert len(contact_pairs(o)) > n  # the scene is in contact
     assert_same_state(g, o)
@@ -182,7 +182,7 @@ def test_fp64_twin_error_is_reported():
     figure is reported; the bound only guards against gross errors, since FP32
     positions of magnitude ~30 already carry ~2e-6 absolute rounding, i.e.
     ~1e-3 of a 1e-3 overlap."""
-    sc, p, ext = dem_scenes.c0_settle(n=1500, seed=9, box=(60, 90), spacing=2.3)
+    sc, p, ext = dem_scenes.dense_bed(n=1500, seed=9)
     with dem.Context(sc, p) as ctx:
         ctx.step(30)
         s30 = ctx.download()
