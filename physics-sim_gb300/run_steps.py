@@ -1,0 +1,40 @@
+"""Step one of the benchmark workloads a fixed number of times (command-line
+counterpart of the reference's script action Advance, src/scripts.rs:334-337).
+
+    python physics-sim_gb300/run_steps.py --workload c1_chains --steps 80
+"""
+import argparse
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+import dem  # noqa: E402
+import dem_scenes  # noqa: E402
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="c1_chains")
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--particles", type=int, default=0)
+    ap.add_argument("--reorder", type=int, default=21)
+    a = ap.parse_args()
+    if a.workload == "c1_chains":
+        sc, p, ext = dem_scenes.c1_chains()
+    elif a.workload == "c0_settle":
+        sc, p, ext = dem_scenes.c0_settle()
+    elif a.workload == "dense_bed":
+        sc, p, ext = dem_scenes.dense_bed(n=a.particles or (1 << 20))
+    else:
+        raise SystemExit("unknown workload")
+    with dem.Context(sc, p, reorder_interval=a.reorder, **ext) as ctx:
+        ctx.step(a.steps)
+        ctx.synchronize()
+        print("ok", a.workload, len(sc["radii"]), "particles", a.steps, "steps", ctx.stats())
+
+
+if __name__ == "__main__":
+    main()
