@@ -194,6 +194,30 @@ int dem_get_stats(dem_ctx *ctx, dem_stats *out);
  * order their own work against the steps. */
 void *dem_stream(dem_ctx *ctx);
 
+/* Broad phase that allocates nothing.  No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc (a framework whose pool owns the
+ * device heap, an allocator that forbids it, a real-time loop that must not
+ * block on it) and so pass only buffers they own.  Inputs: d_pos_radius, n
+ * device float4 {x, y, radius, unused} (16-byte aligned); the search grid
+ * (cell of a position = floor((x - x0) * inv_cell), floor((y - y0) * inv_cell)
+ * clamped to gw x gh; key = cy * gw + cx; zero-radius particles get key
+ * gw * gh).  Outputs (device): d_keys [n], d_order [n] (particle indices in
+ * stable cell order), d_cell_start [gw * gh + 2].  Work is enqueued on
+ * `stream` (a cudaStream_t, NULL = default stream) and not waited for.
+ * Scratch is a fixed device array inside the library, held by every GPU that
+ * loads it until exit: at most DEM_NOALLOC_MAX_CELLS cells (gw * gh + 1),
+ * larger grids are rejected with DEM_E_CAPACITY.  All calls share that array
+ * and it keeps the last call's contents (each call clears what must start at
+ * zero), so calls that overlap on the GPU -- on different streams, or from
+ * different threads on one device -- race and must be serialised by the
+ * caller.  The first call on a device looks up the array's device address;
+ * make it before any stream capture.  Errors: dem_noalloc_last_error(). */
+#define DEM_NOALLOC_MAX_CELLS 262144
+int dem_broad_phase_noalloc(const float *d_pos_radius, int32_t n, float x0, float y0, float inv_cell,
+                            int32_t gw, int32_t gh, int32_t *d_keys, int32_t *d_order,
+                            int32_t *d_cell_start, void *stream);
+const char *dem_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -93,7 +93,7 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_set_control", "dem_get_control", "dem_step", "dem_synchronize", "dem_download",
            "dem_set_properties", "dem_break_events", "dem_get_stats", "dem_stream",
            "dem_debug_broad_phase", "dem_debug_search_grid", "dem_debug_kernel_timing",
-           "dem_debug_kernel_time"]
+           "dem_debug_kernel_time", "dem_broad_phase_noalloc", "dem_noalloc_last_error"]
 
 _lib = None
 
@@ -140,9 +140,13 @@ def lib(path=None):
     L.dem_debug_kernel_timing.argtypes = [C.c_void_p, C.c_int32]
     L.dem_debug_kernel_time.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double),
                                         C.POINTER(C.c_int64)]
+    L.dem_broad_phase_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_float,
+                                          C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]
+    L.dem_noalloc_last_error.restype = C.c_char_p
     for name in SYMBOLS:
         if name not in ("dem_destroy", "dem_ext_defaults", "dem_last_error", "dem_stream",
-                        "dem_abi_version"):
+                        "dem_abi_version", "dem_noalloc_last_error"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
