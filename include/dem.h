@@ -89,11 +89,16 @@ typedef struct dem_ext {
     const float *bond_normal_strength;/* optional per-bond strengths [n_bonds]; NULL = global setting */
     const float *bond_shear_strength;
     int32_t diagnostics;              /* 1: maintain data[7n] every step as the reference does */
-    int32_t reorder_interval;         /* steps between particle reorders by cell; 0 = library default */
+    int32_t reorder_interval;         /* steps per captured CUDA graph; 0 = library default (35) */
     int32_t block_size;               /* threads per block for particle kernels; 0 = default */
-    float search_cell_factor;         /* search-grid cell / (2 r_max); 0 = default 1.0 (minimum) */
+    float search_cell_factor;         /* search-grid cell / (2 r_max + skin); 0 = default 1.0 (minimum) */
     int32_t event_capacity;           /* break-event ring size; 0 = default */
-    int32_t reserved[7];
+    float list_skin;                  /* candidate-list skin / r_max; 0 = default 0.2.  Lists are rebuilt
+                                         when a particle moves beyond half the skin; results do not
+                                         depend on it */
+    int32_t plain_launches;           /* 1: no CUDA graphs (for profilers that cannot see kernels inside
+                                         graphs with conditional nodes) */
+    int32_t reserved[5];
 } dem_ext;
 
 /* One scene in the reference's host layouts (state.rs:69-93).  Arrays hold
@@ -137,10 +142,11 @@ typedef struct dem_stats {
     int64_t capped;             /* narrow phases that reached 14 contacts */
     int64_t events;             /* bond breaks recorded */
     int64_t events_dropped;     /* breaks beyond the event ring */
-    int64_t reorders;           /* particle reorders performed */
+    int64_t reorders;           /* rebuilds (cell sort, reorder by cell, candidate lists) */
     int32_t device_error;       /* sticky device error bits, 0 = none */
     int32_t reserved;
     int64_t kernel_launches;    /* kernels this library launched on the context's stream */
+    int64_t list_overflows;     /* particles whose candidates exceeded the list (searched the cells) */
 } dem_stats;
 
 typedef struct dem_ctx dem_ctx;

@@ -71,15 +71,18 @@ struct Acc3 {
 };
 
 // linear_model (2D_Simulation.wgsl:338-373)
-__device__ __forceinline__ F3 linear_model(const ScenePar &P, const Mat &A, const Mat &B, float4 pa,
+// kns = {1/(1/kn_a + 1/kn_b), 1/(1/ks_a + 1/ks_b)} of the two materials
+// (2D_Simulation.wgsl:345-346), evaluated once per material pair on the host
+// with the same float operations
+__device__ __forceinline__ F3 linear_model(const ScenePar &P, float2 kns, float4 pa,
                                            float4 da, float4 pb, float4 db, float length, float &tf,
                                            Acc3 &acc) {
     F3 out = {0.0f, 0.0f, 0.0f};
     float d2 = distance2(P.use_f64, pa, pb, length);
     float nd = d2 < 0.0f ? d2 : 0.0f;
     if (nd == 0.0f) return out;
-    float kn = 1.0f / (1.0f / A.kn + 1.0f / B.kn);
-    float ks = 1.0f / (1.0f / A.ks + 1.0f / B.ks);
+    float kn = kns.x;
+    float ks = kns.y;
     float Fn = (-nd) * kn;
     float vx = pa.x - pb.x, vy = pa.y - pb.y;
     float L = len2f(vx, vy);
@@ -134,22 +137,35 @@ __device__ __forceinline__ void record_break(const DevWorld &w, const ScenePar &
 }
 
 // ------------------------------------------------------------ LOM kernel
-// 2D_LOM.wgsl:80-152 per particle; then the particle's search-cell key and
-// the histogram count for the counting sort (replaces the atomic bucket
-// insertion of 2D_LOM.wgsl:165-199).
-__global__ void __launch_bounds__(256) k_lom(DevWorld w) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.N) return;
+// Last-block election: after the block's writes are fenced, one thread takes
+// a ticket; the block holding the final ticket sees every other block's writes.
+// Last-warp election: after a warp's writes are fenced, lane 0 takes a
+// ticket; the warp holding the final ticket sees every other warp's writes.
+// Warps never wait for each other (no block barrier).
+__device__ __forceinline__ bool last_warp(uint32_t *ticket) {
+    __syncwarp();
+    uint32_t t = 0;
+    if ((threadIdx.x & 31) == 0) {
+        __threadfence();
+        t = atomicAdd(ticket, 1u);
+    }
+    t = __shfl_sync(0xffffffffu, t, 0);
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    const bool last = (t == warps - 1);
+    if (last) __threadfence();
+    return last;
+}
+
+// 2D_LOM.wgsl:80-152 per particle, plus the candidate-list validity check:
+// a particle that moved more than half the skin since the last rebuild asks
+// for a rebuild before this step's Simulation pass.
+__device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     uint32_t m = w.meta[i];
     int s = (int)meta_scene(m);
     const ScenePar &P = w.par[s];
-    float4 p = w.pr[i];
     if (!P.active) return;
-    if (p.z == 0.0f) {                                            // :83
-        w.keys[i] = (uint32_t)P.dead_cell;
-        atomicAdd(&w.cell_count[P.dead_cell], 1);
-        return;
-    }
+    float4 p = w.pr[i];
+    if (p.z == 0.0f) return;                                       // :83
     const float dT = P.p.dT;
     float4 v = w.vw[i];
     float4 a = w.ac[i];
@@ -210,21 +226,45 @@ __global__ void __launch_bounds__(256) k_lom(DevWorld w) {
     w.pr[i] = p;
     w.vw[i] = make_float4(ivx, ivy, iw, v.w);                      // :151-152
     if (!ext) w.dp[i] = d;
-    int cx, cy;
-    search_xy(P, p.x, p.y, cx, cy);
-    uint32_t key = (uint32_t)(P.cell_base + cy * P.g_w + cx);
-    w.keys[i] = key;
-    atomicAdd(&w.cell_count[key], 1);
+    const float2 b = w.pbuild[i];
+    const float ex = p.x - b.x, ey = p.y - b.y;
+    if (!(ex * ex + ey * ey <= P.disp_limit2)) atomicOr(w.rebuild, 1);
 }
 
-// keys of the current positions without integrating (standalone broad phase,
-// the role of the unused 2D_Broad_Phase.wgsl:78-111)
-__global__ void __launch_bounds__(256) k_keys(DevWorld w) {
+__global__ void __launch_bounds__(256) k_lom(DevWorld w, int in_graph, cudaGraphConditionalHandle cond) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < w.N) lom_particle(w, i);
+    if (last_warp(&w.tickets[0])) {
+        if ((threadIdx.x & 31) == 0) {
+            int need = *(volatile int32_t *)w.rebuild;
+            if (in_graph) cudaGraphSetConditional(cond, need != 0 ? 1u : 0u);
+            w.tickets[0] = 0u;
+        }
+    }
+}
+
+void launch_lom(const DevWorld &w, int block, cudaStream_t st, bool in_graph,
+                cudaGraphConditionalHandle cond) {
+    if (w.N == 0) return;
+    k_lom<<<(w.N + block - 1) / block, block, 0, st>>>(w, in_graph ? 1 : 0, cond);
+}
+
+// ------------------------------------------------------------ broad phase
+// Every kernel of the rebuild takes a gate: when the gate word is 0 the
+// kernel returns at once (plain launches); inside a graph the whole rebuild
+// sits under a conditional node and the gate is always 1.
+__device__ __forceinline__ bool gated_off(const int32_t *gate) {
+    return gate != nullptr && *(volatile const int32_t *)gate == 0;
+}
+
+// search-cell key of every particle (zero-radius ones go to their scene's
+// dead cell) and the per-cell histogram
+__global__ void __launch_bounds__(256) k_keys(DevWorld w, const int32_t *gate) {
+    if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
     uint32_t m = w.meta[i];
     const ScenePar &P = w.par[meta_scene(m)];
-    if (!P.active) return;
     float4 p = w.pr[i];
     uint32_t key;
     if (p.z == 0.0f) {
@@ -238,17 +278,11 @@ __global__ void __launch_bounds__(256) k_keys(DevWorld w) {
     atomicAdd(&w.cell_count[key], 1);
 }
 
-void launch_keys(const DevWorld &w, int block, cudaStream_t st) {
+void launch_keys(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate) {
     if (w.N == 0) return;
-    k_keys<<<(w.N + block - 1) / block, block, 0, st>>>(w);
+    k_keys<<<(w.N + block - 1) / block, block, 0, st>>>(w, gate);
 }
 
-void launch_lom(const DevWorld &w, int block, cudaStream_t st) {
-    if (w.N == 0) return;
-    k_lom<<<(w.N + block - 1) / block, block, 0, st>>>(w);
-}
-
-// ---------------------------------------------------------- broad phase
 // Exclusive scan of the per-cell counts with warp-shuffle scans: each block
 // scans SCAN_TILE counts, a single block scans the tile sums, a third pass
 // adds the tile offsets.
@@ -287,7 +321,9 @@ __device__ __forceinline__ int block_excl_scan(int v, int *total) {
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(const int32_t *__restrict__ in,
                                                              int32_t *__restrict__ out, int n,
-                                                             int32_t *__restrict__ tile_sums) {
+                                                             int32_t *__restrict__ tile_sums,
+                                                             const int32_t *gate) {
+    if (gated_off(gate)) return;
     __shared__ int total;
     int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
     int v[SCAN_PER_THREAD];
@@ -310,7 +346,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(const int32_t *__re
 
 // single block: exclusive scan of the tile sums in place; writes the grand total to out[n]
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(int32_t *tile_sums, int ntiles,
-                                                            int32_t *out, int n) {
+                                                            int32_t *out, int n, const int32_t *gate) {
+    if (gated_off(gate)) return;
     __shared__ int total;
     int carry = 0;
     for (int base = 0; base < ntiles; base += SCAN_THREADS) {
@@ -325,7 +362,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(int32_t *tile_sums, 
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_add(int32_t *out, int n,
-                                                           const int32_t *tile_sums) {
+                                                           const int32_t *tile_sums,
+                                                           const int32_t *gate) {
+    if (gated_off(gate)) return;
     int add = tile_sums[blockIdx.x];
     int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
 #pragma unroll
@@ -338,12 +377,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_add(int32_t *out, int n,
 int scan_tmp_size(int n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
 
 // scatter: slot = start + (count-1) taken by an atomic decrement, which also
-// returns every count to zero for the next step's histogram
-__global__ void __launch_bounds__(256) k_scatter(DevWorld w) {
+// returns every count to zero for the next histogram
+__global__ void __launch_bounds__(256) k_scatter(DevWorld w, const int32_t *gate) {
+    if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
-    uint32_t m = w.meta[i];
-    if (!w.par[meta_scene(m)].active) return;
     uint32_t key = w.keys[i];
     int slot = w.cell_start[key] + atomicSub(&w.cell_count[key], 1) - 1;
     w.sorted[slot] = i;
@@ -351,7 +389,8 @@ __global__ void __launch_bounds__(256) k_scatter(DevWorld w) {
 
 // in-cell ordering: each cell's members sorted by scene-local particle index,
 // so the cell lists equal a stable sort of the particles by cell key
-__global__ void __launch_bounds__(256) k_cell_order(DevWorld w) {
+__global__ void __launch_bounds__(256) k_cell_order(DevWorld w, const int32_t *gate) {
+    if (gated_off(gate)) return;
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= w.C) return;
     int beg = w.cell_start[c], end = w.cell_start[c + 1];
@@ -370,27 +409,29 @@ __global__ void __launch_bounds__(256) k_cell_order(DevWorld w) {
     }
 }
 
-int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st) {
+int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate) {
     if (w.N == 0) return 0;
     int ntiles = (w.C + SCAN_TILE - 1) / SCAN_TILE;
-    k_scan_tiles<<<ntiles, SCAN_THREADS, 0, st>>>(w.cell_count, w.cell_start, w.C, w.scan_tmp);
-    k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(w.scan_tmp, ntiles, w.cell_start, w.C);
-    k_scan_add<<<ntiles, SCAN_THREADS, 0, st>>>(w.cell_start, w.C, w.scan_tmp);
-    k_scatter<<<(w.N + block - 1) / block, block, 0, st>>>(w);
-    k_cell_order<<<(w.C + 255) / 256, 256, 0, st>>>(w);
+    k_scan_tiles<<<ntiles, SCAN_THREADS, 0, st>>>(w.cell_count, w.cell_start, w.C, w.scan_tmp, gate);
+    k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(w.scan_tmp, ntiles, w.cell_start, w.C, gate);
+    k_scan_add<<<ntiles, SCAN_THREADS, 0, st>>>(w.cell_start, w.C, w.scan_tmp, gate);
+    k_scatter<<<(w.N + block - 1) / block, block, 0, st>>>(w, gate);
+    k_cell_order<<<(w.C + 255) / 256, 256, 0, st>>>(w, gate);
     return 0;
 }
 
 // --------------------------------------------------------------- reorder
 // Permute every per-particle array into cell order (new i <- old sorted[i])
 // and remap partner indices; the cell lists become the identity.
-__global__ void __launch_bounds__(256) k_inverse(DevWorld w) {
+__global__ void __launch_bounds__(256) k_inverse(DevWorld w, const int32_t *gate) {
+    if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
     w.inv[w.sorted[i]] = i;
 }
 
-__global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o) {
+__global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o, const int32_t *gate) {
+    if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
     int src = w.sorted[i];
@@ -414,14 +455,103 @@ __global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o) {
         o.s_btf[j * N + i] = w.s_btf[j * N + src];
         o.s_thb[j * N + i] = w.s_thb[j * N + src];
     }
-    w.sorted[i] = i;  // safe: every thread read its own sorted[i] above; inv is read for b
+    w.sorted[i] = i;  // safe: each thread read only its own sorted[i]
 }
 
-void launch_reorder(DevWorld &w, DevWorld &spare, int block, cudaStream_t st) {
+// copy the permuted arrays back, so the live arrays keep their addresses
+// (a rebuild may or may not run in a given step; addresses captured in a
+// CUDA graph must not depend on it)
+__global__ void __launch_bounds__(256) k_copy_back(DevWorld w, DevWorld o, const int32_t *gate) {
+    if (gated_off(gate)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.N) return;
+    w.pr[i] = o.pr[i];
+    w.vw[i] = o.vw[i];
+    w.ac[i] = o.ac[i];
+    w.dp[i] = o.dp[i];
+    w.fx[i] = o.fx[i];
+    w.d4[i] = o.d4[i];
+    w.dF[i] = o.dF[i];
+    w.meta[i] = o.meta[i];
+    w.orig[i] = o.orig[i];
+    w.smask[i] = o.smask[i];
+    const int N = w.N;
+#pragma unroll 2
+    for (int j = 0; j < K; ++j) {
+        w.s_b[j * N + i] = o.s_b[j * N + i];
+        w.s_bonded[j * N + i] = o.s_bonded[j * N + i];
+        w.s_tf[j * N + i] = o.s_tf[j * N + i];
+        w.s_btf[j * N + i] = o.s_btf[j * N + i];
+        w.s_thb[j * N + i] = o.s_thb[j * N + i];
+    }
+}
+
+void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStream_t st,
+                    const int32_t *gate) {
     if (w.N == 0) return;
     int g = (w.N + block - 1) / block;
-    k_inverse<<<g, block, 0, st>>>(w);
-    k_gather<<<g, block, 0, st>>>(w, spare);
+    k_inverse<<<g, block, 0, st>>>(w, gate);
+    k_gather<<<g, block, 0, st>>>(w, spare, gate);
+    k_copy_back<<<g, block, 0, st>>>(w, spare, gate);
+}
+
+// ------------------------------------------------------- candidate lists
+// After the reorder, each particle collects the particles of the 3x3 search
+// cells around it whose centres lie within ra + rb + skin: a superset of
+// every pair the reference can accept while no particle moves more than
+// skin/2.  More than NL candidates: the particle searches the cell table
+// (built in the same rebuild) at every step instead.
+__global__ void __launch_bounds__(256) k_list_build(DevWorld w, const int32_t *gate) {
+    if (gated_off(gate)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.N) return;
+    const uint32_t m = w.meta[i];
+    const ScenePar &P = w.par[meta_scene(m)];
+    const float4 pa = w.pr[i];
+    w.pbuild[i] = make_float2(pa.x, pa.y);
+    if (!P.active || pa.z == 0.0f) {
+        w.nl_count[i] = 0;
+        w.kbuild[i] = (uint32_t)P.dead_cell;
+        return;
+    }
+    int gx, gy;
+    search_xy(P, pa.x, pa.y, gx, gy);
+    w.kbuild[i] = (uint32_t)(P.cell_base + gy * P.g_w + gx);
+    const int N = w.N;
+    const int cy0 = max(gy - 1, 0), cy1 = min(gy + 1, P.g_h - 1);
+    const int cx0 = max(gx - 1, 0), cx1 = min(gx + 1, P.g_w - 1);
+    int cnt = 0;
+    bool over = false;
+    for (int cy = cy0; cy <= cy1; ++cy) {
+        const int row = P.cell_base + cy * P.g_w;
+        const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
+        for (int k = beg; k < end; ++k) {
+            const int b = w.sorted[k];
+            if (b == i) continue;
+            const float4 pb = w.pr[b];
+            if (pb.z == 0.0f) continue;
+            const float dx = pb.x - pa.x, dy = pb.y - pa.y;
+            const float t = (pa.z + pb.z + P.skin) * 1.00001f;
+            if (dx * dx + dy * dy > t * t) continue;
+            if (cnt < NL) w.nl_items[cnt * N + i] = b;
+            else over = true;
+            ++cnt;
+        }
+    }
+    w.nl_count[i] = over ? NL_OVERFLOW : cnt;
+    if (over) atomicAdd(&w.stats[5], 1ull);
+}
+
+__global__ void k_rebuild_done(DevWorld w, const int32_t *gate) {
+    if (gated_off(gate)) return;
+    *w.rebuild = 0;
+    w.stats[4] += 1ull;
+}
+
+void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate) {
+    if (w.N == 0) return;
+    k_list_build<<<(w.N + block - 1) / block, block, 0, st>>>(w, gate);
+    k_rebuild_done<<<1, 1, 0, st>>>(w, gate);
 }
 
 // -------------------------------------------------------------- interact
@@ -431,28 +561,60 @@ void launch_reorder(DevWorld &w, DevWorld &spare, int block, cudaStream_t st) {
 // with the particle's AABB (both inserted into every bucket their AABB covers,
 // 2D_LOM.wgsl:180-199) and |p_b - p_a| < r_b + r_a; it stops at 14 and keeps
 // them in bucket-scan order (rows top to bottom, columns left to right,
-// bucket members in insertion order).  Here candidates come from the 3x3
-// search cells around the particle, the same acceptance test is evaluated
-// exactly, and accepted partners are ordered by (first shared bucket in scan
-// order, particle index) -- the bucket-scan order with insertion in index
-// order -- keeping the first 14.
-__device__ __forceinline__ void top14_insert(unsigned long long key, int idx, unsigned long long *ck,
-                                             int *ci, int &cnt) {
-    if (cnt == K && key >= ck[K - 1]) return;
-    int pos = cnt < K ? cnt : K - 1;
-    while (pos > 0 && ck[pos - 1] > key) {
-        ck[pos] = ck[pos - 1];
-        ci[pos] = ci[pos - 1];
+// bucket members in insertion order).  Here candidates come from the
+// particle's candidate list (or the 3x3 cells of the last rebuild), the same
+// acceptance test is evaluated exactly, and accepted partners are ordered by
+// (first shared bucket in scan order, particle index) -- the bucket-scan
+// order with insertion in index order -- keeping the first 14.
+constexpr int IB = 128;  // threads per k_interact block
+
+// The accepted partners of one thread, kept sorted by (first shared bucket,
+// particle index) in shared memory (slot-major, so a warp's accesses fall in
+// distinct banks): key = rank << 28 | scene-local index.
+struct Narrow {
+    uint32_t *ck;  // [K][IB]
+    int *ci;       // [K][IB]
+    int cnt;
+};
+
+__device__ __forceinline__ void top14_insert(uint32_t key, int idx, Narrow &nr) {
+    const int t = threadIdx.x;
+    if (nr.cnt == K && key >= nr.ck[(K - 1) * IB + t]) return;
+    int pos = nr.cnt < K ? nr.cnt : K - 1;
+    while (pos > 0 && nr.ck[(pos - 1) * IB + t] > key) {
+        nr.ck[pos * IB + t] = nr.ck[(pos - 1) * IB + t];
+        nr.ci[pos * IB + t] = nr.ci[(pos - 1) * IB + t];
         --pos;
     }
-    ck[pos] = key;
-    ci[pos] = idx;
-    if (cnt < K) ++cnt;
+    nr.ck[pos * IB + t] = key;
+    nr.ci[pos * IB + t] = idx;
+    if (nr.cnt < K) ++nr.cnt;
 }
 
-__global__ void __launch_bounds__(128) k_interact(DevWorld w) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.N) return;
+__device__ __forceinline__ void narrow_test(const DevWorld &w, const ScenePar &P, int i, int b, float4 pa,
+                                            int ax0, int ax1, int ay0, int ay1, Narrow &nr) {
+    if (b == i) return;
+    const float4 pb = __ldg(&w.pr[b]);
+    const float dx = pb.x - pa.x, dy = pb.y - pa.y;
+    const float s2 = dx * dx + dy * dy;
+    const float t = pb.z + pa.z;
+    if (s2 > (t * t) * 1.000001f) return;                         // cannot pass the test below
+    if (!(sqrtf(s2) < t)) return;                                  // :159
+    int bx0, bx1, by0, by1;
+    ref_range(P, pb.x, pb.y, pb.z, bx0, bx1, by0, by1);
+    if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) return;
+    const int fy = by0 > ay0 ? by0 : ay0;
+    const int fx = bx0 > ax0 ? bx0 : ax0;
+    unsigned rank = (unsigned)((fy - ay0) * (ax1 - ax0 + 1) + (fx - ax0));
+    if (rank > 15u) {           // AABB wider than 4 buckets: the bucket grid is smaller than 2 r
+        atomicOr(w.err, 2);
+        rank = 15u;
+    }
+    const uint32_t key = (rank << 28) | (uint32_t)__ldg(&w.orig[b]);
+    top14_insert(key, b, nr);
+}
+
+__device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr) {
     const uint32_t m = w.meta[i];
     const int s = (int)meta_scene(m);
     const ScenePar &P = w.par[s];
@@ -462,93 +624,72 @@ __global__ void __launch_bounds__(128) k_interact(DevWorld w) {
         w.dF[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return;
     }
-    const long long step = *w.step;
     const int N = w.N;
     const float4 da = w.dp[i];
     const Mat MA = w.mats[P.mat_base + meta_mat(m)];
     uint32_t mask = w.smask[i];
-    int sb[K];
-#pragma unroll
-    for (int j = 0; j < K; ++j) sb[j] = (mask >> j) & 1u ? w.s_b[j * N + i] : -1;
+    const int bonds_model = P.p.bonds;
 
-    const bool detect = P.p.collisions == 1 &&
-                        detect_at(P.p.collision_interval, P.cc1_0, step - P.step0);
+    const bool detect = P.p.collisions == 1 && w.det[s] != 0;
     if (detect) {                                                  // :126-228
-        unsigned long long ck[K];
-        int ci[K];
-        int cnt = 0;
+        nr.cnt = 0;
         int ax0, ax1, ay0, ay1;
         ref_range(P, pa.x, pa.y, pa.z, ax0, ax1, ay0, ay1);
-        const int awidth = ax1 - ax0 + 1;
-        int gx, gy;
-        search_xy(P, pa.x, pa.y, gx, gy);
-        const int R = P.stencil;
-        const int cy0 = max(gy - R, 0), cy1 = min(gy + R, P.g_h - 1);
-        const int cx0 = max(gx - R, 0), cx1 = min(gx + R, P.g_w - 1);
-        for (int cy = cy0; cy <= cy1; ++cy) {
-            const int row = P.cell_base + cy * P.g_w;
-            const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
-            for (int k = beg; k < end; ++k) {
-                const int b = w.sorted[k];
-                if (b == i) continue;
-                const float4 pb = w.pr[b];
-                const float dx = pb.x - pa.x, dy = pb.y - pa.y;
-                if (!(len2f(dx, dy) < pb.z + pa.z)) continue;      // :159
-                int bx0, bx1, by0, by1;
-                ref_range(P, pb.x, pb.y, pb.z, bx0, bx1, by0, by1);
-                if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) continue;
-                const int fy = by0 > ay0 ? by0 : ay0;
-                const int fx = bx0 > ax0 ? bx0 : ax0;
-                const unsigned rank = (unsigned)((fy - ay0) * awidth + (fx - ax0));
-                const unsigned long long key =
-                    ((unsigned long long)rank << 32) | (unsigned)w.orig[b];
-                        top14_insert(key, b, ck, ci, cnt);
+        const int lc = w.nl_count[i];
+        if (lc != NL_OVERFLOW) {
+            for (int k = 0; k < lc; ++k) narrow_test(w, P, i, __ldg(&w.nl_items[k * N + i]), pa, ax0, ax1, ay0, ay1, nr);
+        } else {
+            const int local = (int)w.kbuild[i] - P.cell_base;
+            const int gx = local % P.g_w, gy = local / P.g_w;
+            const int cy0 = max(gy - 1, 0), cy1 = min(gy + 1, P.g_h - 1);
+            const int cx0 = max(gx - 1, 0), cx1 = min(gx + 1, P.g_w - 1);
+            for (int cy = cy0; cy <= cy1; ++cy) {
+                const int row = P.cell_base + cy * P.g_w;
+                const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
+                for (int k = beg; k < end; ++k) narrow_test(w, P, i, w.sorted[k], pa, ax0, ax1, ay0, ay1, nr);
             }
         }
+        const int cnt = nr.cnt;
+        const int t = threadIdx.x;
         if (cnt == K) atomicAdd(&w.stats[0], 1ull);
         // delete contacts that were not found (:185-204)
-#pragma unroll
-        for (int j = 0; j < K; ++j) {
-            if (sb[j] == -1) continue;
+        for (uint32_t left = mask; left; left &= left - 1) {
+            const int j = __ffs(left) - 1;
+            const int sb = w.s_b[j * N + i];
             bool found = false;
-            for (int q = 0; q < cnt; ++q) found |= (ci[q] == sb[j]);
+            for (int q = 0; q < cnt; ++q) found |= (nr.ci[q * IB + t] == sb);
             if (found) continue;
             const int bonded = w.s_bonded[j * N + i];
-            if (bonded < 0 || P.p.bonds == 0) {
-                sb[j] = -1;
+            if (bonded < 0 || bonds_model == 0) {
                 mask &= ~(1u << j);
-            } else if (bonded > 0 && P.p.bonds <= 1) {
+            } else if (bonded > 0 && bonds_model <= 1) {
                 w.s_tf[j * N + i] = 0.0f;
             }
         }
         // create new contacts in the last empty slot (:207-227)
         for (int q = 0; q < cnt; ++q) {
-            const int c = ci[q];
+            const int c = nr.ci[q * IB + t];
             bool existing = false;
-#pragma unroll
-            for (int j = 0; j < K; ++j) existing |= (sb[j] == c);
+            for (uint32_t left = mask; left && !existing; left &= left - 1)
+                existing = w.s_b[(__ffs(left) - 1) * N + i] == c;
             if (existing) continue;
             const uint32_t empty = (~mask) & ((1u << K) - 1u);
             if (empty == 0u) continue;
             const int j = 31 - __clz(empty);
             mask |= 1u << j;
-#pragma unroll
-            for (int jj = 0; jj < K; ++jj)
-                if (jj == j) sb[jj] = c;
             w.s_b[j * N + i] = c;
             w.s_tf[j * N + i] = 0.0f;
         }
         w.smask[i] = mask;
     }
 
-    // force loop (:230-255)
+    // force loop (:230-255), slots in ascending order
+    const long long step = *w.step;
     float nfx = 0.0f, nfy = 0.0f, nm = 0.0f;
     Acc3 acc = {0.0f, 0.0f, 0.0f};
-    const int bonds_model = P.p.bonds;
-#pragma unroll 1
-    for (int j = 0; j < K; ++j) {
-        const int b = sb[j];
-        if (b == -1) continue;
+    for (uint32_t left = mask; left; left &= left - 1) {
+        const int j = __ffs(left) - 1;
+        const int b = w.s_b[j * N + i];
         int bonded = w.s_bonded[j * N + i];
         if (bonded >= 0) {
             const int st = w.b_status[P.bond_base + bonded];
@@ -557,13 +698,13 @@ __global__ void __launch_bounds__(128) k_interact(DevWorld w) {
                 bonded = st;
             }
         }
-        const float4 pb = w.pr[b];
-        const float4 db = w.dp[b];
-        const Mat MB = w.mats[P.mat_base + meta_mat(w.meta[b])];
+        const float4 pb = __ldg(&w.pr[b]);
+        const float4 db = __ldg(&w.dp[b]);
+        const float2 kns = __ldg(&w.pair[P.pair_base + (int)meta_mat(m) * P.n_mat + (int)meta_mat(__ldg(&w.meta[b]))]);
         F3 f = {0.0f, 0.0f, 0.0f};
         if (bonded < 0 || bonds_model == 0) {
             float tf = w.s_tf[j * N + i];
-            f = linear_model(P, MA, MB, pa, da, pb, db, pa.z + pb.z, tf, acc);
+            f = linear_model(P, kns, pa, da, pb, db, pa.z + pb.z, tf, acc);
             w.s_tf[j * N + i] = tf;
         } else {
             const int bg = P.bond_base + bonded;
@@ -618,7 +759,7 @@ __global__ void __launch_bounds__(128) k_interact(DevWorld w) {
                 acc.d1 = acc.d1 + btf;
                 acc.d2 = acc.d2 + M;
                 float tf = w.s_tf[j * N + i];
-                const F3 lm = linear_model(P, MA, MB, pa, da, pb, db, blen, tf, acc);
+                const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, tf, acc);
                 w.s_tf[j * N + i] = tf;
                 f.x = Fx + lm.x;
                 f.y = Fy + lm.y;
@@ -639,16 +780,15 @@ __global__ void __launch_bounds__(128) k_interact(DevWorld w) {
                     fy = 0.0f;
                 }
                 float tf = w.s_tf[j * N + i];
-                const F3 lm = linear_model(P, MA, MB, pa, da, pb, db, blen, tf, acc);
+                const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, tf, acc);
                 w.s_tf[j * N + i] = tf;
                 f.x = lm.x + fx;
                 f.y = lm.y + fy;
                 f.z = lm.z + 0.0f;
             } else if (bonds_model == 2) {                         // :375-417
                 const float nd = distance1(P.use_f64, pa, pb);
-                const float kb = P.p.bond_normal_stiffness, ksb = P.p.bond_shear_stiffness;
-                const float kn = 1.0f / (1.0f / kb + 1.0f / kb);
-                const float ks = 1.0f / (1.0f / ksb + 1.0f / ksb);
+                const float kn = P.kb2;
+                const float ks = P.ksb2;
                 float Fn = (-nd) * kn;
                 const float vx = pa.x - pb.x, vy = pa.y - pb.y;
                 const float L = len2f(vx, vy);
@@ -727,31 +867,49 @@ __global__ void __launch_bounds__(128) k_interact(DevWorld w) {
     w.dF[i] = make_float4(acc.d0, acc.d1, acc.d2, 0.0f);
 }
 
-void launch_interact(const DevWorld &w, int block, cudaStream_t st) {
-    if (w.N == 0) return;
-    (void)block;
-    k_interact<<<(w.N + 127) / 128, 128, 0, st>>>(w);
-}
-
-// ------------------------------------------------------------ end of step
-// Breaks of this step become visible (status = min code), the positions-set
-// flags clear (2D_Simulation.wgsl:258-261), the step counter advances.
-__global__ void __launch_bounds__(256) k_end_step(DevWorld w) {
-    uint32_t n = *w.pend_count;
+// End of step, run by the last block of k_interact: breaks of this step
+// become visible (status = min code), the positions-set flags clear
+// (2D_Simulation.wgsl:258-261), the step counter advances, and each scene's
+// narrow-phase flag for the next step is set.
+__device__ void end_of_step(const DevWorld &w) {
+    const int lane = threadIdx.x & 31;
+    uint32_t n = *(volatile uint32_t *)w.pend_count;
     if (n > w.pend_cap) n = w.pend_cap;
-    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+    for (uint32_t k = lane; k < n; k += 32) {
         Pending p = w.pend[k];
         atomicMin(&w.b_status[p.bond], p.code);
     }
-    for (int s = threadIdx.x; s < w.S; s += blockDim.x) w.cc3[s] = 0;
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    const long long next = *(volatile long long *)w.step + 1;
+    for (int s = lane; s < w.S; s += 32) {
+        w.cc3[s] = 0;
+        const ScenePar &P = w.par[s];
+        w.det[s] = detect_at(P.p.collision_interval, P.cc1_0, next - P.step0) ? 1 : 0;
+    }
+    __syncwarp();
+    if (lane == 0) {
         *w.pend_count = 0u;
-        *w.step = *w.step + 1;
+        *w.step = next;
+        w.tickets[1] = 0u;
     }
 }
 
-void launch_end_step(const DevWorld &w, cudaStream_t st) { k_end_step<<<1, 256, 0, st>>>(w); }
+__global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w) {
+    __shared__ uint32_t ck[K * IB];
+    __shared__ int ci[K * IB];
+    Narrow nr;
+    nr.ck = ck;
+    nr.ci = ci;
+    nr.cnt = 0;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < w.N) interact_particle(w, i, nr);
+    if (last_warp(&w.tickets[1])) end_of_step(w);
+}
+
+void launch_interact(const DevWorld &w, int block, cudaStream_t st) {
+    (void)block;
+    const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
+    k_interact<<<g, IB, 0, st>>>(w);
+}
 
 // ------------------------------------------------------- Set_Properties
 // Set_Properties.wgsl:68-90; selections are indexed by scene-local particle.

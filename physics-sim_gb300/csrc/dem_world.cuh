@@ -68,8 +68,15 @@ struct ScenePar {
     int32_t active;        // 0 = frozen (skipped by every kernel)
     int64_t step0;         // world step at which the scene's interval counter was cc1_0
     int32_t cc1_0;
+    int32_t pair_base;     // first entry of the scene's material-pair table
+    float kb2, ksb2;       // 1/(1/k + 1/k) of the bond stiffnesses (2D_Simulation.wgsl:378-379)
+    float skin;            // candidate-list skin: lists hold pairs within ra + rb + skin
+    float disp_limit2;     // (skin/2)^2 shrunk by a rounding margin: a move beyond it forces a rebuild
     int32_t pad0;
 };
+
+constexpr int NL = 16;               // candidate-list capacity per particle (SoA [NL][N])
+constexpr int32_t NL_OVERFLOW = 255; // count marking a particle that searches the cell table instead
 
 struct Event {
     int32_t scene, step, bond, code, a, b;
@@ -81,7 +88,7 @@ struct Pending {
 };
 
 struct DevWorld {
-    int32_t N, C, B, S, M;
+    int32_t N, C, B, S, M, MP;
     float4 *pr, *vw, *ac, *dp, *fx, *d4, *dF;
     uint32_t *meta;
     int32_t *orig;
@@ -92,6 +99,7 @@ struct DevWorld {
     float *b_length;
     float2 *b_str;
     Mat *mats;
+    float2 *pair;               // per scene and material pair: {1/(1/kn_a + 1/kn_b), 1/(1/ks_a + 1/ks_b)}
     ScenePar *par;
     int32_t *cc3;              // per scene "positions set externally" flag
     // broad phase
@@ -105,9 +113,17 @@ struct DevWorld {
     Event *ev;
     unsigned long long *ev_count;
     uint32_t ev_cap;
-    unsigned long long *stats;  // [0] capped, [1] events, [2] dropped, [3] pending overflow
+    unsigned long long *stats;  // [0] capped, [1] events, [2] dropped, [3] pending overflow, [4] rebuilds, [5] list overflows
     long long *step;            // device step counter
     int32_t *err;
+    // candidate lists (built at rebuilds)
+    int32_t *nl_count;          // [N] candidates, or NL_OVERFLOW
+    int32_t *nl_items;          // [NL][N] internal indices
+    float2 *pbuild;             // [N] position at the last rebuild
+    uint32_t *kbuild;           // [N] search cell at the last rebuild
+    int32_t *rebuild;           // 1 = the next rebuild body runs
+    uint32_t *tickets;          // [2] last-block counters of k_lom and k_interact
+    int32_t *det;               // [S] narrow phase runs in the current step
 };
 
 // ---- stateless detection schedule -----------------------------------------
@@ -132,12 +148,15 @@ __host__ __device__ inline int32_t cc1_after(int32_t interval, int32_t cc1_0, lo
 }
 
 // host launchers (dem_kernels.cu)
-void launch_lom(const DevWorld &w, int block, cudaStream_t st);
-void launch_keys(const DevWorld &w, int block, cudaStream_t st);
-int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st);
-void launch_reorder(DevWorld &w, DevWorld &spare, int block, cudaStream_t st);
+// LOM of one step; with in_graph its last block sets the rebuild conditional
+void launch_lom(const DevWorld &w, int block, cudaStream_t st, bool in_graph,
+                cudaGraphConditionalHandle cond);
+void launch_keys(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
+int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
+void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStream_t st,
+                    const int32_t *gate);
+void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
 void launch_interact(const DevWorld &w, int block, cudaStream_t st);
-void launch_end_step(const DevWorld &w, cudaStream_t st);
 void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
                            const int32_t *d_props, int block, cudaStream_t st);
 int scan_tmp_size(int n);

@@ -29,8 +29,8 @@ static inline float bits2f(int32_t i) {
 World::~World() {
     set_timing(true);
     set_timing(false);
-    drop_graphs();
     release();
+    if (side) cudaStreamDestroy(side);
 }
 
 int World::fail(int code, const std::string &msg) {
@@ -39,7 +39,7 @@ int World::fail(int code, const std::string &msg) {
 }
 
 void World::release() {
-    drop_graphs();
+    drop_graph();
     for (void *p : owned) cudaFree(p);
     owned.clear();
     d = DevWorld{};
@@ -59,11 +59,11 @@ static T *dalloc(std::vector<void *> &owned, size_t count, bool &ok) {
     return static_cast<T *>(p);
 }
 
-int World::alloc(int N, int C, int B, int S, int M, uint32_t ev_cap) {
+int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
     release();
     bool ok = true;
     DevWorld &w = d;
-    w.N = N; w.C = C; w.B = B; w.S = S; w.M = M;
+    w.N = N; w.C = C; w.B = B; w.S = S; w.M = M; w.MP = MP;
     auto particle_arrays = [&](DevWorld &x) {
         x.pr = dalloc<float4>(owned, N, ok);
         x.vw = dalloc<float4>(owned, N, ok);
@@ -86,6 +86,7 @@ int World::alloc(int N, int C, int B, int S, int M, uint32_t ev_cap) {
     w.b_length = dalloc<float>(owned, B, ok);
     w.b_str = dalloc<float2>(owned, B, ok);
     w.mats = dalloc<Mat>(owned, M, ok);
+    w.pair = dalloc<float2>(owned, MP, ok);
     w.par = dalloc<ScenePar>(owned, S, ok);
     w.cc3 = dalloc<int32_t>(owned, S, ok);
     w.keys = dalloc<uint32_t>(owned, N, ok);
@@ -100,9 +101,16 @@ int World::alloc(int N, int C, int B, int S, int M, uint32_t ev_cap) {
     w.ev_cap = ev_cap;
     w.ev = dalloc<Event>(owned, ev_cap, ok);
     w.ev_count = dalloc<unsigned long long>(owned, 1, ok);
-    w.stats = dalloc<unsigned long long>(owned, 4, ok);
+    w.stats = dalloc<unsigned long long>(owned, 6, ok);
     w.step = dalloc<long long>(owned, 1, ok);
     w.err = dalloc<int32_t>(owned, 1, ok);
+    w.nl_count = dalloc<int32_t>(owned, N, ok);
+    w.nl_items = dalloc<int32_t>(owned, (size_t)NL * N, ok);
+    w.pbuild = dalloc<float2>(owned, N, ok);
+    w.kbuild = dalloc<uint32_t>(owned, N, ok);
+    w.rebuild = dalloc<int32_t>(owned, 1, ok);
+    w.tickets = dalloc<uint32_t>(owned, 2, ok);
+    w.det = dalloc<int32_t>(owned, S, ok);
     spare = w;
     particle_arrays(spare);
     if (!ok) {
@@ -112,7 +120,9 @@ int World::alloc(int N, int C, int B, int S, int M, uint32_t ev_cap) {
     CK(cudaMemsetAsync(w.cell_count, 0, sizeof(int32_t) * (size_t)C, stream));
     CK(cudaMemsetAsync(w.pend_count, 0, sizeof(uint32_t), stream));
     CK(cudaMemsetAsync(w.ev_count, 0, sizeof(unsigned long long), stream));
-    CK(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), stream));
+    CK(cudaMemsetAsync(w.stats, 0, 6 * sizeof(unsigned long long), stream));
+    CK(cudaMemsetAsync(w.tickets, 0, 2 * sizeof(uint32_t), stream));
+    CK(cudaMemsetAsync(w.nl_count, 0, sizeof(int32_t) * (size_t)(N > 0 ? N : 1), stream));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int32_t), stream));
     CK(cudaMemsetAsync(w.cc3, 0, sizeof(int32_t) * (size_t)S, stream));
     CK(cudaMemcpyAsync(w.step, &host_step, sizeof(long long), cudaMemcpyHostToDevice, stream));
@@ -173,7 +183,8 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
     // search grid: centre-binned cells of side >= 2 r_max (1 + pad), covering the
     // walls (or the particles, whichever is smaller in cells)
     const dem_params &p = h.params;
-    float reach = std::max(2.0f * rmax, 1e-30f) * std::max(h.cell_factor, 1.0f);
+    h.skin = skin_factor * rmax;
+    float reach = std::max(2.0f * rmax + h.skin, 1e-30f) * std::max(h.cell_factor, 1.0f);
     double ex0, ex1, ey0, ey1;
     if (p.round_bounds == 0) {
         ex0 = -0.5 * p.hor_bound; ex1 = 0.5 * p.hor_bound;
@@ -198,7 +209,7 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
         span_y = (ey1 - ey0) + 2.0 * reach;
     }
     double qmax = std::max(span_x, span_y) / reach + 2.0;
-    double pad = 1e-5 + 8.0 * std::ldexp(1.0, -24) * qmax;
+    double pad = 3e-5 + 8.0 * std::ldexp(1.0, -24) * qmax;
     float gcs = (float)(reach * (1.0 + pad));
     int gw = (int)std::ceil(span_x / gcs) + 1;
     int gh = (int)std::ceil(span_y / gcs) + 1;
@@ -242,6 +253,33 @@ void World::fill_par(SceneHost &h) {
     P.active = h.active ? 1 : 0;
     P.step0 = h.step0;
     P.cc1_0 = h.cc1_0;
+    P.pair_base = h.pair_base;
+    {
+        const float kb = h.params.bond_normal_stiffness, ksb = h.params.bond_shear_stiffness;
+        P.kb2 = 1.0f / (1.0f / kb + 1.0f / kb);
+        P.ksb2 = 1.0f / (1.0f / ksb + 1.0f / ksb);
+    }
+    P.skin = h.skin;
+    const float half = 0.5f * h.skin * (1.0f - 1e-5f);
+    P.disp_limit2 = half * half;
+}
+
+// narrow-phase flags of the coming step, one per scene
+int World::push_det() {
+    std::vector<int32_t> det(sh.size());
+    for (size_t s = 0; s < sh.size(); ++s)
+        det[s] = detect_at(sh[s].params.collision_interval, sh[s].cc1_0, host_step - sh[s].step0) ? 1 : 0;
+    CK(cudaMemcpyAsync(d.det, det.data(), det.size() * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    return DEM_OK;
+}
+
+// the next step rebuilds the cell table, the particle order and the candidate lists
+int World::force_rebuild() {
+    int32_t one = 1;
+    CK(cudaMemcpyAsync(d.rebuild, &one, 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    return DEM_OK;
 }
 
 int World::push_par(int s) {
@@ -352,13 +390,36 @@ int World::stage_scene(int s, const dem_scene *sc) {
         CK(up(d.b_length + h.bond_base, len));
         CK(up(d.b_str + h.bond_base, str));
     }
-    // materials
-    std::vector<Mat> mats(h.n_mat);
-    for (int k = 0; k < h.n_mat; ++k) {
-        const float *mm = sc->materials + 6 * k;
+    CK(cudaStreamSynchronize(stream));
+    return push_materials(s);
+}
+
+// material records and the material-pair stiffness table of one scene:
+// 1/(1/k_a + 1/k_b) for normal and shear stiffness (2D_Simulation.wgsl:345-346),
+// in float arithmetic, division correctly rounded
+int World::push_materials(int s) {
+    SceneHost &h = sh[s];
+    const int M = h.n_mat;
+    std::vector<Mat> mats(M);
+    std::vector<float2> pair((size_t)M * M);
+    for (int k = 0; k < M; ++k) {
+        const float *mm = h.materials.data() + 6 * k;
         mats[k] = Mat{mm[3], mm[4], mm[5], 0.0f};
     }
-    CK(up(d.mats + h.mat_base, mats));
+    for (int a = 0; a < M; ++a)
+        for (int b = 0; b < M; ++b) {
+            volatile float kna = mats[a].kn, knb = mats[b].kn, ksa = mats[a].ks, ksb = mats[b].ks;
+            volatile float ia = 1.0f / kna, ib = 1.0f / knb;
+            volatile float sum = ia + ib;
+            volatile float kn = 1.0f / sum;
+            volatile float ja = 1.0f / ksa, jb = 1.0f / ksb;
+            volatile float sum2 = ja + jb;
+            volatile float ks = 1.0f / sum2;
+            pair[(size_t)a * M + b] = make_float2(kn, ks);
+        }
+    CK(cudaMemcpyAsync(d.mats + h.mat_base, mats.data(), M * sizeof(Mat), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.pair + h.pair_base, pair.data(), pair.size() * sizeof(float2),
+                       cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
     return DEM_OK;
 }
@@ -373,11 +434,14 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
         block = ext.block_size;
     }
     if (ext.reorder_interval < 0) return fail(DEM_E_INVALID, "reorder_interval < 0");
-    if (ext.reorder_interval > 0) reorder_interval = ext.reorder_interval;
+    if (ext.reorder_interval > 0) graph_steps = ext.reorder_interval;
+    if (ext.list_skin < 0.0f) return fail(DEM_E_INVALID, "list_skin < 0");
+    if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
+    use_graphs = ext.plain_launches == 0;
     if (!(ext.bond_lambda > 0.0f)) return fail(DEM_E_INVALID, "bond_lambda must be > 0");
     diagnostics = ext.diagnostics != 0;
     sh.assign(S, SceneHost{});
-    long long N = 0, C = 0, B = 0, M = 0;
+    long long N = 0, C = 0, B = 0, M = 0, MP = 0;
     for (int s = 0; s < S; ++s) {
         SceneHost &h = sh[s];
         h.params = params[s];
@@ -398,6 +462,7 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
         h.cell_base = (int)C;
         h.bond_base = (int)B;
         h.mat_base = (int)M;
+        h.pair_base = (int)MP;
         h.step0 = host_step;
         h.cc0_0 = scenes[s]->coll_cont[0];
         h.cc1_0 = scenes[s]->coll_cont[1];
@@ -406,11 +471,12 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
         C += h.n_cells;
         B += h.n_bonds;
         M += h.n_mat;
+        MP += (long long)h.n_mat * h.n_mat;
     }
     if (N > (1LL << 30) || C > (1LL << 31) - 2 || B > (1LL << 30))
         return fail(DEM_E_INVALID, "world too large");
     uint32_t ev_cap = ext.event_capacity > 0 ? (uint32_t)ext.event_capacity : 1u << 16;
-    int rc = alloc((int)N, (int)C, (int)B, S, (int)M, ev_cap);
+    int rc = alloc((int)N, (int)C, (int)B, S, (int)M, (int)MP, ev_cap);
     if (rc) return rc;
     for (int s = 0; s < S; ++s) {
         rc = stage_scene(s, scenes[s]);
@@ -421,8 +487,9 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
         CK(cudaMemcpyAsync(d.cc3 + s, &c3, 4, cudaMemcpyHostToDevice, stream));
     }
     CK(cudaStreamSynchronize(stream));
-    steps_since_reorder = 0;
-    return DEM_OK;
+    rc = push_det();
+    if (rc) return rc;
+    return force_rebuild();
 }
 
 int World::upload_scene(int s, const dem_scene *sc) {
@@ -448,7 +515,9 @@ int World::upload_scene(int s, const dem_scene *sc) {
     CK(cudaStreamSynchronize(stream));
     rc = stage_scene(s, sc);
     if (rc) return rc;
-    return push_par(s);
+    rc = push_par(s);
+    if (rc) return rc;
+    return force_rebuild();
 }
 
 int World::set_params(int s, const dem_params &p) {
@@ -468,7 +537,11 @@ int World::set_params(int s, const dem_params &p) {
     h.cc0_0 = cc[0];
     h.cc1_0 = cc[1];
     h.cc2_0 = cc[2];
-    return push_par(s);
+    int rc = push_par(s);
+    if (rc) return rc;
+    rc = push_det();
+    if (rc) return rc;
+    return geometry ? force_rebuild() : DEM_OK;
 }
 
 int World::set_materials(int s, const float *m, int n) {
@@ -476,11 +549,7 @@ int World::set_materials(int s, const float *m, int n) {
     SceneHost &h = sh[s];
     if (!m || n != h.n_mat) return fail(DEM_E_INVALID, "material count must stay the same");
     h.materials.assign(m, m + 6 * (size_t)n);
-    std::vector<Mat> mats(n);
-    for (int k = 0; k < n; ++k) mats[k] = Mat{m[6 * k + 3], m[6 * k + 4], m[6 * k + 5], 0.0f};
-    CK(cudaMemcpyAsync(d.mats + h.mat_base, mats.data(), n * sizeof(Mat), cudaMemcpyHostToDevice, stream));
-    CK(cudaStreamSynchronize(stream));
-    return DEM_OK;
+    return push_materials(s);
 }
 
 void World::control(int s, int32_t cc[4]) const {
@@ -508,31 +577,13 @@ int World::set_control(int s, const int32_t cc[4]) {
     h.cc2_0 = cc[2];
     int32_t c3 = cc[3];
     CK(cudaMemcpyAsync(d.cc3 + s, &c3, 4, cudaMemcpyHostToDevice, stream));
-    return push_par(s);
+    int rc = push_par(s);
+    if (rc) return rc;
+    return push_det();
 }
 
 namespace {
 enum { T_INTERACT = 0, T_LOM = 1, T_BROAD = 2, T_REORDER = 3, T_END = 4 };
-}
-
-// record a start/stop event pair around `fn` when timing is on
-int World::timed(int kind, void (*fn)(World &), bool &ok) {
-    if (!timing) {
-        fn(*this);
-        return 0;
-    }
-    cudaEvent_t a, b;
-    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
-        ok = false;
-        fn(*this);
-        return 0;
-    }
-    cudaEventRecord(a, stream);
-    fn(*this);
-    cudaEventRecord(b, stream);
-    timers[kind].ev.push_back(a);
-    timers[kind].ev.push_back(b);
-    return 0;
 }
 
 void World::set_timing(bool on) {
@@ -565,108 +616,135 @@ int World::kernel_time(int kind, double *ms, long long *n) {
     return DEM_OK;
 }
 
-void World::enqueue_step() {
-    bool ok = true;
-    timed(T_LOM, [](World &w) { launch_lom(w.d, w.block, w.stream); }, ok);
-    timed(T_BROAD, [](World &w) { launch_broad_phase(w.d, w.block, w.stream); }, ok);
-    launches += 6;
-    if (++steps_since_reorder >= reorder_interval) {
-        timed(T_REORDER, [](World &w) { launch_reorder(w.d, w.spare, w.block, w.stream); }, ok);
-        launches += 2;
-        std::swap(d.pr, spare.pr);
-        std::swap(d.vw, spare.vw);
-        std::swap(d.ac, spare.ac);
-        std::swap(d.dp, spare.dp);
-        std::swap(d.fx, spare.fx);
-        std::swap(d.d4, spare.d4);
-        std::swap(d.dF, spare.dF);
-        std::swap(d.meta, spare.meta);
-        std::swap(d.orig, spare.orig);
-        std::swap(d.smask, spare.smask);
-        std::swap(d.s_b, spare.s_b);
-        std::swap(d.s_bonded, spare.s_bonded);
-        std::swap(d.s_tf, spare.s_tf);
-        std::swap(d.s_btf, spare.s_btf);
-        std::swap(d.s_thb, spare.s_thb);
-        steps_since_reorder = 0;
-        reorders++;
-        parity ^= 1;
-    }
-    timed(T_INTERACT, [](World &w) { launch_interact(w.d, w.block, w.stream); }, ok);
-    timed(T_END, [](World &w) { launch_end_step(w.d, w.stream); }, ok);
-    launches += 2;
+// The rebuild body: cell keys, counting sort by cell, in-cell order, reorder
+// of the particle arrays into cell order, candidate lists.  `gate` is the
+// device word that says whether a rebuild is due (kernels return at once when
+// it is 0); inside a conditional graph node it is always 1.
+void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate) {
+    launch_keys(d, block, st, gate);
+    launch_broad_phase(d, block, st, gate);
+    launch_reorder(d, spare, block, st, gate);
+    launch_list_build(d, block, st, gate);
+    rebuild_kernels = 1 + 5 + 3 + 2;
+}
+
+// One step with plain launches; the rebuild kernels run every step and
+// return at once unless a particle moved beyond its skin.
+void World::enqueue_plain_step() {
+    auto rec = [&](int kind, bool begin) {
+        if (!timing) return;
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        cudaEventRecord(e, stream);
+        timers[kind].ev.push_back(e);
+        (void)begin;
+    };
+    rec(T_LOM, true);
+    launch_lom(d, block, stream, false, cudaGraphConditionalHandle{});
+    rec(T_LOM, false);
+    rec(T_BROAD, true);
+    enqueue_rebuild(stream, d.rebuild);
+    rec(T_BROAD, false);
+    rec(T_INTERACT, true);
+    launch_interact(d, block, stream);
+    rec(T_INTERACT, false);
+    launches += 2 + rebuild_kernels;
     host_step++;
 }
 
-void World::drop_graphs() {
-    for (int k = 0; k < 2; ++k) {
-        if (graph[k]) cudaGraphExecDestroy(graph[k]);
-        graph[k] = nullptr;
-        graph_R[k] = 0;
-    }
+void World::drop_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (graph1) cudaGraphExecDestroy(graph1);
+    graph = nullptr;
+    graph1 = nullptr;
+    graph_R = 0;
 }
 
-// Launch one reorder period as a graph (capturing it the first time for the
-// current pointer parity).  Requires steps_since_reorder == 0.
-int World::launch_period() {
-    const int p = parity;
-    const int R = reorder_interval;
-    if (graph[p] && graph_R[p] == R) {
-        CK(cudaGraphLaunch(graph[p], stream));
-        launches += graph_launches[p];
-        // replay the host-side bookkeeping of the captured steps
-        for (int k = 0; k < R; ++k) {
-            if (++steps_since_reorder >= reorder_interval) {
-                std::swap(d.pr, spare.pr); std::swap(d.vw, spare.vw); std::swap(d.ac, spare.ac);
-                std::swap(d.dp, spare.dp); std::swap(d.fx, spare.fx); std::swap(d.d4, spare.d4);
-                std::swap(d.dF, spare.dF); std::swap(d.meta, spare.meta); std::swap(d.orig, spare.orig);
-                std::swap(d.smask, spare.smask); std::swap(d.s_b, spare.s_b);
-                std::swap(d.s_bonded, spare.s_bonded); std::swap(d.s_tf, spare.s_tf);
-                std::swap(d.s_btf, spare.s_btf); std::swap(d.s_thb, spare.s_thb);
-                steps_since_reorder = 0;
-                reorders++;
-                parity ^= 1;
-            }
-            host_step++;
-        }
-        return DEM_OK;
-    }
-    if (graph[p]) {
-        cudaGraphExecDestroy(graph[p]);
-        graph[p] = nullptr;
+#define CKG(call)                                                                         \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            cudaGraph_t junk_ = nullptr;                                                  \
+            cudaStreamEndCapture(stream, &junk_);                                         \
+            if (junk_) cudaGraphDestroy(junk_);                                           \
+            return fail(DEM_E_CUDA, std::string("graph capture: ") + #call + ": " +        \
+                                        cudaGetErrorString(e_));                          \
+        }                                                                                 \
+    } while (0)
+
+// Capture R steps as one graph: per step the LOM kernel, a conditional node
+// whose body is the rebuild (its condition is set on the device by the LOM
+// kernel's last block), and the Simulation kernel.
+int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
+    if (!side) CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int kernels = 0;
+    for (int k = 0; k < R; ++k) {
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t g = nullptr;
+        CKG(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+        cudaGraphConditionalHandle h;
+        CKG(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+        launch_lom(d, block, stream, true, h);
+        const cudaGraphNode_t *deps = nullptr;
+        size_t ndeps = 0;
+        CKG(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeIf;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        CKG(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np));
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        CKG(cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        enqueue_rebuild(side, d.rebuild);
+        cudaGraph_t body_out = nullptr;
+        CKG(cudaStreamEndCapture(side, &body_out));
+        CKG(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        launch_interact(d, block, stream);
+        kernels += 2;
     }
     cudaGraph_t g = nullptr;
-    long long l0 = launches;
-    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < R; ++k) enqueue_step();
-    graph_launches[p] = (int)(launches - l0);
     cudaError_t e = cudaStreamEndCapture(stream, &g);
     if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     cudaGraphExec_t ex = nullptr;
     e = cudaGraphInstantiate(&ex, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    graph[p] = ex;
-    graph_R[p] = R;
-    CK(cudaGraphLaunch(ex, stream));
+    *out = ex;
+    *kernels_out = kernels;
     return DEM_OK;
 }
 
 int World::step(int n_steps) {
     if (n_steps < 0) return fail(DEM_E_INVALID, "n_steps < 0");
     int k = 0;
-    if (use_graphs && !timing && n_steps >= reorder_interval) {
-        while (k < n_steps && steps_since_reorder != 0) {
-            enqueue_step();
-            ++k;
-        }
-        while (n_steps - k >= reorder_interval) {
-            int rc = launch_period();
+    if (use_graphs && !timing && n_steps > 0) {
+        if (n_steps >= graph_steps && (!graph || graph_R != graph_steps)) {
+            if (graph) cudaGraphExecDestroy(graph);
+            graph = nullptr;
+            int rc = capture_graph(graph_steps, &graph, &graph_kernels);
             if (rc) return rc;
-            k += reorder_interval;
+            graph_R = graph_steps;
+        }
+        while (graph && n_steps - k >= graph_steps) {
+            CK(cudaGraphLaunch(graph, stream));
+            launches += graph_kernels;
+            host_step += graph_steps;
+            k += graph_steps;
+        }
+        if (k < n_steps && !graph1) {
+            int rc = capture_graph(1, &graph1, &graph1_kernels);
+            if (rc) return rc;
+        }
+        for (; k < n_steps; ++k) {
+            CK(cudaGraphLaunch(graph1, stream));
+            launches += graph1_kernels;
+            host_step += 1;
         }
     }
-    for (; k < n_steps; ++k) enqueue_step();
+    for (; k < n_steps; ++k) enqueue_plain_step();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     return DEM_OK;
@@ -812,6 +890,7 @@ int World::set_properties(int s, int32_t *selections, const int32_t *props) {
         if (props[13] == 1) h.material_ptr[i] = props[27];
         if (props[9] == 1) h.r_max = std::max(h.r_max, f[23]);
     }
+    if (any && (props[0] == 1 || props[1] == 1 || props[9] == 1)) return force_rebuild();
     return DEM_OK;
 }
 
@@ -838,8 +917,8 @@ int World::broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *c
     if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
     const SceneHost &h = sh[s];
     if (n_cells) *n_cells = h.n_cells;
-    launch_keys(d, block, stream);
-    launch_broad_phase(d, block, stream);
+    launch_keys(d, block, stream, nullptr);
+    launch_broad_phase(d, block, stream, nullptr);
     const int n = h.n, base = h.particle_base;
     std::vector<uint32_t> k(n);
     std::vector<int32_t> srt(n), orig(n), cs((size_t)h.n_cells + 1);
@@ -858,12 +937,13 @@ int World::broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *c
     }
     if (cell_start)
         for (size_t c = 0; c < cs.size(); ++c) cell_start[c] = cs[c] - base;
-    return DEM_OK;
+    // the cell table now describes the current positions, not the last rebuild
+    return force_rebuild();
 }
 
 int World::stats(dem_stats *out) {
     CK(cudaStreamSynchronize(stream));
-    unsigned long long st[4];
+    unsigned long long st[6];
     CK(cudaMemcpy(st, d.stats, sizeof st, cudaMemcpyDeviceToHost));
     int32_t e = 0;
     CK(cudaMemcpy(&e, d.err, 4, cudaMemcpyDeviceToHost));
@@ -872,8 +952,9 @@ int World::stats(dem_stats *out) {
     out->capped = (int64_t)st[0];
     out->events = (int64_t)st[1];
     out->events_dropped = (int64_t)st[2];
-    out->reorders = reorders;
+    out->reorders = (int64_t)st[4];
     out->kernel_launches = launches;
+    out->list_overflows = (int64_t)st[5];
     out->device_error = e | (st[3] ? 1 : 0);
     return DEM_OK;
 }

@@ -28,12 +28,13 @@ struct SceneHost {
     int use_f64 = 0;
     float lambda = 0.5f;
     float cell_factor = 1.0f;
+    float skin = 0.0f;
     // control words (coll_cont) at step0
     long long step0 = 0;
     int32_t cc0_0 = 0, cc1_0 = 0, cc2_0 = 0;
     bool active = true;
     // layout in the world
-    int particle_base = 0, cell_base = 0, n_cells = 0, bond_base = 0, mat_base = 0;
+    int particle_base = 0, cell_base = 0, n_cells = 0, bond_base = 0, mat_base = 0, pair_base = 0;
     ScenePar par;
 };
 
@@ -63,37 +64,15 @@ class World {
 
     std::string err;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;   // captures the rebuild body of a conditional node
     int device = 0;
     int block = 256;
-    int reorder_interval = 20;
+    int graph_steps = 35;          // steps per captured CUDA graph
+    float skin_factor = 0.2f;      // candidate-list skin / r_max
     bool diagnostics = true;
     long long host_step = 0;
-    long long reorders = 0;
     std::vector<SceneHost> sh;
     DevWorld d{};
-
-  private:
-    int fail(int code, const std::string &msg);
-    int alloc(int N, int C, int B, int S, int M, uint32_t ev_cap);
-    void release();
-    int compute_layout(SceneHost &h, const dem_scene *scene);
-    void fill_par(SceneHost &h);
-    int push_par(int s);
-    int stage_scene(int s, const dem_scene *scene);
-    DevWorld spare{};
-    std::vector<void *> owned;
-    int steps_since_reorder = 0;
-    // CUDA graphs of one reorder period (R steps ending in a reorder), one per
-    // pointer parity (each reorder swaps the live and spare particle arrays)
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    int graph_R[2] = {0, 0};
-    int parity = 0;
-    void enqueue_step();
-    void drop_graphs();
-    int launch_period();
-    int graph_launches[2] = {0, 0};
-
-  public:
     bool use_graphs = true;
     long long launches = 0;
     // kernel timing (debug): event pairs per kernel kind, summed on demand
@@ -104,9 +83,32 @@ class World {
         long long n = 0;
     };
     Timer timers[5];
-    int timed(int kind, void (*fn)(World &), bool &ok);
     int kernel_time(int kind, double *ms, long long *n);
     void set_timing(bool on);
+
+  private:
+    int fail(int code, const std::string &msg);
+    int alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap);
+    int push_materials(int s);
+    void release();
+    int compute_layout(SceneHost &h, const dem_scene *scene);
+    void fill_par(SceneHost &h);
+    int push_par(int s);
+    int push_det();
+    int stage_scene(int s, const dem_scene *scene);
+    int force_rebuild();
+    void enqueue_plain_step();
+    void enqueue_rebuild(cudaStream_t st, const int32_t *gate);
+    int capture_graph(int R, cudaGraphExec_t *out, int *kernels);
+    void drop_graph();
+    DevWorld spare{};
+    std::vector<void *> owned;
+    cudaGraphExec_t graph = nullptr;   // graph_steps steps
+    cudaGraphExec_t graph1 = nullptr;  // one step, for remainders
+    int graph_R = 0;
+    int graph_kernels = 0;
+    int graph1_kernels = 0;
+    int rebuild_kernels = 0;
 };
 
 }  // namespace demgb

@@ -60,7 +60,8 @@ class Ext(C.Structure):
                 ("bond_normal_strength", _FP), ("bond_shear_strength", _FP),
                 ("diagnostics", C.c_int32), ("reorder_interval", C.c_int32),
                 ("block_size", C.c_int32), ("search_cell_factor", C.c_float),
-                ("event_capacity", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("event_capacity", C.c_int32), ("list_skin", C.c_float),
+                ("plain_launches", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class Scene(C.Structure):
@@ -81,7 +82,7 @@ class Stats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("capped", C.c_int64), ("events", C.c_int64),
                 ("events_dropped", C.c_int64), ("reorders", C.c_int64),
                 ("device_error", C.c_int32), ("reserved", C.c_int32),
-                ("kernel_launches", C.c_int64)]
+                ("kernel_launches", C.c_int64), ("list_overflows", C.c_int64)]
 
 
 BREAK_DTYPE = np.dtype([("scene", "<i4"), ("step", "<i4"), ("bond", "<i4"), ("code", "<i4"),
@@ -160,7 +161,8 @@ def make_params(d):
 
 
 def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnostics=True,
-             reorder_interval=0, block_size=0, search_cell_factor=0.0, event_capacity=0, keep=None):
+             reorder_interval=0, block_size=0, search_cell_factor=0.0, event_capacity=0,
+             list_skin=0.0, plain_launches=False, keep=None):
     e = Ext()
     lib().dem_ext_defaults(C.byref(e))
     e.use_f64 = 1 if use_f64 else 0
@@ -170,6 +172,8 @@ def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnos
     e.block_size = block_size
     e.search_cell_factor = search_cell_factor
     e.event_capacity = event_capacity
+    e.list_skin = list_skin
+    e.plain_launches = 1 if plain_launches else 0
     for attr, arr in (("bond_normal_strength", bond_sn), ("bond_shear_strength", bond_ss)):
         if arr is not None:
             a = np.ascontiguousarray(arr, dtype=np.float32)

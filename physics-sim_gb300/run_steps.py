@@ -20,7 +20,8 @@ def main():
     ap.add_argument("--workload", default="c1_chains")
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--particles", type=int, default=0)
-    ap.add_argument("--reorder", type=int, default=21)
+    ap.add_argument("--graph-steps", type=int, default=35)
+    ap.add_argument("--plain", action="store_true", help="no CUDA graphs (for ncu)")
     a = ap.parse_args()
     if a.workload == "c1_chains":
         sc, p, ext = dem_scenes.c1_chains()
@@ -30,7 +31,7 @@ def main():
         sc, p, ext = dem_scenes.dense_bed(n=a.particles or (1 << 20))
     else:
         raise SystemExit("unknown workload")
-    with dem.Context(sc, p, reorder_interval=a.reorder, **ext) as ctx:
+    with dem.Context(sc, p, reorder_interval=a.graph_steps, plain_launches=a.plain, **ext) as ctx:
         ctx.step(a.steps)
         ctx.synchronize()
         print("ok", a.workload, len(sc["radii"]), "particles", a.steps, "steps", ctx.stats())
