@@ -39,11 +39,13 @@ FLUSH_BYTES = 2 * L2_BYTES
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1_chains")
-    ap.add_argument("--frame", type=int, default=105)
+    ap.add_argument("--workload", default="c3_batch")
+    ap.add_argument("--frame", type=int, default=0)
+    ap.add_argument("--scenes", type=int, default=512)
+    ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     return ap.parse_args()
@@ -66,6 +68,19 @@ def build_workload(name):
     else:
         raise SystemExit("unknown workload %s" % name)
     return sc, p, ext, desc
+
+
+def build_batch_workload(n_scenes, seed):
+    import dem_scenes
+    items = dem_scenes.c3_batch(n_scenes=n_scenes, seed=seed)
+    ns = [int(it[0]["radii"].shape[0]) for it in items]
+    nb = [int(it[0]["bonds"].shape[0] // 3) if it[0]["bonds"].shape[0] >= 3 else 0 for it in items]
+    desc = {"workload": "c3 batched uneven scenes", "scenes": n_scenes,
+            "particles": int(sum(ns)), "particles_per_scene": "log-uniform [1000, 64000] (min %d, max %d)"
+            % (min(ns), max(ns)), "bond_fraction": "uniform [0, 0.5]", "bonds": int(sum(nb)),
+            "scene_model": "loose c0 disks + bonded chains of 32 (parallel bonds, factor 0.8, Weibull strengths)",
+            "dt": 1e-4, "seed": seed}
+    return items, desc
 
 
 def dist_env():
@@ -364,12 +379,262 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def _okw(ext):
+    kw = {}
+    if "bond_lambda" in ext:
+        kw["bond_lambda"] = ext["bond_lambda"]
+    if "bond_sn" in ext:
+        kw["bond_sn"], kw["bond_ss"] = ext["bond_sn"], ext["bond_ss"]
+    return kw
+
+
+def run_reference_batch(args):
+    """The CPU restatement of the reference step over the batched mix: each
+    bench step advances one scene of the mix (cycling through them) by a
+    bounded number of steps, all host threads."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    items, desc = build_batch_workload(args.scenes, args.seed)
+    states = [{k: (v.copy() if hasattr(v, "copy") else v) for k, v in it[0].items()} for it in items]
+    done = [0] * len(items)
+
+    def one(k, steps):
+        sc, p, ext = items[k]
+        oracle.step(states[k], p, steps, step_base=done[k], **_okw(ext))
+        done[k] += steps
+        return int(sc["radii"].shape[0]) * steps
+
+    sub = args.frame
+    for w in range(args.warmup):
+        one(w % len(items), 1)
+    tot = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        tot += one(k % len(items), sub)
+    dt = time.perf_counter() - t0
+    value = tot / dt
+    cores = os.cpu_count() or 1
+    cfg = dict(desc)
+    cfg.update({"frame_steps": args.frame, "sample": "scene k mod %d advanced %d steps per bench step"
+                % (len(items), sub)})
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": "%d bench steps of %d steps on scenes of the mix, all host threads"
+                             % (args.steps, sub)},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours_batch(args):
+    import torch
+    import build_lib
+    import dem
+    build_lib.build()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    items, desc = build_batch_workload(args.scenes, args.seed + rank)
+    ntot = sum(int(it[0]["radii"].shape[0]) for it in items)
+    F = args.frame
+    batch = dem.Batch(items, device=local, reorder_interval=35)
+    stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        batch.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        batch.step(F)
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    launches0 = batch.stats()["kernel_launches"]
+    sampler.mark()
+    barrier()
+    evs = []
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.step(F)
+        e1.record(stream)
+        evs.append((e0, e1))
+    barrier()
+    wall = time.perf_counter() - wall0
+    sampler.mark()
+    st = batch.stats()
+    launches = st["kernel_launches"] - launches0
+    sampler.stop()
+    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = ntot * F * args.steps * ws / (max_ms / 1e3)
+    clocks = sampler.summary()
+
+    # the same scenes through the plain single-scene path, one after another
+    plain_ms = 0.0
+    plain_ps = 0
+    for sc, p, ext in items:
+        ctx = dem.Context(sc, p, device=local, reorder_interval=35, **ext)
+        cst = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+        ctx.step(35)
+        ctx.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(cst)
+        ctx.step(F)
+        e1.record(cst)
+        e1.synchronize()
+        plain_ms += e0.elapsed_time(e1)
+        plain_ps += int(sc["radii"].shape[0]) * F
+        ctx.close()
+    plain_value = plain_ps / (plain_ms / 1e3)
+
+    # roofline of k_interact over the whole batch (plain launches with events)
+    states = [batch.download(k) for k in range(len(items))]
+    s_u = s_b = 0
+    for stt in states:
+        a, b2 = slot_counts(stt)
+        s_u += a
+        s_b += b2
+    alg_bytes = 12 * s_u + 36 * s_b + 56 * ntot
+    peak, peak_kind = measured_peaks()
+    roofline = {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
+                "kernel": "k_interact", "algorithmic_bytes_per_launch": alg_bytes,
+                "slots_unbonded": s_u, "slots_bonded": s_b, "traffic": profiled_traffic(args.workload)}
+    try:
+        kt = BatchKernelTimer(batch)
+        kt.run(2 * F)
+        roofline.update(kt.figures(alg_bytes, peak))
+    except Exception as exc:  # timing is diagnostic; the value above stands
+        roofline["error"] = str(exc)
+
+    # end to end through the batch API: restore every scene from host arrays,
+    # one frame, read every scene back
+    h2d = sum(scene_bytes(x) for x in states)
+    t0 = time.perf_counter()
+    for k in range(len(items)):
+        batch.upload(k, states[k])
+    batch.step(F)
+    outs = [batch.download(k) for k in range(len(items))]
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    del outs
+    e2e = {"value": ntot * F * ws / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": h2d,
+           "note": "dem_batch_upload of all scenes + dem_batch_step(frame) + dem_batch_download of all scenes"}
+
+    base = None
+    if rank == 0 and ws == 1:
+        base = cpu_baseline_batch(items, args.cpu_seconds)
+    cfg = dict(desc)
+    cfg.update({"frame_steps": F, "parallelism": "replicas" if ws > 1 else "single",
+                "l2": "inputs larger than L2 (and a %d MiB write between frames, untimed)" % (FLUSH_BYTES >> 20),
+                "graph_steps": 35, "plain_path_particle_steps_per_s": plain_value,
+                "batched_over_plain": value / plain_value if plain_value else None,
+                "rebuilds": st["reorders"], "list_overflows": st["list_overflows"]})
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg, "clocks": clocks, "roofline": roofline,
+            "e2e": e2e, "gpu_launches": int(launches), "wall_s": wall}
+    if base is not None:
+        line["cpu_baseline"] = base
+    batch.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+class BatchKernelTimer:
+    """k_interact launch times of a batch, CUDA events on the batch's stream."""
+
+    def __init__(self, batch):
+        import ctypes as C
+        import dem
+        self.L = dem.lib()
+        self.b = batch
+        self.C = C
+        self.L.dem_batch_kernel_timing.argtypes = [C.c_void_p, C.c_int32]
+        self.L.dem_batch_kernel_time.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double),
+                                                 C.POINTER(C.c_int64)]
+
+    def run(self, steps):
+        self.L.dem_batch_kernel_timing(self.b.h, 1)
+        self.b.step(steps)
+        self.b.synchronize()
+
+    def figures(self, alg_bytes, peak):
+        C = self.C
+        out = {}
+        for k in ("interact", "lom", "broad_phase"):
+            ms = C.c_double(0.0)
+            n = C.c_int64(0)
+            self.L.dem_batch_kernel_time(self.b.h, k.encode(), C.byref(ms), C.byref(n))
+            out[k] = (ms.value, n.value)
+        self.L.dem_batch_kernel_timing(self.b.h, 0)
+        ims, inn = out["interact"]
+        avg_s = ims / max(inn, 1) / 1e3
+        achieved = alg_bytes / avg_s / 1e9
+        return {"achieved": achieved, "frac": achieved / peak, "launch_us": avg_s * 1e6,
+                "lom_us": out["lom"][0] / max(out["lom"][1], 1) * 1e3,
+                "rebuild_body_us": out["broad_phase"][0] / max(out["broad_phase"][1], 1) * 1e3}
+
+
+def cpu_baseline_batch(items, seconds):
+    """The oracle on a sample of the mix: consecutive scenes advanced 35 steps
+    each until about `seconds` of CPU time, all host threads."""
+    import oracle
+    done_ps = 0
+    t0 = time.perf_counter()
+    k = 0
+    while time.perf_counter() - t0 < seconds and k < len(items):
+        sc, p, ext = items[k]
+        s = {key: (v.copy() if hasattr(v, "copy") else v) for key, v in sc.items()}
+        oracle.step(s, p, 35, **_okw(ext))
+        done_ps += int(sc["radii"].shape[0]) * 35
+        k += 1
+    dt = time.perf_counter() - t0
+    return {"value": done_ps / dt, "unit": "particle-steps/s", "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": "first %d scenes of the mix, 35 steps each from their initial states (%.1f s)" % (k, dt)}
+
+
 def main():
     args = parse_args()
+    batch = args.workload == "c3_batch"
+    if args.frame <= 0:
+        args.frame = 35 if batch else 105
+    if args.steps <= 0:
+        args.steps = 20 if batch else 200
     if args.impl == "reference":
-        run_reference(args)
+        if batch:
+            run_reference_batch(args)
+        else:
+            run_reference(args)
     else:
-        run_ours(args)
+        if batch:
+            run_ours_batch(args)
+        else:
+            run_ours(args)
 
 
 if __name__ == "__main__":

@@ -200,6 +200,30 @@ int dem_get_stats(dem_ctx *ctx, dem_stats *out);
  * order their own work against the steps. */
 void *dem_stream(dem_ctx *ctx);
 
+/* ---- Batches: many independent scenes stepped together ------------------
+ * No counterpart in the reference (one scene per program there).  A batch
+ * holds n_scenes scenes resident on one GPU; dem_batch_step advances every
+ * scene by n_steps with the same launches, each scene with its own settings,
+ * materials, bonds and extensions (exts may be NULL for defaults; world-wide
+ * options such as block_size are taken from exts[0]).  Per-scene results are
+ * exactly those of a single-scene context on the same scene. */
+typedef struct dem_batch dem_batch;
+int dem_batch_create(const dem_scene *const *scenes, const dem_params *params, const dem_ext *exts,
+                     int32_t n_scenes, int device, dem_batch **out);
+void dem_batch_destroy(dem_batch *b);
+const char *dem_batch_last_error(const dem_batch *b);
+int dem_batch_scene_count(const dem_batch *b);
+int dem_batch_step(dem_batch *b, int32_t n_steps);
+int dem_batch_synchronize(dem_batch *b);
+int dem_batch_download(dem_batch *b, int32_t scene, dem_scene *out);
+int dem_batch_upload(dem_batch *b, int32_t scene, const dem_scene *in);
+int dem_batch_set_params(dem_batch *b, int32_t scene, const dem_params *params);
+int dem_batch_set_properties(dem_batch *b, int32_t scene, int32_t *selections,
+                             const int32_t props[DEM_PROPS_WORDS]);
+int dem_batch_break_events(dem_batch *b, dem_break_event *buf, int32_t cap, int32_t *n);
+int dem_batch_get_stats(dem_batch *b, dem_stats *out);
+void *dem_batch_stream(dem_batch *b);
+
 /* Broad phase that allocates nothing.  No counterpart in the reference: it is
  * for callers that cannot call cudaMalloc (a framework whose pool owns the
  * device heap, an allocator that forbids it, a real-time loop that must not

@@ -34,6 +34,9 @@ int dem_debug_search_grid(dem_ctx *ctx, float *x0, float *y0, float *inv, int32_
  * "broad_phase", "reorder", "end_step") since timing was enabled. */
 int dem_debug_kernel_timing(dem_ctx *ctx, int32_t enable);
 int dem_debug_kernel_time(dem_ctx *ctx, const char *kernel, double *total_ms, int64_t *launches);
+/* The same kernel timing for a batch. */
+int dem_batch_kernel_timing(dem_batch *b, int32_t enable);
+int dem_batch_kernel_time(dem_batch *b, const char *kernel, double *total_ms, int64_t *launches);
 
 #ifdef __cplusplus
 }

@@ -109,7 +109,8 @@ int dem_create(const dem_scene *scene, const dem_params *params, const dem_ext *
     }
     std::vector<const dem_scene *> scenes{scene};
     std::vector<dem_params> ps{*params};
-    int rc = ctx->world.build(scenes, ps, e);
+    std::vector<dem_ext> es{e};
+    int rc = ctx->world.build(scenes, ps, es);
     if (rc != DEM_OK) {
         std::string m = ctx->world.err;
         cudaStreamDestroy(ctx->world.stream);

@@ -265,6 +265,7 @@ __global__ void __launch_bounds__(256) k_keys(DevWorld w, const int32_t *gate) {
     if (i >= w.N) return;
     uint32_t m = w.meta[i];
     const ScenePar &P = w.par[meta_scene(m)];
+    if (!P.active) return;  // frozen scenes keep their order and take no cells
     float4 p = w.pr[i];
     uint32_t key;
     if (p.z == 0.0f) {
@@ -382,6 +383,7 @@ __global__ void __launch_bounds__(256) k_scatter(DevWorld w, const int32_t *gate
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
+    if (!w.par[meta_scene(w.meta[i])].active) return;
     uint32_t key = w.keys[i];
     int slot = w.cell_start[key] + atomicSub(&w.cell_count[key], 1) - 1;
     w.sorted[slot] = i;
@@ -423,18 +425,31 @@ int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int3
 // --------------------------------------------------------------- reorder
 // Permute every per-particle array into cell order (new i <- old sorted[i])
 // and remap partner indices; the cell lists become the identity.
+// The particle at cell-order position k (sorted[k]) moves to its scene's
+// range at the same offset: new = particle_base + (k - first position of the
+// scene's cells).  Particles of frozen scenes stay where they are.
 __global__ void __launch_bounds__(256) k_inverse(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.N) return;
-    w.inv[w.sorted[i]] = i;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= w.N) return;
+    if (t < w.cell_start[w.C]) {
+        const int old = w.sorted[t];
+        const ScenePar &P = w.par[meta_scene(w.meta[old])];
+        const int nw = P.particle_base + (t - w.cell_start[P.cell_base]);
+        w.inv[old] = nw;
+        w.src[nw] = old;
+    }
+    if (!w.par[meta_scene(w.meta[t])].active) {
+        w.inv[t] = t;
+        w.src[t] = t;
+    }
 }
 
 __global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
-    int src = w.sorted[i];
+    int src = w.src[i];
     o.pr[i] = w.pr[src];
     o.vw[i] = w.vw[src];
     o.ac[i] = w.ac[src];
@@ -455,7 +470,9 @@ __global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o, const in
         o.s_btf[j * N + i] = w.s_btf[j * N + src];
         o.s_thb[j * N + i] = w.s_thb[j * N + src];
     }
-    w.sorted[i] = i;  // safe: each thread read only its own sorted[i]
+    // the cell-order list now names the new indices
+    const ScenePar &P = w.par[meta_scene(w.meta[src])];
+    if (P.active) w.sorted[i - P.particle_base + w.cell_start[P.cell_base]] = i;
 }
 
 // copy the permuted arrays back, so the live arrays keep their addresses

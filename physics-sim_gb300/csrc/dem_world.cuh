@@ -104,7 +104,7 @@ struct DevWorld {
     int32_t *cc3;              // per scene "positions set externally" flag
     // broad phase
     uint32_t *keys;
-    int32_t *cell_count, *cell_start, *sorted, *inv, *scan_tmp;
+    int32_t *cell_count, *cell_start, *sorted, *inv, *src, *scan_tmp;
     // bond breaks of the current step (applied after the Simulation pass)
     Pending *pend;
     uint32_t *pend_count;

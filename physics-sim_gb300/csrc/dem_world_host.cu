@@ -94,6 +94,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
     w.cell_start = dalloc<int32_t>(owned, (size_t)C + 1, ok);
     w.sorted = dalloc<int32_t>(owned, N, ok);
     w.inv = dalloc<int32_t>(owned, N, ok);
+    w.src = dalloc<int32_t>(owned, N, ok);
     w.scan_tmp = dalloc<int32_t>(owned, scan_tmp_size(C), ok);
     w.pend_cap = (uint32_t)std::max<long long>(2LL * B + 64, 64);
     w.pend = dalloc<Pending>(owned, w.pend_cap, ok);
@@ -425,9 +426,11 @@ int World::push_materials(int s) {
 }
 
 int World::build(const std::vector<const dem_scene *> &scenes, const std::vector<dem_params> &params,
-                 const dem_ext &ext) {
+                 const std::vector<dem_ext> &exts) {
     const int S = (int)scenes.size();
     if (S <= 0 || S > MAX_SCENES) return fail(DEM_E_INVALID, "scene count out of range");
+    if ((int)params.size() != S || (int)exts.size() != S) return fail(DEM_E_INVALID, "one params/ext per scene");
+    const dem_ext &ext = exts[0];  // world-wide options come from the first scene's ext
     if (ext.block_size) {
         if (ext.block_size < 32 || ext.block_size > 1024 || (ext.block_size & 31))
             return fail(DEM_E_INVALID, "block_size must be a multiple of 32 in [32, 1024]");
@@ -438,22 +441,23 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     if (ext.list_skin < 0.0f) return fail(DEM_E_INVALID, "list_skin < 0");
     if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
     use_graphs = ext.plain_launches == 0;
-    if (!(ext.bond_lambda > 0.0f)) return fail(DEM_E_INVALID, "bond_lambda must be > 0");
     diagnostics = ext.diagnostics != 0;
     sh.assign(S, SceneHost{});
     long long N = 0, C = 0, B = 0, M = 0, MP = 0;
     for (int s = 0; s < S; ++s) {
         SceneHost &h = sh[s];
+        const dem_ext &e = exts[s];
+        if (!(e.bond_lambda > 0.0f)) return fail(DEM_E_INVALID, "bond_lambda must be > 0");
         h.params = params[s];
-        h.use_f64 = ext.use_f64 ? 1 : 0;
-        h.lambda = ext.bond_lambda;
+        h.use_f64 = e.use_f64 ? 1 : 0;
+        h.lambda = e.bond_lambda;
         h.cell_factor = ext.search_cell_factor > 0.0f ? ext.search_cell_factor : 1.0f;
         int rc = compute_layout(h, scenes[s]);
         if (rc) return rc;
-        if (ext.bond_normal_strength && h.n_bonds > 0)
-            h.bond_sn.assign(ext.bond_normal_strength, ext.bond_normal_strength + h.n_bonds);
-        if (ext.bond_shear_strength && h.n_bonds > 0)
-            h.bond_ss.assign(ext.bond_shear_strength, ext.bond_shear_strength + h.n_bonds);
+        if (e.bond_normal_strength && h.n_bonds > 0)
+            h.bond_sn.assign(e.bond_normal_strength, e.bond_normal_strength + h.n_bonds);
+        if (e.bond_shear_strength && h.n_bonds > 0)
+            h.bond_ss.assign(e.bond_shear_strength, e.bond_shear_strength + h.n_bonds);
         if (h.bond_sn.empty() != h.bond_ss.empty()) {
             if (h.bond_sn.empty()) h.bond_sn.assign(h.n_bonds, params[s].bond_normal_strength);
             if (h.bond_ss.empty()) h.bond_ss.assign(h.n_bonds, params[s].bond_shear_strength);
@@ -922,12 +926,14 @@ int World::broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *c
     const int n = h.n, base = h.particle_base;
     std::vector<uint32_t> k(n);
     std::vector<int32_t> srt(n), orig(n), cs((size_t)h.n_cells + 1);
+    CK(cudaMemcpyAsync(cs.data(), d.cell_start + h.cell_base, cs.size() * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    const int first = cs[0];
     if (n > 0) {
         CK(cudaMemcpyAsync(k.data(), d.keys + base, n * 4, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(srt.data(), d.sorted + base, n * 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(srt.data(), d.sorted + first, n * 4, cudaMemcpyDeviceToHost, stream));
         CK(cudaMemcpyAsync(orig.data(), d.orig + base, n * 4, cudaMemcpyDeviceToHost, stream));
     }
-    CK(cudaMemcpyAsync(cs.data(), d.cell_start + h.cell_base, cs.size() * 4, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     for (int i = 0; i < n; ++i) {
         if (keys) keys[orig[i]] = (int32_t)k[i] - h.cell_base;
@@ -936,7 +942,7 @@ int World::broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *c
         if (order) order[i] = orig[src];
     }
     if (cell_start)
-        for (size_t c = 0; c < cs.size(); ++c) cell_start[c] = cs[c] - base;
+        for (size_t c = 0; c < cs.size(); ++c) cell_start[c] = cs[c] - first;
     // the cell table now describes the current positions, not the last rebuild
     return force_rebuild();
 }

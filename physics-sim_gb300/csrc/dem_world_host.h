@@ -47,7 +47,7 @@ class World {
 
     // Lay out the given scenes (host staging), allocate and upload.  Returns DEM_* code.
     int build(const std::vector<const dem_scene *> &scenes, const std::vector<dem_params> &params,
-              const dem_ext &ext);
+              const std::vector<dem_ext> &exts);
     // Replace one scene's state in place (same particle/bond/material counts).
     int upload_scene(int s, const dem_scene *scene);
     int download_scene(int s, dem_scene *out);

@@ -94,7 +94,12 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_set_control", "dem_get_control", "dem_step", "dem_synchronize", "dem_download",
            "dem_set_properties", "dem_break_events", "dem_get_stats", "dem_stream",
            "dem_debug_broad_phase", "dem_debug_search_grid", "dem_debug_kernel_timing",
-           "dem_debug_kernel_time", "dem_broad_phase_noalloc", "dem_noalloc_last_error"]
+           "dem_debug_kernel_time", "dem_broad_phase_noalloc", "dem_noalloc_last_error",
+           "dem_batch_create", "dem_batch_destroy", "dem_batch_last_error", "dem_batch_scene_count",
+           "dem_batch_step", "dem_batch_synchronize", "dem_batch_download", "dem_batch_upload",
+           "dem_batch_set_params", "dem_batch_set_properties", "dem_batch_break_events",
+           "dem_batch_get_stats", "dem_batch_stream", "dem_batch_kernel_timing",
+           "dem_batch_kernel_time"]
 
 _lib = None
 
@@ -145,9 +150,27 @@ def lib(path=None):
                                           C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p]
     L.dem_noalloc_last_error.restype = C.c_char_p
+    L.dem_batch_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int,
+                                   C.POINTER(C.c_void_p)]
+    L.dem_batch_destroy.argtypes = [C.c_void_p]
+    L.dem_batch_destroy.restype = None
+    L.dem_batch_last_error.argtypes = [C.c_void_p]
+    L.dem_batch_last_error.restype = C.c_char_p
+    L.dem_batch_scene_count.argtypes = [C.c_void_p]
+    L.dem_batch_step.argtypes = [C.c_void_p, C.c_int32]
+    L.dem_batch_synchronize.argtypes = [C.c_void_p]
+    L.dem_batch_download.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Scene)]
+    L.dem_batch_upload.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Scene)]
+    L.dem_batch_set_params.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Params)]
+    L.dem_batch_set_properties.argtypes = [C.c_void_p, C.c_int32, _IP, _IP]
+    L.dem_batch_break_events.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
+    L.dem_batch_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    L.dem_batch_stream.argtypes = [C.c_void_p]
+    L.dem_batch_stream.restype = C.c_void_p
     for name in SYMBOLS:
         if name not in ("dem_destroy", "dem_ext_defaults", "dem_last_error", "dem_stream",
-                        "dem_abi_version", "dem_noalloc_last_error"):
+                        "dem_abi_version", "dem_noalloc_last_error", "dem_batch_destroy",
+                        "dem_batch_last_error", "dem_batch_stream"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -361,6 +384,90 @@ class Context:
         _check(L, self.h, L.dem_debug_search_grid(self.h, C.byref(x0), C.byref(y0), C.byref(inv),
                                                   C.byref(gw), C.byref(gh)))
         return x0.value, y0.value, inv.value, gw.value, gh.value
+
+
+class Batch:
+    """Many independent scenes resident on one GPU, stepped together
+    (dem_batch_*).  `items` is a list of (scene, params, ext) triples as the
+    dem_scenes builders return them; ext keys as for Context."""
+
+    def __init__(self, items, *, device=-1, **world_kw):
+        L = lib()
+        self._keep = []
+        n = len(items)
+        scenes = (Scene * n)()
+        params = (Params * n)()
+        exts = (Ext * n)()
+        self._templates = []
+        for k, (sc, p, ext) in enumerate(items):
+            kw = dict(world_kw)
+            kw.update(ext)
+            scenes[k] = make_scene(sc)
+            params[k] = make_params(p)
+            exts[k] = make_ext(keep=self._keep, **kw)
+            self._templates.append({key: (v.copy() if hasattr(v, "copy") else v) for key, v in sc.items()
+                                    if key in F32_KEYS + I32_KEYS + ("grid",)})
+        self._keep.append((scenes, params, exts, [it[0] for it in items]))
+        ptrs = (C.c_void_p * n)(*[C.addressof(scenes[k]) for k in range(n)])
+        h = C.c_void_p()
+        rc = L.dem_batch_create(ptrs, C.addressof(params), C.addressof(exts), n, device, C.byref(h))
+        if rc != 0:
+            raise DemError(rc, (L.dem_batch_last_error(None) or b"").decode())
+        self.h = h
+        self.n_scenes = n
+        self.particles = [int(it[0]["radii"].shape[0]) for it in items]
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().dem_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise DemError(rc, (lib().dem_batch_last_error(self.h) or b"").decode())
+
+    def step(self, n=1):
+        self._check(lib().dem_batch_step(self.h, int(n)))
+
+    def synchronize(self):
+        self._check(lib().dem_batch_synchronize(self.h))
+
+    def download(self, scene):
+        out = empty_like_scene(self._templates[scene])
+        st = make_scene(out)
+        self._check(lib().dem_batch_download(self.h, int(scene), C.byref(st)))
+        out["coll_cont"] = np.array(st.coll_cont[:], dtype=np.int32)
+        return out
+
+    def upload(self, scene, sc):
+        st = make_scene(sc)
+        self._check(lib().dem_batch_upload(self.h, int(scene), C.byref(st)))
+
+    def break_events(self, cap=1 << 18):
+        buf = np.zeros(cap, dtype=BREAK_DTYPE)
+        n = C.c_int32(0)
+        self._check(lib().dem_batch_break_events(self.h, buf.ctypes.data, cap, C.byref(n)))
+        return buf[: n.value].copy()
+
+    def stats(self):
+        s = Stats()
+        self._check(lib().dem_batch_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in Stats._fields_ if k != "reserved"}
+
+    def stream(self):
+        return lib().dem_batch_stream(self.h)
 
 
 def grid_capacity(params, radii, particles):

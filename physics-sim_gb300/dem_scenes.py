@@ -73,6 +73,117 @@ def _bond_record(dx, dy):
     return 1, int(np.array([ang], np.float32).view(np.int32)[0]), int(np.array([mag], np.float32).view(np.int32)[0])
 
 
+def add_straight_chain_bonds(scene, starts, lengths):
+    """Vectorised add_chain_bonds for chains of consecutive indices
+    [start, start + length): the same bond records and slot assignment as
+    regen_bonds (state.rs:291-367) gives such chains (bond to the previous
+    member in slot 0, to the next member in the first free slot)."""
+    pos = scene["pos"].reshape(-1, 2)
+    starts = np.asarray(starts, np.int64)
+    lengths = np.asarray(lengths, np.int64)
+    i_list = np.concatenate([np.arange(s0, s0 + ln - 1) for s0, ln in zip(starts, lengths)]) \
+        if len(starts) else np.zeros(0, np.int64)
+    i_list = np.sort(i_list)
+    j_list = i_list + 1
+    nb = i_list.size
+    if nb == 0:
+        scene["bonds"] = np.full(1, -1, np.int32)
+        return scene
+    dx = (pos[j_list, 0] - pos[i_list, 0]).astype(np.float32)
+    dy = (pos[j_list, 1] - pos[i_list, 1]).astype(np.float32)
+    mag = np.power((dx * dx + dy * dy).astype(np.float32), np.float32(0.5)).astype(np.float32)
+    ang = np.arctan2((dx / mag).astype(np.float32), (dy / mag).astype(np.float32)).astype(np.float32)
+    bonds = np.empty((nb, 3), np.int32)
+    bonds[:, 0] = 1
+    bonds[:, 1] = ang.view(np.int32)
+    bonds[:, 2] = mag.view(np.int32)
+    contacts = scene["contacts"].reshape(-1, MAX_CONTACTS, 6)
+    k = np.arange(nb, dtype=np.int32)
+    is_first = np.zeros(pos.shape[0], bool)
+    is_first[starts] = True
+    slot_i = np.where(is_first[i_list], 0, 1)
+    contacts[i_list, slot_i, 0] = i_list
+    contacts[i_list, slot_i, 1] = j_list
+    contacts[i_list, slot_i, 2:5] = 0
+    contacts[i_list, slot_i, 5] = k
+    contacts[j_list, 0, 0] = j_list
+    contacts[j_list, 0, 1] = i_list
+    contacts[j_list, 0, 2:5] = 0
+    contacts[j_list, 0, 5] = k
+    scene["bonds"] = bonds.reshape(-1).copy()
+    scene["contacts"] = contacts.reshape(-1).copy()
+    return scene
+
+
+def c3_mix_scene(n, bond_fraction, seed):
+    """One scene of the batched mix: n particles, a fraction `bond_fraction`
+    of them in horizontal bonded chains (radius 1, spacing 2, parallel bonds
+    with bond radius factor 0.8, k_n 1e5, k_s 5e4, strengths Weibull(8, 5e3)),
+    the rest loose disks (radii U[0.8, 1.2]) on a jittered lattice below them;
+    gravity on, walls, contacts and dt as in c0_settle."""
+    rng = np.random.default_rng(seed)
+    n_chain = int(round(n * bond_fraction))
+    chain_len = 32
+    n_chains = n_chain // chain_len
+    n_chain = n_chains * chain_len
+    n_loose = n - n_chain
+    # box: ~8 units^2 per particle, aspect 1:2 (c0_settle's density)
+    W = float(np.ceil(np.sqrt(8.0 * n / 2.0)))
+    W = max(W, 2.0 * chain_len + 8.0)
+    H = max(8.0 * n / W, 40.0)
+    H = float(np.ceil(H))
+    pos = np.zeros((n, 2), np.float64)
+    radii = np.ones(n, np.float32)
+    # loose lattice in the lower part
+    if n_loose > 0:
+        spacing = 2.75
+        cols = max(int((W - 2.6) // spacing), 1)
+        idx = np.arange(n_loose)
+        pos[:n_loose, 0] = (idx % cols - (cols - 1) / 2.0) * spacing + rng.uniform(-0.1, 0.1, n_loose)
+        pos[:n_loose, 1] = -H / 2.0 + 1.4 + (idx // cols) * spacing + rng.uniform(-0.1, 0.1, n_loose)
+        radii[:n_loose] = rng.uniform(0.8, 1.2, n_loose).astype(np.float32)
+    top_loose = (pos[:n_loose, 1].max() + 1.3) if n_loose > 0 else -H / 2.0
+    # chains in rows above
+    starts = []
+    if n_chains > 0:
+        per_row = max(int((W - 4.0) // (2.0 * chain_len + 4.0)), 1)
+        for c in range(n_chains):
+            row, col = divmod(c, per_row)
+            x0 = -W / 2.0 + 3.0 + col * (2.0 * chain_len + 4.0)
+            y = top_loose + 4.0 + row * 4.0
+            b0 = n_loose + c * chain_len
+            pos[b0:b0 + chain_len, 0] = x0 + 2.0 * np.arange(chain_len)
+            pos[b0:b0 + chain_len, 1] = y
+            starts.append(b0)
+        H = max(H, 2.0 * (pos[:, 1].max() + 2.0))
+    sc = empty_scene(n, [1, 1, 1, 1.0, 1e5, 5e4])
+    sc["pos"] = pos.astype(np.float32).reshape(-1)
+    sc["radii"] = radii
+    # chains: exact float positions first, then bonds from those positions
+    add_straight_chain_bonds(sc, starts, [chain_len] * len(starts))
+    p = reference_defaults(n)
+    p.update({"hor_bound": W, "vert_bound": H, "planet_mode": 0, "gravity": 1, "gravity_acc": 1.0,
+              "friction_coefficient": 0.5, "dT": 1e-4, "bonds": 3 if n_chains else 0,
+              "bonds_tear": 1, "bond_normal_stiffness": 1e5, "bond_shear_stiffness": 5e4,
+              "bond_normal_strength": 5e3, "bond_shear_strength": 5e3})
+    sc["grid"] = grid_capacity(W, H, sc["radii"], n)
+    ext = {"bond_lambda": 0.8}
+    nb = sc["bonds"].shape[0] // 3
+    if nb > 0:
+        st = (5e3 * rng.weibull(8.0, size=(2, nb))).astype(np.float32)
+        ext["bond_sn"], ext["bond_ss"] = st[0], st[1]
+    return sc, p, ext
+
+
+def c3_batch(n_scenes=512, seed=0, n_min=1000, n_max=64000):
+    """The batched mix: n_scenes scenes with log-uniform particle counts in
+    [n_min, n_max] and bond fractions uniform in [0, 0.5], each seeded."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_scenes)).astype(int)
+    fr = rng.uniform(0.0, 0.5, n_scenes)
+    return [c3_mix_scene(int(n), float(f), seed * 100003 + k) for k, (n, f) in enumerate(zip(ns, fr))]
+
+
 def add_chain_bonds(scene, chains):
     """Bonds and bonded contact slots for particle chains whose consecutive
     members are within 1.05 (r_i + r_j) and whose other pairs are not: the

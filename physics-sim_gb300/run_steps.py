@@ -19,10 +19,18 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="c1_chains")
     ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--particles", type=int, default=0)
+    ap.add_argument("--particles", type=int, default=0, help="particles (dense_bed) or scenes (c3_batch)")
     ap.add_argument("--graph-steps", type=int, default=35)
     ap.add_argument("--plain", action="store_true", help="no CUDA graphs (for ncu)")
     a = ap.parse_args()
+    if a.workload == "c3_batch":
+        items = dem_scenes.c3_batch(n_scenes=a.particles or 512)
+        with dem.Batch(items, reorder_interval=a.graph_steps, plain_launches=a.plain) as b:
+            b.step(a.steps)
+            b.synchronize()
+            print("ok", a.workload, len(items), "scenes", sum(len(x[0]["radii"]) for x in items),
+                  "particles", a.steps, "steps", b.stats())
+        return
     if a.workload == "c1_chains":
         sc, p, ext = dem_scenes.c1_chains()
     elif a.workload == "c0_settle":

@@ -1,0 +1,79 @@
+"""Batches of independent scenes: each scene's result in a batch is the
+result of the same scene run alone, bit for bit (and the oracle's)."""
+import numpy as np
+import pytest
+
+import dem
+import dem_scenes
+import oracle
+from gpu_backend import assert_same_state, copy_scene
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import build_lib
+    build_lib.build()
+
+
+def _items():
+    specs = [(600, 0.0, 1), (1500, 0.3, 2), (900, 0.5, 3), (2500, 0.1, 4), (1200, 0.45, 5)]
+    items = [dem_scenes.c3_mix_scene(n, f, sd) for n, f, sd in specs]
+    items.append(dem_scenes.dense_bed(800, seed=6))
+    items.append(dem_scenes.c1_chains(chains=3, length=20, seed=7, pull_velocity=20.0))
+    return items
+
+
+def _ev_tuples(ev, scene=None):
+    out = []
+    for e in ev:
+        if scene is None or int(e["scene"]) == scene:
+            out.append((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])))
+    return sorted(out)
+
+
+def test_batch_scene_equals_scene_alone():
+    items = _items()
+    steps = 140
+    with dem.Batch(items, reorder_interval=35) as b:
+        b.step(steps)
+        got = [b.download(k) for k in range(len(items))]
+        bev = b.break_events()
+    for k, (sc, p, ext) in enumerate(items):
+        with dem.Context(sc, p, reorder_interval=35, **ext) as ctx:
+            ctx.step(steps)
+            alone = ctx.download()
+            aev = ctx.break_events()
+        assert_same_state(got[k], alone, "scene %d: " % k)
+        assert _ev_tuples(bev, k) == _ev_tuples(aev)
+
+
+def test_batch_matches_oracle():
+    items = _items()[:3]
+    steps = 90
+    with dem.Batch(items) as b:
+        b.step(steps)
+        got = [b.download(k) for k in range(len(items))]
+    for k, (sc, p, ext) in enumerate(items):
+        o = copy_scene(sc)
+        kw = {}
+        if "bond_lambda" in ext:
+            kw["bond_lambda"] = ext["bond_lambda"]
+        if "bond_sn" in ext:
+            kw["bond_sn"], kw["bond_ss"] = ext["bond_sn"], ext["bond_ss"]
+        oracle.step(o, p, steps, **kw)
+        assert_same_state(got[k], o, "scene %d: " % k)
+
+
+def test_batch_upload_replaces_one_scene_only():
+    items = _items()[:4]
+    with dem.Batch(items) as b:
+        b.step(40)
+        before = [b.download(k) for k in range(4)]
+        b.upload(2, items[2][0])
+        b.step(0)
+        after = [b.download(k) for k in range(4)]
+    for k in (0, 1, 3):
+        assert_same_state(after[k], before[k], "scene %d: " % k)
+    assert np.array_equal(after[2]["pos"], items[2][0]["pos"])
