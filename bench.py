@@ -7,7 +7,7 @@ gen_per_frame steps, src/wgpu_prog.rs:1420-1473; the reference default is
 simulation steps / device time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c1_chains|c0_settle|dense_bed] [--frame F]
+                  [--workload c3_batch|c4_serve|c1_chains|c0_settle|dense_bed] [--frame F]
 
 --impl reference times the reference's algorithm on the host cores: the CPU
 restatement under oracle/ (the reference's own WGSL-through-wgpu step cannot
@@ -48,6 +48,16 @@ def parse_args():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-min", type=int, default=2000)
+    ap.add_argument("--serve-max", type=int, default=256000)
+    ap.add_argument("--serve-hmin", type=int, default=1000)
+    ap.add_argument("--serve-hmax", type=int, default=20000)
+    ap.add_argument("--serve-pool", type=int, default=48)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-active", type=int, default=16 << 20)
+    ap.add_argument("--serve-timeout", type=float, default=240.0)
     return ap.parse_args()
 
 
@@ -618,8 +628,85 @@ def cpu_baseline_batch(items, seconds):
             "sample": "first %d scenes of the mix, 35 steps each from their initial states (%.1f s)" % (k, dt)}
 
 
+def run_serve(args):
+    """c4: Poisson arrivals of scene requests (sizes log-uniform, horizons
+    uniform) served by continuous batching; reports aggregate particle-steps/s
+    and completion-latency percentiles of the requests that arrived in the
+    window.  Scene contents come from a seeded pool of pre-built scenes (the
+    cost of building 12k scenes on the host is not part of serving)."""
+    import torch
+    import build_lib
+    import dem
+    import dem_scenes
+    build_lib.build()
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(args.seed)
+    rate, window = args.serve_rate, args.serve_seconds
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * window * 2) + 16))
+    arrivals = arrivals[arrivals < window]
+    pool_n = np.exp(rng.uniform(np.log(args.serve_min), np.log(args.serve_max), args.serve_pool)).astype(int)
+    pool = [dem_scenes.c3_mix_scene(int(n), float(rng.uniform(0, 0.5)), 7919 * k + args.seed)
+            for k, n in enumerate(pool_n)]
+    pick = rng.integers(0, len(pool), size=len(arrivals))
+    horizons = rng.integers(args.serve_hmin, args.serve_hmax + 1, size=len(arrivals))
+    sv = dem.Server(device=local, memory_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
+                    max_active_particles=args.serve_active, reorder_interval=35)
+    t0 = time.perf_counter()
+    nxt = 0
+    submitted = {}
+    done = {}
+    max_queue = max_running = 0
+    chunk = 35
+    limit = t0 + args.serve_timeout
+    while len(done) < len(arrivals) and time.perf_counter() < limit:
+        now = time.perf_counter() - t0
+        while nxt < len(arrivals) and arrivals[nxt] <= now:
+            sc, p, ext = pool[pick[nxt]]
+            rid = sv.submit(sc, p, int(horizons[nxt]), **ext)
+            submitted[rid] = (nxt, int(sc["radii"].shape[0]) * int(horizons[nxt]))
+            nxt += 1
+        sv.advance(chunk)
+        st = sv.stats()
+        max_queue = max(max_queue, st["queued"])
+        max_running = max(max_running, st["running"])
+        tp = time.perf_counter() - t0
+        for rid in sv.poll():
+            k, work = submitted[rid]
+            sv.fetch(rid)
+            done[rid] = (k, tp - arrivals[k], work)
+        if st["running"] == 0 and st["queued"] == 0 and nxt < len(arrivals):
+            time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
+    elapsed = time.perf_counter() - t0
+    st = sv.stats()
+    sv.close()
+    lat = np.array([v[1] for v in done.values()]) if done else np.zeros(1)
+    value = st["particle_steps"] / elapsed
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": 1,
+            "steps": int(st["steps"]), "warmup": 0, "ms_per_step": elapsed / max(st["steps"], 1) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "c4 served stream", "arrival_rate_per_s": rate, "arrival_window_s": window,
+                       "requests": int(len(arrivals)), "completed": int(len(done)),
+                       "particles_per_request": "log-uniform [%d, %d] (pool of %d seeded scenes)"
+                       % (args.serve_min, args.serve_max, args.serve_pool),
+                       "horizon_steps": "uniform [%d, %d]" % (args.serve_hmin, args.serve_hmax),
+                       "memory_budget_gb": args.serve_budget_gb, "max_active_particles": args.serve_active,
+                       "capacity_particles": st["capacity_particles"], "device_bytes": st["device_bytes"],
+                       "max_queue": int(max_queue), "max_running": int(max_running),
+                       "advance_chunk_steps": chunk, "elapsed_s": elapsed},
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                          "p99": float(np.percentile(lat, 99)), "max": float(lat.max())}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.workload == "c4_serve":
+        run_serve(args)
+        return
     batch = args.workload == "c3_batch"
     if args.frame <= 0:
         args.frame = 35 if batch else 105

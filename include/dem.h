@@ -224,6 +224,51 @@ int dem_batch_break_events(dem_batch *b, dem_break_event *buf, int32_t cap, int3
 int dem_batch_get_stats(dem_batch *b, dem_stats *out);
 void *dem_batch_stream(dem_batch *b);
 
+/* ---- Serving: continuous batching of scene requests --------------------
+ * No counterpart in the reference.  A server owns device arenas sized once
+ * from memory_budget_bytes (and at most ~1.25 x max_active_particles
+ * particles, cells_per_particle cells and bonds_per_particle bonds per
+ * particle).  Requests (scene + settings + extensions + horizon in steps) are
+ * copied at submit and queue on the host.  dem_server_advance(sv, n): (1) the
+ * scenes that reached their horizon are copied back to host memory and their
+ * device ranges freed; (2) queued requests are admitted first come first
+ * served while their particles, cells and bonds fit in free ranges and the
+ * running particles stay within max_active_particles; (3) every admitted
+ * scene advances n steps in the same launches.  A scene stops exactly at its
+ * horizon even inside n, so each result equals the scene run alone for that
+ * many steps.  dem_server_poll lists completed ids; dem_server_fetch copies a
+ * result and its submit/admit/done times (seconds, monotonic clock). */
+typedef struct dem_server dem_server;
+typedef struct dem_server_config {
+    int64_t memory_budget_bytes;   /* device memory the arenas may use (default 150 GiB) */
+    int64_t max_active_particles;  /* admission limit on running particles (default 16 Mi) */
+    int32_t max_scenes;            /* concurrent scene slots (default 4096) */
+    float cells_per_particle;      /* search cells reserved per particle (default 4) */
+    float bonds_per_particle;      /* bond records reserved per particle (default 1) */
+    int32_t reserved;
+    dem_ext ext;                   /* world-wide options (graph steps, skin, block size) */
+} dem_server_config;
+typedef struct dem_server_stats {
+    int64_t queued, running, completed;
+    int64_t active_particles;      /* particles of running scenes */
+    int64_t particle_steps;        /* particle-steps executed so far */
+    int64_t capacity_particles, used_particles, device_bytes;
+    int64_t steps;                 /* steps of the shared world so far */
+} dem_server_stats;
+void dem_server_config_defaults(dem_server_config *cfg);
+int dem_server_create(const dem_server_config *cfg, int device, dem_server **out);
+void dem_server_destroy(dem_server *sv);
+const char *dem_server_last_error(const dem_server *sv);
+int dem_server_submit(dem_server *sv, const dem_scene *scene, const dem_params *params, const dem_ext *ext,
+                      int64_t horizon_steps, int64_t *request_id);
+int dem_server_advance(dem_server *sv, int32_t n_steps);
+int dem_server_poll(dem_server *sv, int64_t *done_ids, int32_t cap, int32_t *n);
+int dem_server_fetch(dem_server *sv, int64_t id, dem_scene *out, double times[3]);
+int dem_server_events(dem_server *sv, int64_t id, dem_break_event *buf, int32_t cap, int32_t *n);
+int dem_server_release(dem_server *sv, int64_t id);
+int dem_server_get_stats(dem_server *sv, dem_server_stats *out);
+void *dem_server_stream(dem_server *sv);
+
 /* Broad phase that allocates nothing.  No counterpart in the reference: it is
  * for callers that cannot call cudaMalloc (a framework whose pool owns the
  * device heap, an allocator that forbids it, a real-time loop that must not

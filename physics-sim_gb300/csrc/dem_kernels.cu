@@ -162,8 +162,8 @@ __device__ __forceinline__ bool last_warp(uint32_t *ticket) {
 __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     uint32_t m = w.meta[i];
     int s = (int)meta_scene(m);
+    if (!w.act[s]) return;
     const ScenePar &P = w.par[s];
-    if (!P.active) return;
     float4 p = w.pr[i];
     if (p.z == 0.0f) return;                                       // :83
     const float dT = P.p.dT;
@@ -264,8 +264,8 @@ __global__ void __launch_bounds__(256) k_keys(DevWorld w, const int32_t *gate) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
     uint32_t m = w.meta[i];
+    if (!w.act[meta_scene(m)]) return;  // frozen scenes keep their order and take no cells
     const ScenePar &P = w.par[meta_scene(m)];
-    if (!P.active) return;  // frozen scenes keep their order and take no cells
     float4 p = w.pr[i];
     uint32_t key;
     if (p.z == 0.0f) {
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(256) k_scatter(DevWorld w, const int32_t *gate
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
-    if (!w.par[meta_scene(w.meta[i])].active) return;
+    if (!w.act[meta_scene(w.meta[i])]) return;
     uint32_t key = w.keys[i];
     int slot = w.cell_start[key] + atomicSub(&w.cell_count[key], 1) - 1;
     w.sorted[slot] = i;
@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(256) k_inverse(DevWorld w, const int32_t *gate
         w.inv[old] = nw;
         w.src[nw] = old;
     }
-    if (!w.par[meta_scene(w.meta[t])].active) {
+    if (!w.act[meta_scene(w.meta[t])]) {
         w.inv[t] = t;
         w.src[t] = t;
     }
@@ -471,8 +471,11 @@ __global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o, const in
         o.s_thb[j * N + i] = w.s_thb[j * N + src];
     }
     // the cell-order list now names the new indices
-    const ScenePar &P = w.par[meta_scene(w.meta[src])];
-    if (P.active) w.sorted[i - P.particle_base + w.cell_start[P.cell_base]] = i;
+    const int ss = (int)meta_scene(w.meta[src]);
+    if (w.act[ss]) {
+        const ScenePar &P = w.par[ss];
+        w.sorted[i - P.particle_base + w.cell_start[P.cell_base]] = i;
+    }
 }
 
 // copy the permuted arrays back, so the live arrays keep their addresses
@@ -526,7 +529,7 @@ __global__ void __launch_bounds__(256) k_list_build(DevWorld w, const int32_t *g
     const ScenePar &P = w.par[meta_scene(m)];
     const float4 pa = w.pr[i];
     w.pbuild[i] = make_float2(pa.x, pa.y);
-    if (!P.active || pa.z == 0.0f) {
+    if (!w.act[meta_scene(m)] || pa.z == 0.0f) {
         w.nl_count[i] = 0;
         w.kbuild[i] = (uint32_t)P.dead_cell;
         return;
@@ -634,8 +637,8 @@ __device__ __forceinline__ void narrow_test(const DevWorld &w, const ScenePar &P
 __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr) {
     const uint32_t m = w.meta[i];
     const int s = (int)meta_scene(m);
+    if (!w.act[s]) return;
     const ScenePar &P = w.par[s];
-    if (!P.active) return;
     const float4 pa = w.pr[i];
     if (pa.z == 0.0f) {                                            // :113-118
         w.dF[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -901,6 +904,11 @@ __device__ void end_of_step(const DevWorld &w) {
         w.cc3[s] = 0;
         const ScenePar &P = w.par[s];
         w.det[s] = detect_at(P.p.collision_interval, P.cc1_0, next - P.step0) ? 1 : 0;
+        if (w.act[s]) {
+            const long long left = w.remaining[s] - 1;
+            w.remaining[s] = left;
+            if (left <= 0) w.act[s] = 0;  // a served scene stops at its horizon
+        }
     }
     __syncwarp();
     if (lane == 0) {
@@ -926,6 +934,23 @@ void launch_interact(const DevWorld &w, int block, cudaStream_t st) {
     (void)block;
     const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
     k_interact<<<g, IB, 0, st>>>(w);
+}
+
+// ------------------------------------------------------- free ranges
+__global__ void k_mark_free(DevWorld w, int first, int count, int free_scene) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int i = first + k;
+    w.meta[i] = (uint32_t)free_scene << 16;
+    w.pr[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    w.smask[i] = 0u;
+    w.nl_count[i] = 0;
+    w.orig[i] = k;
+}
+
+void launch_mark_free(const DevWorld &w, int first, int count, int free_scene, cudaStream_t st) {
+    if (count <= 0) return;
+    k_mark_free<<<(count + 255) / 256, 256, 0, st>>>(w, first, count, free_scene);
 }
 
 // ------------------------------------------------------- Set_Properties

@@ -65,7 +65,7 @@ struct ScenePar {
     int32_t use_f64;
     float lambda;
     int32_t has_strength;
-    int32_t active;        // 0 = frozen (skipped by every kernel)
+    int32_t active;        // host bookkeeping; the kernels read DevWorld::act
     int64_t step0;         // world step at which the scene's interval counter was cc1_0
     int32_t cc1_0;
     int32_t pair_base;     // first entry of the scene's material-pair table
@@ -124,6 +124,8 @@ struct DevWorld {
     int32_t *rebuild;           // 1 = the next rebuild body runs
     uint32_t *tickets;          // [2] last-block counters of k_lom and k_interact
     int32_t *det;               // [S] narrow phase runs in the current step
+    int32_t *act;               // [S] 1 = the scene steps; 0 = frozen (finished or free slot)
+    long long *remaining;       // [S] steps left before the scene freezes (served scenes)
 };
 
 // ---- stateless detection schedule -----------------------------------------
@@ -160,5 +162,7 @@ void launch_interact(const DevWorld &w, int block, cudaStream_t st);
 void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
                            const int32_t *d_props, int block, cudaStream_t st);
 int scan_tmp_size(int n);
+// mark particles [first, first + count) as unused: scene `free_scene`, radius 0
+void launch_mark_free(const DevWorld &w, int first, int count, int free_scene, cudaStream_t st);
 
 }  // namespace demgb

@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <climits>
 #include <limits>
 
 #include "dem_world_host.h"
@@ -24,6 +25,45 @@ static inline float bits2f(int32_t i) {
     float f;
     std::memcpy(&f, &i, 4);
     return f;
+}
+
+void RangeAlloc::reset(long long capacity) {
+    free_.clear();
+    cap_ = capacity;
+    used_ = 0;
+    if (capacity > 0) free_[0] = capacity;
+}
+
+long long RangeAlloc::alloc(long long n) {
+    if (n <= 0) return 0;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+        if (it->second >= n) {
+            long long off = it->first, len = it->second;
+            free_.erase(it);
+            if (len > n) free_[off + n] = len - n;
+            used_ += n;
+            return off;
+        }
+    }
+    return -1;
+}
+
+void RangeAlloc::release(long long off, long long n) {
+    if (n <= 0) return;
+    used_ -= n;
+    auto it = free_.emplace(off, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) {
+            pv->second += it->second;
+            free_.erase(it);
+        }
+    }
 }
 
 World::~World() {
@@ -112,6 +152,8 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
     w.rebuild = dalloc<int32_t>(owned, 1, ok);
     w.tickets = dalloc<uint32_t>(owned, 2, ok);
     w.det = dalloc<int32_t>(owned, S, ok);
+    w.act = dalloc<int32_t>(owned, S, ok);
+    w.remaining = dalloc<long long>(owned, S, ok);
     spare = w;
     particle_arrays(spare);
     if (!ok) {
@@ -126,6 +168,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
     CK(cudaMemsetAsync(w.nl_count, 0, sizeof(int32_t) * (size_t)(N > 0 ? N : 1), stream));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int32_t), stream));
     CK(cudaMemsetAsync(w.cc3, 0, sizeof(int32_t) * (size_t)S, stream));
+    CK(cudaMemsetAsync(w.act, 0, sizeof(int32_t) * (size_t)S, stream));
     CK(cudaMemcpyAsync(w.step, &host_step, sizeof(long long), cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
     return DEM_OK;
@@ -286,6 +329,17 @@ int World::force_rebuild() {
 int World::push_par(int s) {
     fill_par(sh[s]);
     CK(cudaMemcpyAsync(d.par + s, &sh[s].par, sizeof(ScenePar), cudaMemcpyHostToDevice, stream));
+    return DEM_OK;
+}
+
+// a scene steps (act = 1) for `steps` more steps, or freezes (act = 0)
+int World::push_active(int s, bool on, long long steps) {
+    int32_t a = on ? 1 : 0;
+    long long r = steps;
+    CK(cudaMemcpyAsync(d.act + s, &a, 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.remaining + s, &r, 8, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    sh[s].active = on;
     return DEM_OK;
 }
 
@@ -487,12 +541,151 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
         if (rc) return rc;
         rc = push_par(s);
         if (rc) return rc;
+        rc = push_active(s, true, LLONG_MAX);
+        if (rc) return rc;
         int32_t c3 = scenes[s]->coll_cont[3];
         CK(cudaMemcpyAsync(d.cc3 + s, &c3, 4, cudaMemcpyHostToDevice, stream));
     }
     CK(cudaStreamSynchronize(stream));
     rc = push_det();
     if (rc) return rc;
+    return force_rebuild();
+}
+
+long long World::bytes_per_particle() const {
+    // live + spare particle records, slots, broad phase and candidate lists
+    const long long rec = 7 * 16 + 3 * 4 + (long long)K * 5 * 4;
+    return 2 * rec + 4 * 4 + 4 + (long long)NL * 4 + 8 + 4;
+}
+
+int World::build_capacity(long long particles, long long cells, long long bonds, int scenes, int materials,
+                          const dem_ext &ext) {
+    if (particles <= 0 || cells <= 0 || scenes <= 0 || materials <= 0)
+        return fail(DEM_E_INVALID, "capacities must be positive");
+    if (scenes >= MAX_SCENES) return fail(DEM_E_INVALID, "too many scene slots");
+    if (particles > (1LL << 30) || cells > (1LL << 31) - 2 || bonds > (1LL << 30))
+        return fail(DEM_E_INVALID, "capacity too large");
+    if (ext.block_size) block = ext.block_size;
+    if (ext.reorder_interval > 0) graph_steps = ext.reorder_interval;
+    if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
+    use_graphs = ext.plain_launches == 0;
+    diagnostics = ext.diagnostics != 0;
+    const int S = scenes + 1;  // the last slot owns the unused particles
+    free_slot = scenes;
+    sh.assign(S, SceneHost{});
+    for (auto &h : sh) {
+        h.active = false;
+        h.params.collision_interval = 1;
+    }
+    const long long pairs = (long long)materials * 16;
+    uint32_t ev_cap = ext.event_capacity > 0 ? (uint32_t)ext.event_capacity : 1u << 18;
+    int rc = alloc((int)particles, (int)cells, (int)std::max(bonds, 1LL), S, materials, (int)pairs, ev_cap);
+    if (rc) return rc;
+    launch_mark_free(d, 0, (int)particles, free_slot, stream);
+    a_part.reset(particles);
+    a_cell.reset(cells);
+    a_bond.reset(std::max(bonds, 1LL));
+    a_mat.reset(materials);
+    a_pair.reset(pairs);
+    free_slots.clear();
+    for (int s = scenes - 1; s >= 0; --s) free_slots.push_back(s);
+    for (int s = 0; s < S; ++s) {
+        SceneHost &h = sh[s];
+        h.cell_base = 0;
+        h.n_cells = 1;
+        h.par.g_w = h.par.g_h = 1;
+        h.par.g_inv = 1.0f;
+        h.grid.cell_size = 1.0f;
+        h.grid.w = h.grid.h = 1;
+        rc = push_par(s);
+        if (rc) return rc;
+        rc = push_active(s, false, 0);
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(stream));
+    rc = push_det();
+    if (rc) return rc;
+    return force_rebuild();
+}
+
+int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e, long long horizon) {
+    if (free_slots.empty()) return fail(DEM_E_CAPACITY, "no free scene slot");
+    if (horizon <= 0) return fail(DEM_E_INVALID, "horizon must be > 0");
+    if (!(e.bond_lambda > 0.0f)) return fail(DEM_E_INVALID, "bond_lambda must be > 0");
+    SceneHost h;
+    h.params = params;
+    h.use_f64 = e.use_f64 ? 1 : 0;
+    h.lambda = e.bond_lambda;
+    h.cell_factor = 1.0f;
+    int rc = compute_layout(h, sc);
+    if (rc) return rc;
+    if (h.n_mat > 16) return fail(DEM_E_CAPACITY, "served scenes carry at most 16 materials");
+    long long pp = a_part.alloc(h.n);
+    long long pc = pp >= 0 ? a_cell.alloc(h.n_cells) : -1;
+    long long pb = pc >= 0 ? a_bond.alloc(h.n_bonds) : -1;
+    long long pm = pb >= 0 ? a_mat.alloc(h.n_mat) : -1;
+    long long pq = pm >= 0 ? a_pair.alloc((long long)h.n_mat * h.n_mat) : -1;
+    if (pq < 0) {
+        if (pm >= 0) a_mat.release(pm, h.n_mat);
+        if (pb >= 0) a_bond.release(pb, h.n_bonds);
+        if (pc >= 0) a_cell.release(pc, h.n_cells);
+        if (pp >= 0) a_part.release(pp, h.n);
+        return fail(DEM_E_CAPACITY, "no free range large enough");
+    }
+    const int s = free_slots.back();
+    free_slots.pop_back();
+    h.particle_base = (int)pp;
+    h.cell_base = (int)pc;
+    h.bond_base = (int)pb;
+    h.mat_base = (int)pm;
+    h.pair_base = (int)pq;
+    if (e.bond_normal_strength && h.n_bonds > 0)
+        h.bond_sn.assign(e.bond_normal_strength, e.bond_normal_strength + h.n_bonds);
+    if (e.bond_shear_strength && h.n_bonds > 0)
+        h.bond_ss.assign(e.bond_shear_strength, e.bond_shear_strength + h.n_bonds);
+    if (h.bond_sn.empty() != h.bond_ss.empty()) {
+        if (h.bond_sn.empty()) h.bond_sn.assign(h.n_bonds, params.bond_normal_strength);
+        if (h.bond_ss.empty()) h.bond_ss.assign(h.n_bonds, params.bond_shear_strength);
+    }
+    h.step0 = host_step;
+    h.cc0_0 = sc->coll_cont[0];
+    h.cc1_0 = sc->coll_cont[1];
+    h.cc2_0 = sc->coll_cont[2];
+    h.active = true;
+    sh[s] = h;
+    rc = stage_scene(s, sc);
+    if (rc == DEM_OK) rc = push_par(s);
+    if (rc == DEM_OK) {
+        int32_t c3 = sc->coll_cont[3];
+        cudaError_t ce = cudaMemcpyAsync(d.cc3 + s, &c3, 4, cudaMemcpyHostToDevice, stream);
+        if (ce != cudaSuccess) rc = fail(DEM_E_CUDA, cudaGetErrorString(ce));
+    }
+    if (rc == DEM_OK) rc = push_active(s, true, horizon);
+    if (rc == DEM_OK) rc = push_det();
+    if (rc == DEM_OK) rc = force_rebuild();
+    if (rc != DEM_OK) {
+        retire(s);
+        return rc;
+    }
+    return s;
+}
+
+int World::retire(int s) {
+    if (s < 0 || s >= (int)sh.size() || s == free_slot) return fail(DEM_E_INVALID, "bad scene slot");
+    SceneHost &h = sh[s];
+    int rc = push_active(s, false, 0);
+    if (rc) return rc;
+    launch_mark_free(d, h.particle_base, h.n, free_slot, stream);
+    CK(cudaStreamSynchronize(stream));
+    a_part.release(h.particle_base, h.n);
+    a_cell.release(h.cell_base, h.n_cells);
+    a_bond.release(h.bond_base, h.n_bonds);
+    a_mat.release(h.mat_base, h.n_mat);
+    a_pair.release(h.pair_base, (long long)h.n_mat * h.n_mat);
+    h = SceneHost{};
+    h.params.collision_interval = 1;
+    h.n_cells = 1;
+    free_slots.push_back(s);
     return force_rebuild();
 }
 

@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -38,6 +39,20 @@ struct SceneHost {
     ScenePar par;
 };
 
+// First-fit allocator of index ranges [0, capacity) with merging on release.
+class RangeAlloc {
+  public:
+    void reset(long long capacity);
+    long long alloc(long long n);  // offset, or -1 when no free range is long enough
+    void release(long long off, long long n);
+    long long used() const { return used_; }
+    long long capacity() const { return cap_; }
+
+  private:
+    std::map<long long, long long> free_;  // offset -> length
+    long long used_ = 0, cap_ = 0;
+};
+
 class World {
   public:
     World() = default;
@@ -58,9 +73,22 @@ class World {
     int sync();
     int drain_events(std::vector<dem_break_event> &out);
     int stats(dem_stats *out);
+    int push_active(int s, bool on, long long steps);
     int broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *cell_start, int32_t *n_cells);
     void control(int s, int32_t cc[4]) const;
     int set_control(int s, const int32_t cc[4]);
+
+    // capacity mode (served scenes): arenas allocated once, scenes admitted
+    // into free ranges and retired from them
+    int build_capacity(long long particles, long long cells, long long bonds, int scenes, int materials,
+                       const dem_ext &ext);
+    // admit a scene that will run `horizon` steps; returns its slot or a negative DEM_E_* code
+    int admit(const dem_scene *scene, const dem_params &params, const dem_ext &ext, long long horizon);
+    int retire(int slot);
+    int free_slot = -1;                 // scene index of unused particles (never active)
+    RangeAlloc a_part, a_cell, a_bond, a_mat, a_pair;
+    std::vector<int> free_slots;
+    long long bytes_per_particle() const;
 
     std::string err;
     cudaStream_t stream = nullptr;

@@ -85,6 +85,18 @@ class Stats(C.Structure):
                 ("kernel_launches", C.c_int64), ("list_overflows", C.c_int64)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("memory_budget_bytes", C.c_int64), ("max_active_particles", C.c_int64),
+                ("max_scenes", C.c_int32), ("cells_per_particle", C.c_float),
+                ("bonds_per_particle", C.c_float), ("reserved", C.c_int32), ("ext", Ext)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("queued", "running", "completed", "active_particles",
+                                         "particle_steps", "capacity_particles", "used_particles",
+                                         "device_bytes", "steps")]
+
+
 BREAK_DTYPE = np.dtype([("scene", "<i4"), ("step", "<i4"), ("bond", "<i4"), ("code", "<i4"),
                         ("a", "<i4"), ("b", "<i4")])
 
@@ -99,7 +111,10 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_batch_step", "dem_batch_synchronize", "dem_batch_download", "dem_batch_upload",
            "dem_batch_set_params", "dem_batch_set_properties", "dem_batch_break_events",
            "dem_batch_get_stats", "dem_batch_stream", "dem_batch_kernel_timing",
-           "dem_batch_kernel_time"]
+           "dem_batch_kernel_time", "dem_server_config_defaults", "dem_server_create",
+           "dem_server_destroy", "dem_server_last_error", "dem_server_submit", "dem_server_advance",
+           "dem_server_poll", "dem_server_fetch", "dem_server_events", "dem_server_release",
+           "dem_server_get_stats", "dem_server_stream"]
 
 _lib = None
 
@@ -167,10 +182,28 @@ def lib(path=None):
     L.dem_batch_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     L.dem_batch_stream.argtypes = [C.c_void_p]
     L.dem_batch_stream.restype = C.c_void_p
+    L.dem_server_config_defaults.argtypes = [C.POINTER(ServerConfig)]
+    L.dem_server_config_defaults.restype = None
+    L.dem_server_create.argtypes = [C.POINTER(ServerConfig), C.c_int, C.POINTER(C.c_void_p)]
+    L.dem_server_destroy.argtypes = [C.c_void_p]
+    L.dem_server_destroy.restype = None
+    L.dem_server_last_error.argtypes = [C.c_void_p]
+    L.dem_server_last_error.restype = C.c_char_p
+    L.dem_server_submit.argtypes = [C.c_void_p, C.POINTER(Scene), C.POINTER(Params), C.POINTER(Ext),
+                                    C.c_int64, C.POINTER(C.c_int64)]
+    L.dem_server_advance.argtypes = [C.c_void_p, C.c_int32]
+    L.dem_server_poll.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32)]
+    L.dem_server_fetch.argtypes = [C.c_void_p, C.c_int64, C.POINTER(Scene), C.POINTER(C.c_double)]
+    L.dem_server_events.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
+    L.dem_server_release.argtypes = [C.c_void_p, C.c_int64]
+    L.dem_server_get_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+    L.dem_server_stream.argtypes = [C.c_void_p]
+    L.dem_server_stream.restype = C.c_void_p
     for name in SYMBOLS:
         if name not in ("dem_destroy", "dem_ext_defaults", "dem_last_error", "dem_stream",
                         "dem_abi_version", "dem_noalloc_last_error", "dem_batch_destroy",
-                        "dem_batch_last_error", "dem_batch_stream"):
+                        "dem_batch_last_error", "dem_batch_stream", "dem_server_config_defaults",
+                        "dem_server_destroy", "dem_server_last_error", "dem_server_stream"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -468,6 +501,103 @@ class Batch:
 
     def stream(self):
         return lib().dem_batch_stream(self.h)
+
+
+class Server:
+    """Continuous batching of scene requests on one GPU (dem_server_*)."""
+
+    def __init__(self, *, device=-1, memory_budget_bytes=None, max_active_particles=None,
+                 max_scenes=None, cells_per_particle=None, bonds_per_particle=None, **ext_kw):
+        L = lib()
+        cfg = ServerConfig()
+        L.dem_server_config_defaults(C.byref(cfg))
+        if memory_budget_bytes is not None:
+            cfg.memory_budget_bytes = int(memory_budget_bytes)
+        if max_active_particles is not None:
+            cfg.max_active_particles = int(max_active_particles)
+        if max_scenes is not None:
+            cfg.max_scenes = int(max_scenes)
+        if cells_per_particle is not None:
+            cfg.cells_per_particle = float(cells_per_particle)
+        if bonds_per_particle is not None:
+            cfg.bonds_per_particle = float(bonds_per_particle)
+        self._keep = []
+        cfg.ext = make_ext(keep=self._keep, **ext_kw)
+        h = C.c_void_p()
+        rc = L.dem_server_create(C.byref(cfg), device, C.byref(h))
+        if rc != 0:
+            raise DemError(rc, (L.dem_server_last_error(None) or b"").decode())
+        self.h = h
+        self._templates = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().dem_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise DemError(rc, (lib().dem_server_last_error(self.h) or b"").decode())
+
+    def submit(self, scene, params, horizon, **ext_kw):
+        keep = []
+        st = make_scene(scene)
+        p = make_params(params)
+        e = make_ext(keep=keep, **ext_kw)
+        rid = C.c_int64(0)
+        self._check(lib().dem_server_submit(self.h, C.byref(st), C.byref(p), C.byref(e), int(horizon),
+                                            C.byref(rid)))
+        self._templates[rid.value] = {k: (v.copy() if hasattr(v, "copy") else v) for k, v in scene.items()
+                                      if k in F32_KEYS + I32_KEYS + ("grid",)}
+        return rid.value
+
+    def advance(self, n):
+        self._check(lib().dem_server_advance(self.h, int(n)))
+
+    def poll(self, cap=4096):
+        ids = (C.c_int64 * cap)()
+        n = C.c_int32(0)
+        self._check(lib().dem_server_poll(self.h, ids, cap, C.byref(n)))
+        return [ids[k] for k in range(n.value)]
+
+    def fetch(self, rid, release=True):
+        out = empty_like_scene(self._templates[rid])
+        st = make_scene(out)
+        times = (C.c_double * 3)()
+        self._check(lib().dem_server_fetch(self.h, int(rid), C.byref(st), times))
+        out["coll_cont"] = np.array(st.coll_cont[:], dtype=np.int32)
+        ev = self.events(rid)
+        if release:
+            self._check(lib().dem_server_release(self.h, int(rid)))
+            self._templates.pop(rid, None)
+        return out, (times[0], times[1], times[2]), ev
+
+    def events(self, rid):
+        n = C.c_int32(0)
+        self._check(lib().dem_server_events(self.h, int(rid), None, 0, C.byref(n)))
+        buf = np.zeros(max(n.value, 1), dtype=BREAK_DTYPE)
+        self._check(lib().dem_server_events(self.h, int(rid), buf.ctypes.data, n.value, C.byref(n)))
+        return buf[: n.value].copy()
+
+    def stats(self):
+        s = ServerStats()
+        self._check(lib().dem_server_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def stream(self):
+        return lib().dem_server_stream(self.h)
 
 
 def grid_capacity(params, radii, particles):

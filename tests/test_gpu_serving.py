@@ -1,0 +1,89 @@
+"""Serving: scenes admitted while others run, each stopping at its own
+horizon, give exactly the results of running them alone."""
+import numpy as np
+import pytest
+
+import dem
+import dem_scenes
+from gpu_backend import assert_same_state
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import build_lib
+    build_lib.build()
+
+
+def _alone(sc, p, ext, steps):
+    with dem.Context(sc, p, **ext) as ctx:
+        ctx.step(steps)
+        return ctx.download(), ctx.break_events()
+
+
+def _ev(ev):
+    return sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in ev)
+
+
+def test_each_result_equals_the_scene_alone():
+    reqs = [
+        (dem_scenes.c3_mix_scene(1500, 0.3, 11), 100),
+        (dem_scenes.dense_bed(900, seed=12), 70),
+        (dem_scenes.c1_chains(chains=3, length=24, seed=13, pull_velocity=20.0), 130),
+        (dem_scenes.c3_mix_scene(2200, 0.0, 14), 45),
+        (dem_scenes.c3_mix_scene(700, 0.5, 15), 60),
+    ]
+    with dem.Server(memory_budget_bytes=1 << 30, max_active_particles=4000, max_scenes=8,
+                    reorder_interval=35) as sv:
+        ids = {}
+        # two requests up front, the others arrive while those run
+        for k in (0, 1):
+            (sc, p, ext), h = reqs[k]
+            ids[sv.submit(sc, p, h, **ext)] = k
+        sv.advance(35)
+        (sc, p, ext), h = reqs[2]
+        ids[sv.submit(sc, p, h, **ext)] = 2
+        sv.advance(35)
+        for k in (3, 4):
+            (sc, p, ext), h = reqs[k]
+            ids[sv.submit(sc, p, h, **ext)] = k
+        done = {}
+        for _ in range(40):
+            sv.advance(35)
+            for rid in sv.poll():
+                done[rid] = sv.fetch(rid)
+            if len(done) == len(reqs):
+                break
+        st = sv.stats()
+    assert len(done) == len(reqs), st
+    admits = {}
+    for rid, (got, times, ev) in done.items():
+        k = ids[rid]
+        (sc, p, ext), h = reqs[k]
+        ref, rev = _alone(sc, p, ext, h)
+        assert_same_state(got, ref, "request %d: " % k)
+        assert _ev(ev) == _ev(rev)
+        admits[k] = times[1]
+        assert times[0] <= times[1] <= times[2]
+    # max_active_particles = 4000 delays request 3 (2200 particles) until room frees
+    assert admits[3] >= admits[2]
+
+
+def test_capacity_refuses_nothing_and_queues():
+    sc, p, ext = dem_scenes.dense_bed(3000, seed=21)
+    with dem.Server(memory_budget_bytes=1 << 30, max_active_particles=3000, max_scenes=4) as sv:
+        a = sv.submit(sc, p, 40)
+        b = sv.submit(sc, p, 40)
+        sv.advance(35)
+        s1 = sv.stats()
+        assert s1["running"] == 1 and s1["queued"] == 1
+        out = {}
+        for _ in range(10):
+            sv.advance(35)
+            for rid in sv.poll():
+                out[rid] = sv.fetch(rid)
+        assert set(out) == {a, b}
+        ga, _, _ = out[a]
+        gb, _, _ = out[b]
+        assert_same_state(ga, gb)
