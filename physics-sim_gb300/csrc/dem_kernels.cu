@@ -35,6 +35,23 @@ __device__ __forceinline__ void ref_range(const ScenePar &P, float px, float py,
     y1 = d < P.ref_h - 1 ? d : P.ref_h - 1;
 }
 
+// The range packed in 16-bit fields: an empty side (x0 beyond the grid or x1
+// below it) is stored as w (resp. -1), which intersects no range exactly as
+// the unclamped value does.  Grids are limited to 32766 buckets per side.
+__device__ __forceinline__ int2 pack_range(const ScenePar &P, int x0, int x1, int y0, int y1) {
+    x0 = x0 < P.ref_w ? x0 : P.ref_w;
+    y0 = y0 < P.ref_h ? y0 : P.ref_h;
+    x1 = x1 >= 0 ? x1 : -1;
+    y1 = y1 >= 0 ? y1 : -1;
+    return make_int2((x0 & 0xFFFF) | (x1 << 16), (y0 & 0xFFFF) | (y1 << 16));
+}
+__device__ __forceinline__ void unpack_range(int2 r, int &x0, int &x1, int &y0, int &y1) {
+    x0 = (int)(short)(r.x & 0xFFFF);
+    x1 = r.x >> 16;
+    y0 = (int)(short)(r.y & 0xFFFF);
+    y1 = r.y >> 16;
+}
+
 // search-grid cell of a position (floor, clamped to the grid)
 __device__ __forceinline__ void search_xy(const ScenePar &P, float x, float y, int &cx, int &cy) {
     int a = __float2int_rd((x - P.g_x0) * P.g_inv);
@@ -224,6 +241,11 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     p.y = p.y + d.y;
     p.w = p.w + d.z;                                               // :149
     w.pr[i] = p;
+    {
+        int x0, x1, y0, y1;                                        // 2D_LOM.wgsl:167-178
+        ref_range(P, p.x, p.y, p.z, x0, x1, y0, y1);
+        w.rr[i] = pack_range(P, x0, x1, y0, y1);
+    }
     w.vw[i] = make_float4(ivx, ivy, iw, v.w);                      // :151-152
     if (!ext) w.dp[i] = d;
     const float2 b = w.pbuild[i];
@@ -460,6 +482,7 @@ __global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o, const in
     o.meta[i] = w.meta[src];
     o.orig[i] = w.orig[src];
     o.smask[i] = w.smask[src];
+    o.rr[i] = w.rr[src];
     const int N = w.N;
 #pragma unroll 2
     for (int j = 0; j < K; ++j) {
@@ -495,6 +518,7 @@ __global__ void __launch_bounds__(256) k_copy_back(DevWorld w, DevWorld o, const
     w.meta[i] = o.meta[i];
     w.orig[i] = o.orig[i];
     w.smask[i] = o.smask[i];
+    w.rr[i] = o.rr[i];
     const int N = w.N;
 #pragma unroll 2
     for (int j = 0; j < K; ++j) {
@@ -621,7 +645,7 @@ __device__ __forceinline__ void narrow_test(const DevWorld &w, const ScenePar &P
     if (s2 > (t * t) * 1.000001f) return;                         // cannot pass the test below
     if (!(sqrtf(s2) < t)) return;                                  // :159
     int bx0, bx1, by0, by1;
-    ref_range(P, pb.x, pb.y, pb.z, bx0, bx1, by0, by1);
+    unpack_range(__ldg(&w.rr[b]), bx0, bx1, by0, by1);
     if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) return;
     const int fy = by0 > ay0 ? by0 : ay0;
     const int fx = bx0 > ax0 ? bx0 : ax0;
@@ -654,7 +678,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     if (detect) {                                                  // :126-228
         nr.cnt = 0;
         int ax0, ax1, ay0, ay1;
-        ref_range(P, pa.x, pa.y, pa.z, ax0, ax1, ay0, ay1);
+        unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
         const int lc = w.nl_count[i];
         if (lc != NL_OVERFLOW) {
             for (int k = 0; k < lc; ++k) narrow_test(w, P, i, __ldg(&w.nl_items[k * N + i]), pa, ax0, ax1, ay0, ay1, nr);
@@ -672,12 +696,19 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         const int cnt = nr.cnt;
         const int t = threadIdx.x;
         if (cnt == K) atomicAdd(&w.stats[0], 1ull);
-        // delete contacts that were not found (:185-204)
+        // delete contacts that were not found (:185-204); `matched` marks the
+        // accepted partners that already own a slot
+        uint32_t matched = 0u;
+        const uint32_t before = mask;
         for (uint32_t left = mask; left; left &= left - 1) {
             const int j = __ffs(left) - 1;
             const int sb = w.s_b[j * N + i];
             bool found = false;
-            for (int q = 0; q < cnt; ++q) found |= (nr.ci[q * IB + t] == sb);
+            for (int q = 0; q < cnt; ++q) {
+                const bool hit = nr.ci[q * IB + t] == sb;
+                found |= hit;
+                matched |= hit ? (1u << q) : 0u;
+            }
             if (found) continue;
             const int bonded = w.s_bonded[j * N + i];
             if (bonded < 0 || bonds_model == 0) {
@@ -686,21 +717,19 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 w.s_tf[j * N + i] = 0.0f;
             }
         }
-        // create new contacts in the last empty slot (:207-227)
+        // create new contacts in the last empty slot (:207-227); a deleted
+        // slot never holds an accepted partner, so `matched` is the
+        // reference's "existing" test
         for (int q = 0; q < cnt; ++q) {
-            const int c = nr.ci[q * IB + t];
-            bool existing = false;
-            for (uint32_t left = mask; left && !existing; left &= left - 1)
-                existing = w.s_b[(__ffs(left) - 1) * N + i] == c;
-            if (existing) continue;
+            if ((matched >> q) & 1u) continue;
             const uint32_t empty = (~mask) & ((1u << K) - 1u);
             if (empty == 0u) continue;
             const int j = 31 - __clz(empty);
             mask |= 1u << j;
-            w.s_b[j * N + i] = c;
+            w.s_b[j * N + i] = nr.ci[q * IB + t];
             w.s_tf[j * N + i] = 0.0f;
         }
-        w.smask[i] = mask;
+        if (mask != before) w.smask[i] = mask;
     }
 
     // force loop (:230-255), slots in ascending order

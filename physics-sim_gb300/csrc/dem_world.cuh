@@ -93,6 +93,7 @@ struct DevWorld {
     uint32_t *meta;
     int32_t *orig;
     uint32_t *smask;
+    int2 *rr;                   // reference bucket range of the AABB: {x0 | x1 << 16, y0 | y1 << 16}
     int32_t *s_b, *s_bonded;
     float *s_tf, *s_btf, *s_thb;
     int32_t *b_status;

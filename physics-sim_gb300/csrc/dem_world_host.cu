@@ -115,6 +115,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
         x.meta = dalloc<uint32_t>(owned, N, ok);
         x.orig = dalloc<int32_t>(owned, N, ok);
         x.smask = dalloc<uint32_t>(owned, N, ok);
+        x.rr = dalloc<int2>(owned, N, ok);
         x.s_b = dalloc<int32_t>(owned, (size_t)K * N, ok);
         x.s_bonded = dalloc<int32_t>(owned, (size_t)K * N, ok);
         x.s_tf = dalloc<float>(owned, (size_t)K * N, ok);
@@ -223,6 +224,7 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
         if (dem_grid_capacity(&h.params, sc->radii, n, n, &g) != 0)
             return fail(DEM_E_INVALID, "cannot derive the bucket grid");
     }
+    if (g.w > 32766 || g.h > 32766) return fail(DEM_E_UNSUPPORTED, "bucket grid wider than 32766 cells");
     h.grid = g;
     // search grid: centre-binned cells of side >= 2 r_max (1 + pad), covering the
     // walls (or the particles, whichever is smaller in cells)
@@ -554,7 +556,7 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
 
 long long World::bytes_per_particle() const {
     // live + spare particle records, slots, broad phase and candidate lists
-    const long long rec = 7 * 16 + 3 * 4 + (long long)K * 5 * 4;
+    const long long rec = 7 * 16 + 3 * 4 + 8 + (long long)K * 5 * 4;
     return 2 * rec + 4 * 4 + 4 + (long long)NL * 4 + 8 + 4;
 }
 
