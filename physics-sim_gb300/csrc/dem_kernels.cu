@@ -253,10 +253,13 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     if (!(ex * ex + ey * ey <= P.disp_limit2)) atomicOr(w.rebuild, 1);
 }
 
+// With w.ticket the kernel's last warp sets the rebuild conditional; without
+// it (large worlds, where thousands of fenced ticket atomics cost more than a
+// launch) k_decide does it.
 __global__ void __launch_bounds__(256) k_lom(DevWorld w, int in_graph, cudaGraphConditionalHandle cond) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < w.N) lom_particle(w, i);
-    if (last_warp(&w.tickets[0])) {
+    if (w.ticket && last_warp(&w.tickets[0])) {
         if ((threadIdx.x & 31) == 0) {
             int need = *(volatile int32_t *)w.rebuild;
             if (in_graph) cudaGraphSetConditional(cond, need != 0 ? 1u : 0u);
@@ -265,10 +268,22 @@ __global__ void __launch_bounds__(256) k_lom(DevWorld w, int in_graph, cudaGraph
     }
 }
 
-void launch_lom(const DevWorld &w, int block, cudaStream_t st, bool in_graph,
-                cudaGraphConditionalHandle cond) {
-    if (w.N == 0) return;
-    k_lom<<<(w.N + block - 1) / block, block, 0, st>>>(w, in_graph ? 1 : 0, cond);
+__global__ void k_decide(DevWorld w, cudaGraphConditionalHandle cond) {
+    if (threadIdx.x == 0) cudaGraphSetConditional(cond, *(volatile int32_t *)w.rebuild != 0 ? 1u : 0u);
+}
+
+int launch_lom(const DevWorld &w, int block, cudaStream_t st, bool in_graph,
+               cudaGraphConditionalHandle cond) {
+    int k = 0;
+    if (w.N > 0) {
+        k_lom<<<(w.N + block - 1) / block, block, 0, st>>>(w, in_graph ? 1 : 0, cond);
+        k++;
+    }
+    if (in_graph && (!w.ticket || w.N == 0)) {
+        k_decide<<<1, 32, 0, st>>>(w, cond);
+        k++;
+    }
+    return k;
 }
 
 // ------------------------------------------------------------ broad phase
@@ -916,7 +931,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     w.dF[i] = make_float4(acc.d0, acc.d1, acc.d2, 0.0f);
 }
 
-// End of step, run by the last block of k_interact: breaks of this step
+// End of step, run by one warp (the last warp of k_interact, or k_end_step): breaks of this step
 // become visible (status = min code), the positions-set flags clear
 // (2D_Simulation.wgsl:258-261), the step counter advances, and each scene's
 // narrow-phase flag for the next step is set.
@@ -956,13 +971,18 @@ __global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w) {
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < w.N) interact_particle(w, i, nr);
-    if (last_warp(&w.tickets[1])) end_of_step(w);
+    if (w.ticket && last_warp(&w.tickets[1])) end_of_step(w);
 }
 
-void launch_interact(const DevWorld &w, int block, cudaStream_t st) {
+__global__ void k_end_step(DevWorld w) { end_of_step(w); }
+
+int launch_interact(const DevWorld &w, int block, cudaStream_t st) {
     (void)block;
     const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
     k_interact<<<g, IB, 0, st>>>(w);
+    if (w.ticket) return 1;
+    k_end_step<<<1, 32, 0, st>>>(w);
+    return 2;
 }
 
 // ------------------------------------------------------- free ranges

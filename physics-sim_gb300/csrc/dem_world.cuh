@@ -123,7 +123,8 @@ struct DevWorld {
     float2 *pbuild;             // [N] position at the last rebuild
     uint32_t *kbuild;           // [N] search cell at the last rebuild
     int32_t *rebuild;           // 1 = the next rebuild body runs
-    uint32_t *tickets;          // [2] last-block counters of k_lom and k_interact
+    uint32_t *tickets;          // [2] last-warp counters of k_lom and k_interact
+    int32_t ticket;             // 1: those kernels' last warps end the step; 0: separate one-warp kernels
     int32_t *det;               // [S] narrow phase runs in the current step
     int32_t *act;               // [S] 1 = the scene steps; 0 = frozen (finished or free slot)
     long long *remaining;       // [S] steps left before the scene freezes (served scenes)
@@ -150,16 +151,22 @@ __host__ __device__ inline int32_t cc1_after(int32_t interval, int32_t cc1_0, lo
     return (int32_t)since;
 }
 
+// Worlds up to this many particles end LOM and Simulation passes by last-warp
+// election (no extra launches); larger ones use two one-warp kernels instead,
+// because the fenced per-warp ticket costs ~0.4 ns x warps on each kernel.
+constexpr int TICKET_MAX_N = 131072;
+
 // host launchers (dem_kernels.cu)
-// LOM of one step; with in_graph its last block sets the rebuild conditional
-void launch_lom(const DevWorld &w, int block, cudaStream_t st, bool in_graph,
+// LOM of one step; with in_graph the rebuild conditional is set on the device.
+// Both launchers return the number of kernels they launched.
+int launch_lom(const DevWorld &w, int block, cudaStream_t st, bool in_graph,
                 cudaGraphConditionalHandle cond);
 void launch_keys(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
 int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
 void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStream_t st,
                     const int32_t *gate);
 void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
-void launch_interact(const DevWorld &w, int block, cudaStream_t st);
+int launch_interact(const DevWorld &w, int block, cudaStream_t st);
 void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
                            const int32_t *d_props, int block, cudaStream_t st);
 int scan_tmp_size(int n);

@@ -104,6 +104,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
     bool ok = true;
     DevWorld &w = d;
     w.N = N; w.C = C; w.B = B; w.S = S; w.M = M; w.MP = MP;
+    w.ticket = N <= TICKET_MAX_N ? 1 : 0;
     auto particle_arrays = [&](DevWorld &x) {
         x.pr = dalloc<float4>(owned, N, ok);
         x.vw = dalloc<float4>(owned, N, ok);
@@ -839,15 +840,15 @@ void World::enqueue_plain_step() {
         (void)begin;
     };
     rec(T_LOM, true);
-    launch_lom(d, block, stream, false, cudaGraphConditionalHandle{});
+    int k = launch_lom(d, block, stream, false, cudaGraphConditionalHandle{});
     rec(T_LOM, false);
     rec(T_BROAD, true);
     enqueue_rebuild(stream, d.rebuild);
     rec(T_BROAD, false);
     rec(T_INTERACT, true);
-    launch_interact(d, block, stream);
+    k += launch_interact(d, block, stream);
     rec(T_INTERACT, false);
-    launches += 2 + rebuild_kernels;
+    launches += k + rebuild_kernels;
     host_step++;
 }
 
@@ -873,7 +874,8 @@ void World::drop_graph() {
 
 // Capture R steps as one graph: per step the LOM kernel, a conditional node
 // whose body is the rebuild (its condition is set on the device by the LOM
-// kernel's last block), and the Simulation kernel.
+// kernel's last warp or by k_decide), and the Simulation kernel (followed by
+// k_end_step in large worlds).
 int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
     if (!side) CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -884,7 +886,7 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
         CKG(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
         cudaGraphConditionalHandle h;
         CKG(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
-        launch_lom(d, block, stream, true, h);
+        kernels += launch_lom(d, block, stream, true, h);
         const cudaGraphNode_t *deps = nullptr;
         size_t ndeps = 0;
         CKG(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &ndeps));
@@ -901,8 +903,7 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
         cudaGraph_t body_out = nullptr;
         CKG(cudaStreamEndCapture(side, &body_out));
         CKG(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-        launch_interact(d, block, stream);
-        kernels += 2;
+        kernels += launch_interact(d, block, stream);
     }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(stream, &g);

@@ -72,6 +72,21 @@ def test_chains_with_breaks_bit_exact():
     assert got == ref
 
 
+def test_large_world_end_of_step_kernels_bit_exact():
+    """Above 131072 particles the step ends in separate one-warp kernels
+    (rebuild decision, break application, counters) instead of the last warp
+    of the LOM and Simulation kernels; breaks, events and state must not
+    change."""
+    sc, p, ext = dem_scenes.c1_chains(chains=640, length=256, seed=3, pull_velocity=20.0)
+    assert sc["radii"].size > 131072
+    g, o, gev, oev = run_both(sc, p, 300, chunk=100, **ext)
+    assert len(oev) > 0, "the pull must break bonds"
+    assert_same_state(g, o)
+    got = sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in gev)
+    ref = sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in oev)
+    assert got == ref
+
+
 @pytest.mark.parametrize("model", [1, 2, 3])
 def test_bond_models_bit_exact(model):
     sc, p, ext = dem_scenes.c1_chains(chains=3, length=24, seed=5, pull_velocity=8.0)
