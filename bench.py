@@ -58,6 +58,9 @@ def parse_args():
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-active", type=int, default=16 << 20)
     ap.add_argument("--serve-timeout", type=float, default=240.0)
+    ap.add_argument("--plain", action="store_true",
+                    help="plain kernel launches instead of CUDA graphs, so that ncu can list every "
+                         "launch (a profiling aid, not a bench configuration)")
     return ap.parse_args()
 
 
@@ -282,7 +285,7 @@ def run_ours(args):
     sc, p, ext, desc = build_workload(args.workload)
     n = int(sc["radii"].shape[0])
     F = args.frame
-    ctx = dem.Context(sc, p, device=local, reorder_interval=21, **ext)
+    ctx = dem.Context(sc, p, device=local, reorder_interval=21, plain_launches=args.plain, **ext)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -455,7 +458,7 @@ def run_ours_batch(args):
     items, desc = build_batch_workload(args.scenes, args.seed + rank)
     ntot = sum(int(it[0]["radii"].shape[0]) for it in items)
     F = args.frame
-    batch = dem.Batch(items, device=local, reorder_interval=35)
+    batch = dem.Batch(items, device=local, reorder_interval=35, plain_launches=args.plain)
     stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -503,7 +506,7 @@ def run_ours_batch(args):
     plain_ms = 0.0
     plain_ps = 0
     for sc, p, ext in items:
-        ctx = dem.Context(sc, p, device=local, reorder_interval=35, **ext)
+        ctx = dem.Context(sc, p, device=local, reorder_interval=35, plain_launches=args.plain, **ext)
         cst = torch.cuda.ExternalStream(ctx.stream(), device=dev)
         ctx.step(35)
         ctx.synchronize()

@@ -558,8 +558,9 @@ void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStr
 // After the reorder, each particle collects the particles of the 3x3 search
 // cells around it whose centres lie within ra + rb + skin: a superset of
 // every pair the reference can accept while no particle moves more than
-// skin/2.  More than NL candidates: the particle searches the cell table
-// (built in the same rebuild) at every step instead.
+// skin/2.  More than NL candidates, or one farther than an int16 offset can
+// reach: the particle searches the cell table (built in the same rebuild) at
+// every step instead.
 __global__ void __launch_bounds__(256) k_list_build(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -568,15 +569,15 @@ __global__ void __launch_bounds__(256) k_list_build(DevWorld w, const int32_t *g
     const ScenePar &P = w.par[meta_scene(m)];
     const float4 pa = w.pr[i];
     w.pbuild[i] = make_float2(pa.x, pa.y);
+    int16_t *h = reinterpret_cast<int16_t *>(w.nl + 2 * (size_t)i);
     if (!w.act[meta_scene(m)] || pa.z == 0.0f) {
-        w.nl_count[i] = 0;
+        h[0] = 0;
         w.kbuild[i] = (uint32_t)P.dead_cell;
         return;
     }
     int gx, gy;
     search_xy(P, pa.x, pa.y, gx, gy);
     w.kbuild[i] = (uint32_t)(P.cell_base + gy * P.g_w + gx);
-    const int N = w.N;
     const int cy0 = max(gy - 1, 0), cy1 = min(gy + 1, P.g_h - 1);
     const int cx0 = max(gx - 1, 0), cx1 = min(gx + 1, P.g_w - 1);
     int cnt = 0;
@@ -592,12 +593,13 @@ __global__ void __launch_bounds__(256) k_list_build(DevWorld w, const int32_t *g
             const float dx = pb.x - pa.x, dy = pb.y - pa.y;
             const float t = (pa.z + pb.z + P.skin) * 1.00001f;
             if (dx * dx + dy * dy > t * t) continue;
-            if (cnt < NL) w.nl_items[cnt * N + i] = b;
+            const int off = b - i;
+            if (cnt < NL && off >= -32768 && off <= 32767) h[1 + cnt] = (int16_t)off;
             else over = true;
             ++cnt;
         }
     }
-    w.nl_count[i] = over ? NL_OVERFLOW : cnt;
+    h[0] = (int16_t)(over ? NL_OVERFLOW : cnt);
     if (over) atomicAdd(&w.stats[5], 1ull);
 }
 
@@ -650,15 +652,19 @@ __device__ __forceinline__ void top14_insert(uint32_t key, int idx, Narrow &nr) 
     if (nr.cnt < K) ++nr.cnt;
 }
 
-__device__ __forceinline__ void narrow_test(const DevWorld &w, const ScenePar &P, int i, int b, float4 pa,
-                                            int ax0, int ax1, int ay0, int ay1, Narrow &nr) {
-    if (b == i) return;
-    const float4 pb = __ldg(&w.pr[b]);
+// |p_b - p_a| < r_b + r_a (2D_Simulation.wgsl:159)
+__device__ __forceinline__ bool touching(float4 pa, float4 pb) {
     const float dx = pb.x - pa.x, dy = pb.y - pa.y;
     const float s2 = dx * dx + dy * dy;
     const float t = pb.z + pa.z;
-    if (s2 > (t * t) * 1.000001f) return;                         // cannot pass the test below
-    if (!(sqrtf(s2) < t)) return;                                  // :159
+    if (s2 > (t * t) * 1.000001f) return false;                   // cannot pass the test below
+    return sqrtf(s2) < t;
+}
+
+// b passed the distance test: keep it when its AABB shares a reference
+// bucket with the particle's, keyed by the first shared bucket
+__device__ __forceinline__ void accept_partner(const DevWorld &w, int b, int ax0, int ax1, int ay0, int ay1,
+                                               Narrow &nr) {
     int bx0, bx1, by0, by1;
     unpack_range(__ldg(&w.rr[b]), bx0, bx1, by0, by1);
     if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) return;
@@ -673,6 +679,21 @@ __device__ __forceinline__ void narrow_test(const DevWorld &w, const ScenePar &P
     top14_insert(key, b, nr);
 }
 
+__device__ __forceinline__ void narrow_test(const DevWorld &w, int i, int b, float4 pa, int ax0, int ax1,
+                                            int ay0, int ay1, Narrow &nr) {
+    if (b == i) return;
+    if (!touching(pa, __ldg(&w.pr[b]))) return;
+    accept_partner(w, b, ax0, ax1, ay0, ay1, nr);
+}
+
+// entry k (0..15) of a candidate list held in two int4
+__device__ __forceinline__ int nl_entry(int4 a, int4 b, int k) {
+    const int q = k >> 1;
+    const int v = q == 0 ? a.x : q == 1 ? a.y : q == 2 ? a.z : q == 3 ? a.w
+                : q == 4 ? b.x : q == 5 ? b.y : q == 6 ? b.z : b.w;
+    return (k & 1) ? (v >> 16) : (int)(int16_t)(v & 0xFFFF);
+}
+
 __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr) {
     const uint32_t m = w.meta[i];
     const int s = (int)meta_scene(m);
@@ -684,20 +705,31 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         return;
     }
     const int N = w.N;
-    const float4 da = w.dp[i];
-    const Mat MA = w.mats[P.mat_base + meta_mat(m)];
     uint32_t mask = w.smask[i];
+    const uint32_t before = mask;
     const int bonds_model = P.p.bonds;
 
+    // Loads that only some particles need (the bucket range, the second half
+    // of the candidate list, del_pos) wait until the particle needs them.
     const bool detect = P.p.collisions == 1 && w.det[s] != 0;
     if (detect) {                                                  // :126-228
         nr.cnt = 0;
         int ax0, ax1, ay0, ay1;
-        unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
-        const int lc = w.nl_count[i];
+        const int4 la = __ldg(&w.nl[2 * (size_t)i]);
+        const int lc = la.x & 0xFFFF;
         if (lc != NL_OVERFLOW) {
-            for (int k = 0; k < lc; ++k) narrow_test(w, P, i, __ldg(&w.nl_items[k * N + i]), pa, ax0, ax1, ay0, ay1, nr);
+            const int4 lb = lc > 7 ? __ldg(&w.nl[2 * (size_t)i + 1]) : make_int4(0, 0, 0, 0);
+            // distance tests first, all gathers independent; then the bucket
+            // test and ordering of the partners that touch
+            uint32_t pass = 0u;
+#pragma unroll
+            for (int k = 1; k <= NL; ++k)
+                if (k <= lc && touching(pa, __ldg(&w.pr[i + nl_entry(la, lb, k)]))) pass |= 1u << k;
+            if (pass) unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
+            for (; pass; pass &= pass - 1)
+                accept_partner(w, i + nl_entry(la, lb, __ffs(pass) - 1), ax0, ax1, ay0, ay1, nr);
         } else {
+            unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
             const int local = (int)w.kbuild[i] - P.cell_base;
             const int gx = local % P.g_w, gy = local / P.g_w;
             const int cy0 = max(gy - 1, 0), cy1 = min(gy + 1, P.g_h - 1);
@@ -705,7 +737,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             for (int cy = cy0; cy <= cy1; ++cy) {
                 const int row = P.cell_base + cy * P.g_w;
                 const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
-                for (int k = beg; k < end; ++k) narrow_test(w, P, i, w.sorted[k], pa, ax0, ax1, ay0, ay1, nr);
+                for (int k = beg; k < end; ++k) narrow_test(w, i, w.sorted[k], pa, ax0, ax1, ay0, ay1, nr);
             }
         }
         const int cnt = nr.cnt;
@@ -714,8 +746,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         // delete contacts that were not found (:185-204); `matched` marks the
         // accepted partners that already own a slot
         uint32_t matched = 0u;
-        const uint32_t before = mask;
-        for (uint32_t left = mask; left; left &= left - 1) {
+        for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
             const int j = __ffs(left) - 1;
             const int sb = w.s_b[j * N + i];
             bool found = false;
@@ -725,10 +756,10 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 matched |= hit ? (1u << q) : 0u;
             }
             if (found) continue;
-            const int bonded = w.s_bonded[j * N + i];
-            if (bonded < 0 || bonds_model == 0) {
+            const bool bonded_nn = (mask >> (BSHIFT + j)) & 1u;   // bonded >= 0
+            if (!bonded_nn || bonds_model == 0) {
                 mask &= ~(1u << j);
-            } else if (bonded > 0 && bonds_model <= 1) {
+            } else if (bonds_model <= 1 && w.s_bonded[j * N + i] > 0) {
                 w.s_tf[j * N + i] = 0.0f;
             }
         }
@@ -744,22 +775,24 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             w.s_b[j * N + i] = nr.ci[q * IB + t];
             w.s_tf[j * N + i] = 0.0f;
         }
-        if (mask != before) w.smask[i] = mask;
     }
 
     // force loop (:230-255), slots in ascending order
+    const float4 da = (mask & ((1u << K) - 1u)) ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const long long step = *w.step;
     float nfx = 0.0f, nfy = 0.0f, nm = 0.0f;
     Acc3 acc = {0.0f, 0.0f, 0.0f};
-    for (uint32_t left = mask; left; left &= left - 1) {
+    for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
         const int j = __ffs(left) - 1;
         const int b = w.s_b[j * N + i];
-        int bonded = w.s_bonded[j * N + i];
-        if (bonded >= 0) {
+        int bonded = -1;                                           // any negative value acts alike
+        if ((mask >> (BSHIFT + j)) & 1u) {
+            bonded = w.s_bonded[j * N + i];
             const int st = w.b_status[P.bond_base + bonded];
             if (st < 0) {                                          // :236-239
                 w.s_bonded[j * N + i] = st;
                 bonded = st;
+                mask &= ~(1u << (BSHIFT + j));
             }
         }
         const float4 pb = __ldg(&w.pr[b]);
@@ -811,6 +844,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     const int code = -10 + sign_i32(nd);
                     record_break(w, P, s, step, bg, code, i, b);
                     w.s_bonded[j * N + i] = code;
+                    mask &= ~(1u << (BSHIFT + j));
                     Fn = 0.0f;
                     btf = 0.0f;
                     Fx = 0.0f;
@@ -840,6 +874,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     const int code = -10 + sign_i32(disp);
                     record_break(w, P, s, step, bg, code, i, b);
                     w.s_bonded[j * N + i] = code;
+                    mask &= ~(1u << (BSHIFT + j));
                     fx = 0.0f;
                     fy = 0.0f;
                 }
@@ -873,6 +908,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     const int code = -10 + sign_i32(nd);
                     record_break(w, P, s, step, bg, code, i, b);
                     w.s_bonded[j * N + i] = code;
+                    mask &= ~(1u << (BSHIFT + j));
                     Fn = 0.0f;
                     w.s_btf[j * N + i] = 0.0f;
                     Fx = 0.0f;
@@ -894,6 +930,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     }
 
     // store_forces (:434-478)
+    const Mat MA = w.mats[P.mat_base + meta_mat(m)];
     const float r = pa.z;
     const float mass = ((MA.density * 3.14159274101257324219f) * r) * r;
     const float rot_inertia = ((0.5f * mass) * r) * r;
@@ -928,7 +965,12 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     if (m & M_KICK_Y) v.y = v.y + (0.5f * ay) * dT;
     if (m & M_KICK_R) v.z = v.z + (0.5f * al) * dT;
     w.vw[i] = v;
-    w.dF[i] = make_float4(acc.d0, acc.d1, acc.d2, 0.0f);
+    // data[0..2]; a particle without contacts writes +0 every step, which the
+    // slot word's DF_ZERO bit lets it skip
+    const bool zero = (__float_as_uint(acc.d0) | __float_as_uint(acc.d1) | __float_as_uint(acc.d2)) == 0u;
+    if (!(zero && (mask & DF_ZERO))) w.dF[i] = make_float4(acc.d0, acc.d1, acc.d2, 0.0f);
+    mask = zero ? (mask | DF_ZERO) : (mask & ~DF_ZERO);
+    if (mask != before) w.smask[i] = mask;
 }
 
 // End of step, run by one warp (the last warp of k_interact, or k_end_step): breaks of this step
@@ -993,7 +1035,7 @@ __global__ void k_mark_free(DevWorld w, int first, int count, int free_scene) {
     w.meta[i] = (uint32_t)free_scene << 16;
     w.pr[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     w.smask[i] = 0u;
-    w.nl_count[i] = 0;
+    w.nl[2 * (size_t)i] = make_int4(0, 0, 0, 0);
     w.orig[i] = k;
 }
 

@@ -14,8 +14,12 @@
 //   fx  {forces.x, forces.y, forces.rot, -} (external forces, read when M_FEXT)
 //   d4  {v_half.x, v_half.y, w_half, -}     data[4..6] written by the LOM pass
 //   dF  {sum Fn, sum Ft, sum M, -}          data[0..2] written by the Simulation pass
-// Contact slots are SoA [14][N] (slot j of particle i at j*N+i), with a
-// 14-bit occupancy mask per particle so empty slots are never read.
+// Contact slots are SoA [14][N] (slot j of particle i at j*N+i).  The slot
+// word smask[i] holds the occupancy of the 14 slots in bits 0-13, so empty
+// slots are never read, and in bits 16-29 whether each slot's `bonded` field
+// is >= 0 (kept for empty slots too, whose stale field a new contact
+// inherits), so unbonded slots never read `bonded`.  Bit 31 (DF_ZERO) records
+// that dF is all +0, so particles without contacts skip rewriting it.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -25,6 +29,8 @@
 namespace demgb {
 
 constexpr int K = DEM_MAX_CONTACTS;
+constexpr int BSHIFT = 16;  // first bonded-field bit of the slot word
+constexpr uint32_t DF_ZERO = 1u << 31;  // slot-word bit: dF holds +0, +0, +0
 
 // meta word: fixity predicates, external-force flag, material, scene
 enum : uint32_t {
@@ -75,7 +81,10 @@ struct ScenePar {
     int32_t pad0;
 };
 
-constexpr int NL = 16;               // candidate-list capacity per particle (SoA [NL][N])
+// Candidate list of particle i: 32 bytes, 16 int16 {count, b_1 - i, ..., b_15 - i}
+// (two int4 at nl[2i], nl[2i+1]), so one warp reads its lists in two coalesced
+// 16-byte loads per lane and every candidate is known before the first gather.
+constexpr int NL = 15;               // candidate-list capacity per particle
 constexpr int32_t NL_OVERFLOW = 255; // count marking a particle that searches the cell table instead
 
 struct Event {
@@ -92,7 +101,7 @@ struct DevWorld {
     float4 *pr, *vw, *ac, *dp, *fx, *d4, *dF;
     uint32_t *meta;
     int32_t *orig;
-    uint32_t *smask;
+    uint32_t *smask;            // bits 0-13: occupied slots; 16-29: slot's bonded field >= 0; 31: DF_ZERO
     int2 *rr;                   // reference bucket range of the AABB: {x0 | x1 << 16, y0 | y1 << 16}
     int32_t *s_b, *s_bonded;
     float *s_tf, *s_btf, *s_thb;
@@ -118,8 +127,7 @@ struct DevWorld {
     long long *step;            // device step counter
     int32_t *err;
     // candidate lists (built at rebuilds)
-    int32_t *nl_count;          // [N] candidates, or NL_OVERFLOW
-    int32_t *nl_items;          // [NL][N] internal indices
+    int4 *nl;                   // [N][2] candidate lists (see NL)
     float2 *pbuild;             // [N] position at the last rebuild
     uint32_t *kbuild;           // [N] search cell at the last rebuild
     int32_t *rebuild;           // 1 = the next rebuild body runs

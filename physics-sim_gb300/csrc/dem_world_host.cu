@@ -147,8 +147,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
     w.stats = dalloc<unsigned long long>(owned, 6, ok);
     w.step = dalloc<long long>(owned, 1, ok);
     w.err = dalloc<int32_t>(owned, 1, ok);
-    w.nl_count = dalloc<int32_t>(owned, N, ok);
-    w.nl_items = dalloc<int32_t>(owned, (size_t)NL * N, ok);
+    w.nl = dalloc<int4>(owned, 2 * (size_t)N, ok);
     w.pbuild = dalloc<float2>(owned, N, ok);
     w.kbuild = dalloc<uint32_t>(owned, N, ok);
     w.rebuild = dalloc<int32_t>(owned, 1, ok);
@@ -167,7 +166,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
     CK(cudaMemsetAsync(w.ev_count, 0, sizeof(unsigned long long), stream));
     CK(cudaMemsetAsync(w.stats, 0, 6 * sizeof(unsigned long long), stream));
     CK(cudaMemsetAsync(w.tickets, 0, 2 * sizeof(uint32_t), stream));
-    CK(cudaMemsetAsync(w.nl_count, 0, sizeof(int32_t) * (size_t)(N > 0 ? N : 1), stream));
+    CK(cudaMemsetAsync(w.nl, 0, sizeof(int4) * 2 * (size_t)(N > 0 ? N : 1), stream));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int32_t), stream));
     CK(cudaMemsetAsync(w.cc3, 0, sizeof(int32_t) * (size_t)S, stream));
     CK(cudaMemsetAsync(w.act, 0, sizeof(int32_t) * (size_t)S, stream));
@@ -394,6 +393,7 @@ int World::stage_scene(int s, const dem_scene *sc) {
         for (int j = 0; j < K; ++j) {
             const int32_t *c = sc->contacts + 6 * ((size_t)i * K + j);
             size_t at = (size_t)j * n + i;
+            if (c[5] >= 0) mk |= 1u << (BSHIFT + j);
             if (c[1] != -1) {
                 mk |= 1u << j;
                 sb[at] = base + c[1];
@@ -405,6 +405,8 @@ int World::stage_scene(int s, const dem_scene *sc) {
             sthb[at] = bits2f(c[4]);
             sbd[at] = c[5];
         }
+        const float4 z = dF[i];
+        if ((f2bits(z.x) | f2bits(z.y) | f2bits(z.z)) == 0) mk |= DF_ZERO;
         mask[i] = mk;
     }
     auto up = [&](auto *dst, const auto &src) -> cudaError_t {
@@ -558,7 +560,7 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
 long long World::bytes_per_particle() const {
     // live + spare particle records, slots, broad phase and candidate lists
     const long long rec = 7 * 16 + 3 * 4 + 8 + (long long)K * 5 * 4;
-    return 2 * rec + 4 * 4 + 4 + (long long)NL * 4 + 8 + 4;
+    return 2 * rec + 4 * 4 + 4 + 32 + 8 + 4;
 }
 
 int World::build_capacity(long long particles, long long cells, long long bonds, int scenes, int materials,
