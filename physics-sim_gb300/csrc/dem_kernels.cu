@@ -695,17 +695,18 @@ __device__ __forceinline__ int nl_entry(int4 a, int4 b, int k) {
 }
 
 __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr) {
+    // the particle's own records, issued together
     const uint32_t m = w.meta[i];
+    const float4 pa = w.pr[i];
+    uint32_t mask = w.smask[i];
     const int s = (int)meta_scene(m);
     if (!w.act[s]) return;
     const ScenePar &P = w.par[s];
-    const float4 pa = w.pr[i];
     if (pa.z == 0.0f) {                                            // :113-118
         w.dF[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return;
     }
     const int N = w.N;
-    uint32_t mask = w.smask[i];
     const uint32_t before = mask;
     const int bonds_model = P.p.bonds;
 
@@ -778,40 +779,55 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     }
 
     // force loop (:230-255), slots in ascending order
+    // Per slot, every load is issued before any result is used: the slot
+    // fields, then what they index (partner records, bond records), so a
+    // slot costs two dependent memory round trips instead of five.
     const float4 da = (mask & ((1u << K) - 1u)) ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const long long step = *w.step;
+    const bool one_mat = P.n_mat == 1;
+    const float2 kns1 = __ldg(&w.pair[P.pair_base]);
     float nfx = 0.0f, nfy = 0.0f, nm = 0.0f;
     Acc3 acc = {0.0f, 0.0f, 0.0f};
     for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
         const int j = __ffs(left) - 1;
+        const bool bnn = (mask >> (BSHIFT + j)) & 1u;              // bonded >= 0
         const int b = w.s_b[j * N + i];
+        const float tf0 = w.s_tf[j * N + i];
         int bonded = -1;                                           // any negative value acts alike
-        if ((mask >> (BSHIFT + j)) & 1u) {
+        float btf0 = 0.0f, thb0 = 0.0f;
+        if (bnn) {
             bonded = w.s_bonded[j * N + i];
-            const int st = w.b_status[P.bond_base + bonded];
-            if (st < 0) {                                          // :236-239
-                w.s_bonded[j * N + i] = st;
-                bonded = st;
-                mask &= ~(1u << (BSHIFT + j));
+            if (bonds_model == 3) {
+                btf0 = w.s_btf[j * N + i];
+                thb0 = w.s_thb[j * N + i];
             }
         }
         const float4 pb = __ldg(&w.pr[b]);
         const float4 db = __ldg(&w.dp[b]);
-        const float2 kns = __ldg(&w.pair[P.pair_base + (int)meta_mat(m) * P.n_mat + (int)meta_mat(__ldg(&w.meta[b]))]);
+        const uint32_t mb = one_mat ? 0u : __ldg(&w.meta[b]);
+        int st = 0;
+        float blen = 0.0f;
+        float2 str = make_float2(P.p.bond_normal_strength, P.p.bond_shear_strength);
+        if (bnn) {
+            const int bg = P.bond_base + bonded;
+            st = w.b_status[bg];
+            blen = w.b_length[bg];
+            if (P.has_strength) str = w.b_str[bg];
+        }
+        if (st < 0) {                                              // :236-239
+            w.s_bonded[j * N + i] = st;
+            bonded = st;
+            mask &= ~(1u << (BSHIFT + j));
+        }
+        const float2 kns = one_mat ? kns1 : __ldg(&w.pair[P.pair_base + (int)meta_mat(m) * P.n_mat + (int)meta_mat(mb)]);
         F3 f = {0.0f, 0.0f, 0.0f};
         if (bonded < 0 || bonds_model == 0) {
-            float tf = w.s_tf[j * N + i];
+            float tf = tf0;
             f = linear_model(P, kns, pa, da, pb, db, pa.z + pb.z, tf, acc);
             w.s_tf[j * N + i] = tf;
         } else {
             const int bg = P.bond_base + bonded;
-            const float blen = w.b_length[bg];
-            float sn = P.p.bond_normal_strength, ss = P.p.bond_shear_strength;
-            if (P.has_strength) {
-                const float2 str = w.b_str[bg];
-                sn = str.x;
-                ss = str.y;
-            }
+            const float sn = str.x, ss = str.y;
             if (bonds_model == 3) {                                // :286-336
                 const float kn = P.p.bond_normal_stiffness, ks = P.p.bond_shear_stiffness;
                 const float Rr = P.lambda * (pa.z < pb.z ? pa.z : pb.z);
@@ -827,8 +843,8 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 const float rx = db.x - da.x, ry = db.y - da.y;
                 const float rr = drb + dra;
                 const float rt = (rx * tx + ry * ty) + rr;
-                float btf = w.s_btf[j * N + i];
-                float thb = w.s_thb[j * N + i];
+                float btf = btf0;
+                float thb = thb0;
                 btf = btf + (rt * ks) * A;
                 const float dtb = da.z - db.z;
                 thb = thb + dtb;
@@ -856,7 +872,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 acc.d0 = acc.d0 + (-Fn);
                 acc.d1 = acc.d1 + btf;
                 acc.d2 = acc.d2 + M;
-                float tf = w.s_tf[j * N + i];
+                float tf = tf0;
                 const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, tf, acc);
                 w.s_tf[j * N + i] = tf;
                 f.x = Fx + lm.x;
@@ -878,7 +894,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     fx = 0.0f;
                     fy = 0.0f;
                 }
-                float tf = w.s_tf[j * N + i];
+                float tf = tf0;
                 const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, tf, acc);
                 w.s_tf[j * N + i] = tf;
                 f.x = lm.x + fx;
@@ -897,7 +913,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 const float rx = db.x - da.x, ry = db.y - da.y;
                 const float rr = drb + dra;
                 const float rt = (rx * tx + ry * ty) + rr;
-                float tf = w.s_tf[j * N + i];
+                float tf = tf0;
                 tf = tf + rt * ks;
                 const float cd = P.p.contact_damping;
                 float Fx = cd * (nx * Fn + tx * tf);
