@@ -17,8 +17,9 @@ extern "C" {
 /* Run the broad phase on the current positions (no integration) and return,
  * per scene-local particle, its search-cell key; the particle indices in
  * stable cell order; the cell start table (n_cells + 1 entries).  Any pointer
- * may be NULL; *n_cells receives the scene's cell count (incl. its cell for
- * zero-radius particles). */
+ * may be NULL; *n_cells receives the scene's cell count: the gw * gh search
+ * cells plus one last cell, key gw * gh, holding the particles no cell search
+ * visits (zero radius, and the scene's large particles, which come first). */
 int dem_debug_broad_phase(dem_ctx *ctx, int32_t *keys, int32_t *order, int32_t *cell_start,
                           int32_t *n_cells);
 

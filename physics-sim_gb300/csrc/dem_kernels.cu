@@ -60,6 +60,15 @@ __device__ __forceinline__ void search_xy(const ScenePar &P, float x, float y, i
     cy = b < 0 ? 0 : (b > P.g_h - 1 ? P.g_h - 1 : b);
 }
 
+// internal index range of the scene's large particles since the last rebuild
+// (the reorder leaves every cell's members contiguous, in cell order)
+__device__ __forceinline__ void big_range(const DevWorld &w, const ScenePar &P, int &beg, int &cnt) {
+    const int c0 = w.cell_start[P.cell_base];
+    const int b0 = w.cell_start[P.big_cell];
+    beg = P.particle_base + (b0 - c0);
+    cnt = w.cell_start[P.big_cell + 1] - b0;
+}
+
 struct F3 {
     float x, y, z;
 };
@@ -307,6 +316,8 @@ __global__ void __launch_bounds__(256) k_keys(DevWorld w, const int32_t *gate) {
     uint32_t key;
     if (p.z == 0.0f) {
         key = (uint32_t)P.dead_cell;
+    } else if (m & M_BIG) {
+        key = (uint32_t)P.big_cell;
     } else {
         int cx, cy;
         search_xy(P, p.x, p.y, cx, cy);
@@ -575,6 +586,11 @@ __global__ void __launch_bounds__(256) k_list_build(DevWorld w, const int32_t *g
         w.kbuild[i] = (uint32_t)P.dead_cell;
         return;
     }
+    if (m & M_BIG) {
+        h[0] = (int16_t)NL_BIG;
+        w.kbuild[i] = (uint32_t)P.big_cell;
+        return;
+    }
     int gx, gy;
     search_xy(P, pa.x, pa.y, gx, gy);
     w.kbuild[i] = (uint32_t)(P.cell_base + gy * P.g_w + gx);
@@ -599,7 +615,21 @@ __global__ void __launch_bounds__(256) k_list_build(DevWorld w, const int32_t *g
             ++cnt;
         }
     }
-    h[0] = (int16_t)(over ? NL_OVERFLOW : cnt);
+    int flags = 0;
+    if (P.n_big > 0) {
+        int bb, bn;
+        big_range(w, P, bb, bn);
+        for (int b = bb; b < bb + bn; ++b) {
+            const float4 pb = w.pr[b];
+            const float dx = pb.x - pa.x, dy = pb.y - pa.y;
+            const float t = (pa.z + pb.z + P.skin) * 1.00001f;
+            if (pb.z != 0.0f && dx * dx + dy * dy <= t * t) {
+                flags = NL_NEAR_BIG;
+                break;
+            }
+        }
+    }
+    h[0] = (int16_t)((over ? NL_OVERFLOW : cnt) | flags);
     if (over) atomicAdd(&w.stats[5], 1ull);
 }
 
@@ -717,8 +747,17 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         nr.cnt = 0;
         int ax0, ax1, ay0, ay1;
         const int4 la = __ldg(&w.nl[2 * (size_t)i]);
-        const int lc = la.x & 0xFFFF;
-        if (lc != NL_OVERFLOW) {
+        const int h0 = la.x & 0xFFFF;
+        const int lc = h0 & 0xFF;
+        if (lc == NL_BIG) {
+            // a large particle: k_big_narrow left its partners, in order
+            int bb, bn;
+            big_range(w, P, bb, bn);
+            const int32_t *acc_g = w.big_acc + 16 * (size_t)(P.big_base + (i - bb));
+            const int n = acc_g[15];
+            for (int q = 0; q < n; ++q) nr.ci[q * IB + threadIdx.x] = acc_g[q];
+            nr.cnt = n;
+        } else if (lc != NL_OVERFLOW) {
             const int4 lb = lc > 7 ? __ldg(&w.nl[2 * (size_t)i + 1]) : make_int4(0, 0, 0, 0);
             // distance tests first, all gathers independent; then the bucket
             // test and ordering of the partners that touch
@@ -726,11 +765,21 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
 #pragma unroll
             for (int k = 1; k <= NL; ++k)
                 if (k <= lc && touching(pa, __ldg(&w.pr[i + nl_entry(la, lb, k)]))) pass |= 1u << k;
-            if (pass) unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
+            if (pass || (h0 & NL_NEAR_BIG)) unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
             for (; pass; pass &= pass - 1)
                 accept_partner(w, i + nl_entry(la, lb, __ffs(pass) - 1), ax0, ax1, ay0, ay1, nr);
+            if (h0 & NL_NEAR_BIG) {
+                int bb, bn;
+                big_range(w, P, bb, bn);
+                for (int b = bb; b < bb + bn; ++b) narrow_test(w, i, b, pa, ax0, ax1, ay0, ay1, nr);
+            }
         } else {
             unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
+            if (P.n_big > 0) {
+                int bb, bn;
+                big_range(w, P, bb, bn);
+                for (int b = bb; b < bb + bn; ++b) narrow_test(w, i, b, pa, ax0, ax1, ay0, ay1, nr);
+            }
             const int local = (int)w.kbuild[i] - P.cell_base;
             const int gx = local % P.g_w, gy = local / P.g_w;
             const int cy0 = max(gy - 1, 0), cy1 = min(gy + 1, P.g_h - 1);
@@ -1034,13 +1083,136 @@ __global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w) {
 
 __global__ void k_end_step(DevWorld w) { end_of_step(w); }
 
-int launch_interact(const DevWorld &w, int block, cudaStream_t st) {
+// Narrow phase of one large particle per block (2D_Simulation.wgsl:126-170
+// with the particle's whole neighbourhood): every particle of the search
+// cells within r + r_grid + skin of its position at the last rebuild, and
+// every other large particle of the scene, goes through the same acceptance
+// test as in k_interact; the 14 smallest keys are kept, in key order, for
+// the particle's thread in k_interact.
+constexpr int BIG_THREADS = 256;
+
+__global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
+    __shared__ uint32_t skey[BIG_ACC_MAX];
+    __shared__ int32_t sidx[BIG_ACC_MAX];
+    __shared__ int scount;
+    __shared__ uint32_t wkey[BIG_THREADS / 32];
+    __shared__ int32_t wpos[BIG_THREADS / 32];
+    const int g = blockIdx.x;
+    const int s = w.big_scene[g];
+    if (s < 0 || !w.act[s]) return;
+    const ScenePar &P = w.par[s];
+    if (!(P.p.collisions == 1 && w.det[s] != 0)) return;
+    int bb, bn;
+    big_range(w, P, bb, bn);
+    const int k = g - P.big_base;
+    if (k >= bn) return;  // this record's particle left the big cell (radius 0)
+    const int i = bb + k;
+    const float4 pa = w.pr[i];
+    int32_t *out = w.big_acc + 16 * (size_t)g;
+    if (pa.z == 0.0f) {
+        if (threadIdx.x == 0) out[15] = 0;
+        return;
+    }
+    int ax0, ax1, ay0, ay1;
+    unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
+    const float2 p0 = w.pbuild[i];
+    const float reach = pa.z + P.r_grid + P.skin;
+    int cx0, cy0, cx1, cy1;
+    search_xy(P, p0.x - reach, p0.y - reach, cx0, cy0);
+    search_xy(P, p0.x + reach, p0.y + reach, cx1, cy1);
+    if (threadIdx.x == 0) scount = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c0 = w.cell_start[P.cell_base];
+    auto consider = [&](int b) {
+        if (b == i) return;
+        if (!touching(pa, __ldg(&w.pr[b]))) return;
+        int bx0, bx1, by0, by1;
+        unpack_range(__ldg(&w.rr[b]), bx0, bx1, by0, by1);
+        if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) return;
+        const int fy = by0 > ay0 ? by0 : ay0;
+        const int fx = bx0 > ax0 ? bx0 : ax0;
+        unsigned rank = (unsigned)((fy - ay0) * (ax1 - ax0 + 1) + (fx - ax0));
+        if (rank > 15u) {
+            atomicOr(w.err, 2);
+            rank = 15u;
+        }
+        const int q = atomicAdd(&scount, 1);
+        if (q < BIG_ACC_MAX) {
+            skey[q] = (rank << 28) | (uint32_t)__ldg(&w.orig[b]);
+            sidx[q] = b;
+        }
+    };
+    for (int cy = cy0 + warp; cy <= cy1; cy += BIG_THREADS / 32) {
+        const int row = P.cell_base + cy * P.g_w;
+        const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
+        for (int q = beg + lane; q < end; q += 32) consider(P.particle_base + (q - c0));
+    }
+    for (int b = bb + threadIdx.x; b < bb + bn; b += BIG_THREADS) consider(b);
+    __syncthreads();
+    int n = scount;
+    if (n > BIG_ACC_MAX) {
+        if (threadIdx.x == 0) atomicOr(w.err, 4);
+        n = BIG_ACC_MAX;
+    }
+    const int keep = n < K ? n : K;
+    // keys are distinct: round r takes the smallest key above round r-1's
+    uint32_t prev = 0u;
+    for (int r = 0; r < keep; ++r) {
+        uint32_t best = 0xFFFFFFFFu;
+        int pos = -1;
+        for (int q = threadIdx.x; q < n; q += BIG_THREADS) {
+            const uint32_t kq = skey[q];
+            if ((r == 0 || kq > prev) && (pos < 0 || kq < best)) {
+                best = kq;
+                pos = q;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            const uint32_t ok = __shfl_down_sync(0xffffffffu, best, o);
+            const int op = __shfl_down_sync(0xffffffffu, pos, o);
+            if (op >= 0 && (pos < 0 || ok < best)) {
+                best = ok;
+                pos = op;
+            }
+        }
+        if (lane == 0) {
+            wkey[warp] = best;
+            wpos[warp] = pos;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t bk = 0xFFFFFFFFu;
+            int bp = -1;
+            for (int v = 0; v < BIG_THREADS / 32; ++v)
+                if (wpos[v] >= 0 && (bp < 0 || wkey[v] < bk)) {
+                    bk = wkey[v];
+                    bp = wpos[v];
+                }
+            out[r] = sidx[bp];
+            wkey[0] = bk;
+        }
+        __syncthreads();
+        prev = wkey[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[15] = keep;
+}
+
+int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs) {
     (void)block;
+    int k = 0;
+    if (bigs && w.n_big_slots > 0) {
+        k_big_narrow<<<w.n_big_slots, BIG_THREADS, 0, st>>>(w);
+        k++;
+    }
     const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
     k_interact<<<g, IB, 0, st>>>(w);
-    if (w.ticket) return 1;
+    k++;
+    if (w.ticket) return k;
     k_end_step<<<1, 32, 0, st>>>(w);
-    return 2;
+    return k + 1;
 }
 
 // ------------------------------------------------------- free ranges

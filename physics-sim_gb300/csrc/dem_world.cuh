@@ -41,6 +41,7 @@ enum : uint32_t {
     M_FIX_Y = 1u << 4,
     M_FIX_R = 1u << 5,
     M_FEXT = 1u << 6,    // external force record is not all zero
+    M_BIG = 1u << 7,     // large particle: kept out of the search cells (see ScenePar::big_cell)
 };
 __host__ __device__ inline uint32_t meta_mat(uint32_t m) { return (m >> 8) & 0xFFu; }
 __host__ __device__ inline uint32_t meta_scene(uint32_t m) { return m >> 16; }
@@ -78,7 +79,17 @@ struct ScenePar {
     float kb2, ksb2;       // 1/(1/k + 1/k) of the bond stiffnesses (2D_Simulation.wgsl:378-379)
     float skin;            // candidate-list skin: lists hold pairs within ra + rb + skin
     float disp_limit2;     // (skin/2)^2 shrunk by a rounding margin: a move beyond it forces a rebuild
-    int32_t pad0;
+    // Large particles (radius above 4x the scene's median, few of them) would
+    // inflate the search cells for everyone.  They are binned into their own
+    // cell, big_cell, which the cell searches never visit: after a rebuild they
+    // sit at internal indices [big_begin, big_begin + count) of the scene (in
+    // scene-local index order), each small particle's list records whether
+    // any of them was within reach, and k_big_narrow gives each its accepted
+    // partners with one thread block.
+    int32_t big_cell;      // global cell of the scene's large particles
+    int32_t big_base;      // first big-partner record of the scene
+    int32_t n_big;         // large particles of the scene at the last layout
+    float r_grid;          // largest radius the search cells are sized for
 };
 
 // Candidate list of particle i: 32 bytes, 16 int16 {count, b_1 - i, ..., b_15 - i}
@@ -86,6 +97,9 @@ struct ScenePar {
 // 16-byte loads per lane and every candidate is known before the first gather.
 constexpr int NL = 15;               // candidate-list capacity per particle
 constexpr int32_t NL_OVERFLOW = 255; // count marking a particle that searches the cell table instead
+constexpr int32_t NL_BIG = 254;      // count marking a large particle (partners from k_big_narrow)
+constexpr int32_t NL_NEAR_BIG = 0x100; // count flag: a large particle was within reach at the rebuild
+constexpr int BIG_ACC_MAX = 2048;    // partners a large particle may touch at once
 
 struct Event {
     int32_t scene, step, bond, code, a, b;
@@ -133,6 +147,9 @@ struct DevWorld {
     int32_t *rebuild;           // 1 = the next rebuild body runs
     uint32_t *tickets;          // [2] last-warp counters of k_lom and k_interact
     int32_t ticket;             // 1: those kernels' last warps end the step; 0: separate one-warp kernels
+    int32_t *big_acc;           // [slots][16]: accepted partners of a large particle, [15] = count
+    int32_t *big_scene;         // [slots] scene of each big-partner record, -1 unused
+    int32_t n_big_slots;
     int32_t *det;               // [S] narrow phase runs in the current step
     int32_t *act;               // [S] 1 = the scene steps; 0 = frozen (finished or free slot)
     long long *remaining;       // [S] steps left before the scene freezes (served scenes)
@@ -174,7 +191,7 @@ int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int3
 void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStream_t st,
                     const int32_t *gate);
 void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
-int launch_interact(const DevWorld &w, int block, cudaStream_t st);
+int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs);
 void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
                            const int32_t *d_props, int block, cudaStream_t st);
 int scan_tmp_size(int n);

@@ -99,7 +99,7 @@ static T *dalloc(std::vector<void *> &owned, size_t count, bool &ok) {
     return static_cast<T *>(p);
 }
 
-int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
+int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_cap) {
     release();
     bool ok = true;
     DevWorld &w = d;
@@ -152,6 +152,9 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
     w.kbuild = dalloc<uint32_t>(owned, N, ok);
     w.rebuild = dalloc<int32_t>(owned, 1, ok);
     w.tickets = dalloc<uint32_t>(owned, 2, ok);
+    w.n_big_slots = TB;
+    w.big_acc = dalloc<int32_t>(owned, 16 * (size_t)std::max(TB, 1), ok);
+    w.big_scene = dalloc<int32_t>(owned, std::max(TB, 1), ok);
     w.det = dalloc<int32_t>(owned, S, ok);
     w.act = dalloc<int32_t>(owned, S, ok);
     w.remaining = dalloc<long long>(owned, S, ok);
@@ -168,6 +171,8 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap) {
     CK(cudaMemsetAsync(w.tickets, 0, 2 * sizeof(uint32_t), stream));
     CK(cudaMemsetAsync(w.nl, 0, sizeof(int4) * 2 * (size_t)(N > 0 ? N : 1), stream));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int32_t), stream));
+    CK(cudaMemsetAsync(w.big_scene, 0xFF, sizeof(int32_t) * (size_t)std::max(TB, 1), stream));
+    CK(cudaMemsetAsync(w.big_acc, 0, sizeof(int32_t) * 16 * (size_t)std::max(TB, 1), stream));
     CK(cudaMemsetAsync(w.cc3, 0, sizeof(int32_t) * (size_t)S, stream));
     CK(cudaMemsetAsync(w.act, 0, sizeof(int32_t) * (size_t)S, stream));
     CK(cudaMemcpyAsync(w.step, &host_step, sizeof(long long), cudaMemcpyHostToDevice, stream));
@@ -217,6 +222,32 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
             if (c[0] != owner) return fail(DEM_E_INVALID, "contact record's a differs from its owner");
         }
     }
+    // Large particles: radius above 4x the median of the nonzero radii, when
+    // there are few of them (at most max(64, n/256)); the search cells are
+    // then sized by the largest of the others.
+    h.r_big = std::numeric_limits<float>::infinity();
+    h.n_big = 0;
+    {
+        std::vector<float> rs;
+        rs.reserve(n);
+        for (int i = 0; i < n; ++i)
+            if (sc->radii[i] > 0.0f) rs.push_back(sc->radii[i]);
+        if (!rs.empty()) {
+            std::nth_element(rs.begin(), rs.begin() + rs.size() / 2, rs.end());
+            const float thr = 4.0f * rs[rs.size() / 2];
+            int cnt = 0;
+            float rsmall = 0.0f;
+            for (float r : rs) {
+                if (r > thr) ++cnt;
+                else rsmall = std::max(rsmall, r);
+            }
+            if (cnt > 0 && cnt <= std::max(64, n / 256)) {
+                h.r_big = thr;
+                h.n_big = cnt;
+                rmax = rsmall;
+            }
+        }
+    }
     h.r_max = rmax;
     // reference bucket grid
     dem_grid_info g = sc->grid;
@@ -262,7 +293,7 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
     gw = std::max(gw, 1);
     gh = std::max(gh, 1);
     if ((double)gw * gh > 2.0e9) return fail(DEM_E_INVALID, "search grid too large");
-    h.n_cells = gw * gh + 1;
+    h.n_cells = gw * gh + 2;  // search cells, the large particles' cell, the dead cell
     ScenePar &P = h.par;
     std::memset(&P, 0, sizeof P);
     P.g_cs = gcs;
@@ -288,6 +319,10 @@ void World::fill_par(SceneHost &h) {
     P.ref_base_y = (h.grid.cell_size * (float)h.grid.h) * 0.5f;
     P.cell_base = h.cell_base;
     P.dead_cell = h.cell_base + h.n_cells - 1;
+    P.big_cell = h.cell_base + P.g_w * P.g_h;
+    P.big_base = h.big_base;
+    P.n_big = h.n_big;
+    P.r_grid = h.r_max;
     P.particle_base = h.particle_base;
     P.n_particles = h.n;
     P.bond_base = h.bond_base;
@@ -326,6 +361,29 @@ int World::force_rebuild() {
     CK(cudaMemcpyAsync(d.rebuild, &one, 4, cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
     return DEM_OK;
+}
+
+// big-partner records [big_base, big_base + big_cap) of scene s belong to
+// `scene_or_free` (-1: unused)
+int World::push_bigs(int s, int scene_or_free) {
+    const SceneHost &h = sh[s];
+    if (h.big_cap <= 0) return DEM_OK;
+    std::vector<int32_t> v(h.big_cap, scene_or_free);
+    CK(cudaMemcpyAsync(d.big_scene + h.big_base, v.data(), 4 * (size_t)h.big_cap, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    update_has_bigs();
+    return DEM_OK;
+}
+
+// k_big_narrow is part of the step only while some scene has large
+// particles; the captured graphs follow when that changes
+void World::update_has_bigs() {
+    bool any = false;
+    for (const auto &h : sh) any |= h.big_cap > 0;
+    if (any != has_bigs) {
+        has_bigs = any;
+        drop_graph();
+    }
 }
 
 int World::push_par(int s) {
@@ -387,6 +445,7 @@ int World::stage_scene(int s, const dem_scene *sc) {
         if (f[0] != 0.0f || f[1] != 0.0f || f[2] != 0.0f) m |= M_FEXT;
         m |= ((uint32_t)sc->material_pointers[i] & 0xFFu) << 8;
         m |= (uint32_t)s << 16;
+        if (sc->radii[i] > h.r_big) m |= M_BIG;
         meta[i] = m;
         orig[i] = i;
         uint32_t mk = 0;
@@ -502,7 +561,7 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     use_graphs = ext.plain_launches == 0;
     diagnostics = ext.diagnostics != 0;
     sh.assign(S, SceneHost{});
-    long long N = 0, C = 0, B = 0, M = 0, MP = 0;
+    long long N = 0, C = 0, B = 0, M = 0, MP = 0, TB = 0;
     for (int s = 0; s < S; ++s) {
         SceneHost &h = sh[s];
         const dem_ext &e = exts[s];
@@ -526,6 +585,8 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
         h.bond_base = (int)B;
         h.mat_base = (int)M;
         h.pair_base = (int)MP;
+        h.big_base = (int)TB;
+        h.big_cap = h.n_big;
         h.step0 = host_step;
         h.cc0_0 = scenes[s]->coll_cont[0];
         h.cc1_0 = scenes[s]->coll_cont[1];
@@ -535,14 +596,18 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
         B += h.n_bonds;
         M += h.n_mat;
         MP += (long long)h.n_mat * h.n_mat;
+        TB += h.n_big;
     }
     if (N > (1LL << 30) || C > (1LL << 31) - 2 || B > (1LL << 30))
         return fail(DEM_E_INVALID, "world too large");
     uint32_t ev_cap = ext.event_capacity > 0 ? (uint32_t)ext.event_capacity : 1u << 16;
-    int rc = alloc((int)N, (int)C, (int)B, S, (int)M, (int)MP, ev_cap);
+    int rc = alloc((int)N, (int)C, (int)B, S, (int)M, (int)MP, (int)TB, ev_cap);
     if (rc) return rc;
+    update_has_bigs();
     for (int s = 0; s < S; ++s) {
         rc = stage_scene(s, scenes[s]);
+        if (rc) return rc;
+        rc = push_bigs(s, s);
         if (rc) return rc;
         rc = push_par(s);
         if (rc) return rc;
@@ -584,9 +649,12 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     }
     const long long pairs = (long long)materials * 16;
     uint32_t ev_cap = ext.event_capacity > 0 ? (uint32_t)ext.event_capacity : 1u << 18;
-    int rc = alloc((int)particles, (int)cells, (int)std::max(bonds, 1LL), S, materials, (int)pairs, ev_cap);
+    const long long bigs = std::max(64LL, particles / 1024);
+    int rc = alloc((int)particles, (int)cells, (int)std::max(bonds, 1LL), S, materials, (int)pairs, (int)bigs,
+                   ev_cap);
     if (rc) return rc;
     launch_mark_free(d, 0, (int)particles, free_slot, stream);
+    a_big.reset(bigs);
     a_part.reset(particles);
     a_cell.reset(cells);
     a_bond.reset(std::max(bonds, 1LL));
@@ -630,7 +698,9 @@ int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e
     long long pb = pc >= 0 ? a_bond.alloc(h.n_bonds) : -1;
     long long pm = pb >= 0 ? a_mat.alloc(h.n_mat) : -1;
     long long pq = pm >= 0 ? a_pair.alloc((long long)h.n_mat * h.n_mat) : -1;
-    if (pq < 0) {
+    long long pg = pq >= 0 ? (h.n_big > 0 ? a_big.alloc(h.n_big) : 0) : -1;
+    if (pg < 0) {
+        if (pq >= 0) a_pair.release(pq, (long long)h.n_mat * h.n_mat);
         if (pm >= 0) a_mat.release(pm, h.n_mat);
         if (pb >= 0) a_bond.release(pb, h.n_bonds);
         if (pc >= 0) a_cell.release(pc, h.n_cells);
@@ -644,6 +714,8 @@ int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e
     h.bond_base = (int)pb;
     h.mat_base = (int)pm;
     h.pair_base = (int)pq;
+    h.big_base = (int)pg;
+    h.big_cap = h.n_big;
     if (e.bond_normal_strength && h.n_bonds > 0)
         h.bond_sn.assign(e.bond_normal_strength, e.bond_normal_strength + h.n_bonds);
     if (e.bond_shear_strength && h.n_bonds > 0)
@@ -659,6 +731,7 @@ int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e
     h.active = true;
     sh[s] = h;
     rc = stage_scene(s, sc);
+    if (rc == DEM_OK) rc = push_bigs(s, s);
     if (rc == DEM_OK) rc = push_par(s);
     if (rc == DEM_OK) {
         int32_t c3 = sc->coll_cont[3];
@@ -687,6 +760,11 @@ int World::retire(int s) {
     a_bond.release(h.bond_base, h.n_bonds);
     a_mat.release(h.mat_base, h.n_mat);
     a_pair.release(h.pair_base, (long long)h.n_mat * h.n_mat);
+    if (h.big_cap > 0) {
+        rc = push_bigs(s, -1);
+        if (rc) return rc;
+        a_big.release(h.big_base, h.big_cap);
+    }
     h = SceneHost{};
     h.params.collision_interval = 1;
     h.n_cells = 1;
@@ -706,7 +784,11 @@ int World::upload_scene(int s, const dem_scene *sc) {
         return fail(DEM_E_UNSUPPORTED, "uploaded scene needs a larger search grid; create a new context");
     // keep the cell budget; adopt the new geometry inside it
     probe.n_cells = h.n_cells;
+    if (probe.n_big > h.big_cap)
+        return fail(DEM_E_UNSUPPORTED, "uploaded scene has more large particles; create a new context");
     h.r_max = probe.r_max;
+    h.r_big = probe.r_big;
+    h.n_big = probe.n_big;
     h.grid = probe.grid;
     h.par.g_cs = probe.par.g_cs;
     h.par.g_inv = probe.par.g_inv;
@@ -848,7 +930,7 @@ void World::enqueue_plain_step() {
     enqueue_rebuild(stream, d.rebuild);
     rec(T_BROAD, false);
     rec(T_INTERACT, true);
-    k += launch_interact(d, block, stream);
+    k += launch_interact(d, block, stream, has_bigs);
     rec(T_INTERACT, false);
     launches += k + rebuild_kernels;
     host_step++;
@@ -905,7 +987,7 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
         cudaGraph_t body_out = nullptr;
         CKG(cudaStreamEndCapture(side, &body_out));
         CKG(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-        kernels += launch_interact(d, block, stream);
+        kernels += launch_interact(d, block, stream, has_bigs);
     }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(stream, &g);
@@ -1118,7 +1200,10 @@ int World::broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *c
                                 int32_t *n_cells) {
     if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
     const SceneHost &h = sh[s];
-    if (n_cells) *n_cells = h.n_cells;
+    // reported layout: the search cells, then one cell for the large and the
+    // zero-radius particles (internally two cells, large first)
+    const int grid_cells = h.par.g_w * h.par.g_h;
+    if (n_cells) *n_cells = grid_cells + 1;
     launch_keys(d, block, stream, nullptr);
     launch_broad_phase(d, block, stream, nullptr);
     const int n = h.n, base = h.particle_base;
@@ -1134,13 +1219,15 @@ int World::broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *c
     }
     CK(cudaStreamSynchronize(stream));
     for (int i = 0; i < n; ++i) {
-        if (keys) keys[orig[i]] = (int32_t)k[i] - h.cell_base;
+        if (keys) keys[orig[i]] = std::min((int32_t)k[i] - h.cell_base, grid_cells);
         int src = srt[i] - base;
         if (src < 0 || src >= n) return fail(DEM_E_STATE, "sorted order leaves its scene");
         if (order) order[i] = orig[src];
     }
-    if (cell_start)
-        for (size_t c = 0; c < cs.size(); ++c) cell_start[c] = cs[c] - first;
+    if (cell_start) {
+        for (int c = 0; c <= grid_cells; ++c) cell_start[c] = cs[c] - first;
+        cell_start[grid_cells + 1] = cs[h.n_cells] - first;
+    }
     // the cell table now describes the current positions, not the last rebuild
     return force_rebuild();
 }

@@ -25,7 +25,10 @@ struct SceneHost {
     dem_params params;
     dem_grid_info grid;
     int n = 0, n_bonds = 0, n_mat = 0;
-    float r_max = 0.0f;
+    float r_max = 0.0f;                // largest radius the search cells are sized for
+    float r_big = 3.0e38f;             // radius above which a particle is large (none: above any radius)
+    int n_big = 0;                     // large particles
+    int big_cap = 0, big_base = 0;     // big-partner records owned by the scene
     int use_f64 = 0;
     float lambda = 0.5f;
     float cell_factor = 1.0f;
@@ -86,7 +89,7 @@ class World {
     int admit(const dem_scene *scene, const dem_params &params, const dem_ext &ext, long long horizon);
     int retire(int slot);
     int free_slot = -1;                 // scene index of unused particles (never active)
-    RangeAlloc a_part, a_cell, a_bond, a_mat, a_pair;
+    RangeAlloc a_part, a_cell, a_bond, a_mat, a_pair, a_big;
     std::vector<int> free_slots;
     long long bytes_per_particle() const;
 
@@ -102,6 +105,7 @@ class World {
     std::vector<SceneHost> sh;
     DevWorld d{};
     bool use_graphs = true;
+    bool has_bigs = false;         // some scene has large particles: k_big_narrow runs each step
     long long launches = 0;
     // kernel timing (debug): event pairs per kernel kind, summed on demand
     bool timing = false;
@@ -116,7 +120,9 @@ class World {
 
   private:
     int fail(int code, const std::string &msg);
-    int alloc(int N, int C, int B, int S, int M, int MP, uint32_t ev_cap);
+    int alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_cap);
+    int push_bigs(int s, int scene_or_free);
+    void update_has_bigs();
     int push_materials(int s);
     void release();
     int compute_layout(SceneHost &h, const dem_scene *scene);

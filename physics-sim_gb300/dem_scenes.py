@@ -289,6 +289,67 @@ def c1_chains(chains=64, length=256, seed=0, pull_velocity=0.1):
     return sc, p, ext
 
 
+def c2_impact(cols=1024, rows=4096, seed=0, projectile_radius=40.0, projectile_speed=50.0,
+              bonded_fraction=0.3, cluster_min=4, cluster_max=32, sigma=0.15, projectiles=1):
+    """Single large impact scene: cols x rows disks on a square lattice of
+    pitch 2 (the default 1024 x 4096 = 4,194,304 disks fill a 2048 x 8192
+    bed), radii log-normal with median 1 and log-sigma `sigma` (so lattice
+    neighbours overlap where r_i + r_j > 2 and push apart from the first
+    step), walls at the bed's sides and bottom; about `bonded_fraction` of the
+    disks in horizontal clusters of cluster_min..cluster_max lattice
+    neighbours joined by parallel bonds (bond radius factor 0.8, k_n 1e5,
+    k_s 5e4, strengths Weibull(8, 5e3) per bond); one projectile disk of
+    radius `projectile_radius` resting 0.3 into the bed's top row, moving
+    down at `projectile_speed`; gravity, friction 0.5, k_n 1e5, k_s 5e4,
+    dt 5e-5.  The projectile is the last particle; with projectiles > 1 they
+    are the last ones, side by side, each 0.2 into its neighbour."""
+    rng = np.random.default_rng(seed)
+    nb = cols * rows
+    n = nb + projectiles
+    W = 2.0 * cols
+    bed_h = 2.0 * rows
+    H = bed_h + 4.0 * projectile_radius + 20.0
+    pos = np.zeros((n, 2), np.float64)
+    col = np.arange(nb) % cols
+    row = np.arange(nb) // cols
+    pos[:nb, 0] = (col - (cols - 1) / 2.0) * 2.0
+    pos[:nb, 1] = -H / 2.0 + 1.0 + row * 2.0
+    radii = np.exp(rng.normal(0.0, sigma, n)).astype(np.float32)
+    radii[:nb] = np.minimum(radii[:nb], np.float32(W / 4.0))
+    radii[nb:] = np.float32(projectile_radius)
+    pitch = 2.0 * projectile_radius - 0.2
+    for j in range(projectiles):
+        pos[nb + j] = ((j - (projectiles - 1) / 2.0) * pitch, pos[:nb, 1].max() + 1.0 + projectile_radius - 0.3)
+    # bonded clusters: each row cut into runs of cluster_min..cluster_max
+    # consecutive columns, each run bonded with probability bonded_fraction
+    per_row = cols // cluster_min + 1
+    L = rng.integers(cluster_min, cluster_max + 1, size=(rows, per_row))
+    c0 = np.cumsum(L, axis=1) - L
+    pick = rng.random((rows, per_row)) < bonded_fraction
+    ln = np.minimum(L, cols - c0)
+    ok = (c0 < cols) & (ln >= 2) & pick
+    rr, kk = np.nonzero(ok)
+    starts = (rr * cols + c0[rr, kk]).astype(np.int64)
+    lengths = ln[rr, kk].astype(np.int64)
+    sc = empty_scene(n, [1, 1, 1, 1.0, 1e5, 5e4])
+    sc["pos"] = pos.astype(np.float32).reshape(-1)
+    sc["radii"] = radii
+    sc["vel"].reshape(-1, 2)[nb:, 1] = -projectile_speed
+    add_straight_chain_bonds(sc, starts, lengths)
+    p = reference_defaults(n)
+    p.update({"hor_bound": W + 2.0, "vert_bound": H, "planet_mode": 0, "gravity": 1, "gravity_acc": 1.0,
+              "friction_coefficient": 0.5, "dT": 5e-5, "bonds": 3 if len(starts) else 0,
+              "bonds_tear": 1, "bond_normal_stiffness": 1e5, "bond_shear_stiffness": 5e4,
+              "bond_normal_strength": 5e3, "bond_shear_strength": 5e3})
+    sc["grid"] = grid_capacity(p["hor_bound"], H, sc["radii"], n)
+    ext = {"bond_lambda": 0.8}
+    nbnd = sc["bonds"].shape[0] // 3
+    if len(starts) and nbnd > 0:
+        st = (5e3 * rng.weibull(8.0, size=(2, nbnd))).astype(np.float32)
+        ext["bond_sn"], ext["bond_ss"] = st[0], st[1]
+    return sc, p, ext
+
+
 def dense_bed(n, seed=0, spacing=2.05, aspect=1.0):
     """A packed bed for contact-heavy runs: the c0_settle particle and material
     model on a jittered square lattice of the given spacing (radii U[0.8, 1.2],

@@ -22,6 +22,10 @@ def _items():
     items = [dem_scenes.c3_mix_scene(n, f, sd) for n, f, sd in specs]
     items.append(dem_scenes.dense_bed(800, seed=6))
     items.append(dem_scenes.c1_chains(chains=3, length=20, seed=7, pull_velocity=20.0))
+    # scenes with large particles (their own cell and partner records)
+    items.append(dem_scenes.c2_impact(cols=32, rows=64, seed=8, projectile_radius=8.0, projectile_speed=400.0,
+                                      projectiles=2))
+    items.append(dem_scenes.c2_impact(cols=40, rows=40, seed=9, projectile_radius=7.0, projectile_speed=300.0))
     return items
 
 

@@ -87,6 +87,32 @@ def test_large_world_end_of_step_kernels_bit_exact():
     assert got == ref
 
 
+@pytest.mark.parametrize("projectiles", [1, 3])
+def test_large_particle_impact_bit_exact(projectiles):
+    """A bonded, polydisperse bed hit by projectiles of radius 12 (12x the
+    median): the projectiles live outside the search cells and get their
+    partners from one thread block each; their contact sets hit the cap of 14
+    while more bed particles touch them, and side by side they touch each
+    other."""
+    sc, p, ext = dem_scenes.c2_impact(cols=64, rows=128, seed=1, projectile_radius=12.0,
+                                      projectile_speed=400.0, projectiles=projectiles)
+    n = sc["radii"].size
+    with dem.Context(sc, p, **ext) as ctx:
+        keys, _, _ = ctx.broad_phase()
+        _, _, _, gw, gh = ctx.search_grid()
+    assert (keys[n - projectiles:] == gw * gh).all(), "projectiles must sit in the large-particle cell"
+    g, o, gev, oev = run_both(sc, p, 600, chunk=100, **ext)
+    assert_same_state(g, o)
+    got = sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in gev)
+    ref = sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in oev)
+    assert got == ref
+    c = g["contacts"].reshape(-1, 14, 6)
+    assert (c[n - 1, :, 1] != -1).sum() == 14, "the projectile's contact set must reach the cap"
+    assert (c[:, :, 1] == n - 1).sum() > 14
+    if projectiles > 1:
+        assert (c[n - 1, :, 1] >= n - projectiles).any() or (c[n - 2, :, 1] >= n - projectiles).any()
+
+
 @pytest.mark.parametrize("model", [1, 2, 3])
 def test_bond_models_bit_exact(model):
     sc, p, ext = dem_scenes.c1_chains(chains=3, length=24, seed=5, pull_velocity=8.0)
