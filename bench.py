@@ -78,9 +78,29 @@ def build_workload(name):
         n = 1 << 20
         sc, p, ext = dem_scenes.dense_bed(n=n)
         desc = {"workload": "dense bed (c0 particle model, packed)", "particles": n, "dt": 1e-4}
+    elif name == "c2_impact":
+        sc, p, ext = dem_scenes.c2_impact()
+        nb = int(sc["bonds"].shape[0] // 3)
+        desc = {"workload": "c2 single large impact scene", "particles": int(sc["radii"].shape[0]),
+                "bed": [2048, 8192], "lattice": "1024 x 4096, pitch 2", "radii": "log-normal, median 1, sigma 0.15",
+                "bonded_fraction": 0.3, "clusters": "horizontal runs of 4-32", "bonds": nb,
+                "bond_model": "parallel (bonds=3), factor 0.8, Weibull(8, 5e3) strengths",
+                "projectile": {"radius": 40, "speed": 50}, "dt": 5e-5}
     else:
         raise SystemExit("unknown workload %s" % name)
     return sc, p, ext, desc
+
+
+def cpu_sample_workload(name, sc, p, ext):
+    """The scene the CPU arms time.  For c2 a 128 x 256 crop of the same bed
+    model with the same r = 40 projectile: the reference's bucket side is set
+    by the largest radius (80), so each particle scans as many bucket members
+    as in the full scene and the per-particle cost is the same."""
+    if name == "c2_impact":
+        import dem_scenes
+        s2, p2, e2 = dem_scenes.c2_impact(cols=128, rows=256)
+        return s2, p2, e2, "c2 crop: 128 x 256 bed + r=40 projectile (%d particles)" % s2["radii"].shape[0]
+    return sc, p, ext, None
 
 
 def build_batch_workload(n_scenes, seed):
@@ -228,6 +248,10 @@ def run_reference(args):
     if rank != 0:
         return
     sc, p, ext, desc = build_workload(args.workload)
+    sc, p, ext, crop = cpu_sample_workload(args.workload, sc, p, ext)
+    if crop:
+        desc = dict(desc)
+        desc["cpu_sample_scene"] = crop
     import oracle
     okw = {}
     if "bond_lambda" in ext:
@@ -373,7 +397,10 @@ def run_ours(args):
 
     base = None
     if rank == 0 and ws == 1:
-        base, _ = cpu_baseline(sc, p, ext, args.cpu_seconds, F)
+        csc, cp, cext, crop = cpu_sample_workload(args.workload, sc, p, ext)
+        base, _ = cpu_baseline(csc, cp, cext, args.cpu_seconds, F)
+        if crop:
+            base["sample"] = crop + "; " + base["sample"]
     cfg = dict(desc)
     cfg.update({"frame_steps": F, "parallelism": "replicas" if ws > 1 else "single",
                 "l2": "flushed between frames (write of %d MiB on the stream, untimed)" % (FLUSH_BYTES >> 20),

@@ -662,32 +662,41 @@ constexpr int IB = 128;  // threads per k_interact block
 // The accepted partners of one thread, kept sorted by (first shared bucket,
 // particle index) in shared memory (slot-major, so a warp's accesses fall in
 // distinct banks): key = rank << 28 | scene-local index.
+__shared__ uint32_t nr_ck[K * IB];  // [K][IB] sort keys of the accepted partners
+__shared__ int nr_ci[K * IB];       // [K][IB] their internal indices
+
 struct Narrow {
-    uint32_t *ck;  // [K][IB]
-    int *ci;       // [K][IB]
     int cnt;
 };
 
 __device__ __forceinline__ void top14_insert(uint32_t key, int idx, Narrow &nr) {
     const int t = threadIdx.x;
-    if (nr.cnt == K && key >= nr.ck[(K - 1) * IB + t]) return;
+    if (nr.cnt == K && key >= nr_ck[(K - 1) * IB + t]) return;
     int pos = nr.cnt < K ? nr.cnt : K - 1;
-    while (pos > 0 && nr.ck[(pos - 1) * IB + t] > key) {
-        nr.ck[pos * IB + t] = nr.ck[(pos - 1) * IB + t];
-        nr.ci[pos * IB + t] = nr.ci[(pos - 1) * IB + t];
+    while (pos > 0 && nr_ck[(pos - 1) * IB + t] > key) {
+        nr_ck[pos * IB + t] = nr_ck[(pos - 1) * IB + t];
+        nr_ci[pos * IB + t] = nr_ci[(pos - 1) * IB + t];
         --pos;
     }
-    nr.ck[pos * IB + t] = key;
-    nr.ci[pos * IB + t] = idx;
+    nr_ck[pos * IB + t] = key;
+    nr_ci[pos * IB + t] = idx;
     if (nr.cnt < K) ++nr.cnt;
 }
 
-// |p_b - p_a| < r_b + r_a (2D_Simulation.wgsl:159)
+// |p_b - p_a| < r_b + r_a (2D_Simulation.wgsl:159).  The square root is only
+// taken near the boundary: while t*t is a normal float, s2 > t*t*1.000001
+// cannot pass and s2 < t*t*0.999999 must (each side leaves more than 8e-7
+// relative margin for the roundings of t*t, of the factor and of sqrtf), so
+// both shortcuts give the result of the full test.
 __device__ __forceinline__ bool touching(float4 pa, float4 pb) {
     const float dx = pb.x - pa.x, dy = pb.y - pa.y;
     const float s2 = dx * dx + dy * dy;
     const float t = pb.z + pa.z;
-    if (s2 > (t * t) * 1.000001f) return false;                   // cannot pass the test below
+    const float t2 = t * t;
+    if (t2 >= 1e-30f) {
+        if (s2 > t2 * 1.000001f) return false;
+        if (s2 < t2 * 0.999999f) return true;
+    }
     return sqrtf(s2) < t;
 }
 
@@ -755,7 +764,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             big_range(w, P, bb, bn);
             const int32_t *acc_g = w.big_acc + 16 * (size_t)(P.big_base + (i - bb));
             const int n = acc_g[15];
-            for (int q = 0; q < n; ++q) nr.ci[q * IB + threadIdx.x] = acc_g[q];
+            for (int q = 0; q < n; ++q) nr_ci[q * IB + threadIdx.x] = acc_g[q];
             nr.cnt = n;
         } else if (lc != NL_OVERFLOW) {
             const int4 lb = lc > 7 ? __ldg(&w.nl[2 * (size_t)i + 1]) : make_int4(0, 0, 0, 0);
@@ -801,7 +810,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             const int sb = w.s_b[j * N + i];
             bool found = false;
             for (int q = 0; q < cnt; ++q) {
-                const bool hit = nr.ci[q * IB + t] == sb;
+                const bool hit = nr_ci[q * IB + t] == sb;
                 found |= hit;
                 matched |= hit ? (1u << q) : 0u;
             }
@@ -822,7 +831,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             if (empty == 0u) continue;
             const int j = 31 - __clz(empty);
             mask |= 1u << j;
-            w.s_b[j * N + i] = nr.ci[q * IB + t];
+            w.s_b[j * N + i] = nr_ci[q * IB + t];
             w.s_tf[j * N + i] = 0.0f;
         }
     }
@@ -832,9 +841,6 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     // fields, then what they index (partner records, bond records), so a
     // slot costs two dependent memory round trips instead of five.
     const float4 da = (mask & ((1u << K) - 1u)) ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const long long step = *w.step;
-    const bool one_mat = P.n_mat == 1;
-    const float2 kns1 = __ldg(&w.pair[P.pair_base]);
     float nfx = 0.0f, nfy = 0.0f, nm = 0.0f;
     Acc3 acc = {0.0f, 0.0f, 0.0f};
     for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
@@ -853,7 +859,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         }
         const float4 pb = __ldg(&w.pr[b]);
         const float4 db = __ldg(&w.dp[b]);
-        const uint32_t mb = one_mat ? 0u : __ldg(&w.meta[b]);
+        const uint32_t mb = P.n_mat == 1 ? 0u : __ldg(&w.meta[b]);
         int st = 0;
         float blen = 0.0f;
         float2 str = make_float2(P.p.bond_normal_strength, P.p.bond_shear_strength);
@@ -868,7 +874,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             bonded = st;
             mask &= ~(1u << (BSHIFT + j));
         }
-        const float2 kns = one_mat ? kns1 : __ldg(&w.pair[P.pair_base + (int)meta_mat(m) * P.n_mat + (int)meta_mat(mb)]);
+        const float2 kns = __ldg(&w.pair[P.pair_base + (int)meta_mat(m) * P.n_mat + (int)meta_mat(mb)]);
         F3 f = {0.0f, 0.0f, 0.0f};
         if (bonded < 0 || bonds_model == 0) {
             float tf = tf0;
@@ -907,7 +913,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     ((Fn / A) - (P.p.moment_contribution_factor * (bend * Rr)) / I < -sn ||
                      abtf / A > ss)) {
                     const int code = -10 + sign_i32(nd);
-                    record_break(w, P, s, step, bg, code, i, b);
+                    record_break(w, P, s, *w.step, bg, code, i, b);
                     w.s_bonded[j * N + i] = code;
                     mask &= ~(1u << (BSHIFT + j));
                     Fn = 0.0f;
@@ -937,7 +943,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 fy = fy + sf * (vy / L);
                 if (P.p.bonds_tear == 1 && sf >= sn) {
                     const int code = -10 + sign_i32(disp);
-                    record_break(w, P, s, step, bg, code, i, b);
+                    record_break(w, P, s, *w.step, bg, code, i, b);
                     w.s_bonded[j * N + i] = code;
                     mask &= ~(1u << (BSHIFT + j));
                     fx = 0.0f;
@@ -971,7 +977,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 const float atf = tf < 0.0f ? -tf : tf;
                 if (P.p.bonds_tear == 1 && (Fn < -sn || atf > ss)) {
                     const int code = -10 + sign_i32(nd);
-                    record_break(w, P, s, step, bg, code, i, b);
+                    record_break(w, P, s, *w.step, bg, code, i, b);
                     w.s_bonded[j * N + i] = code;
                     mask &= ~(1u << (BSHIFT + j));
                     Fn = 0.0f;
@@ -1070,11 +1076,7 @@ __device__ void end_of_step(const DevWorld &w) {
 }
 
 __global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w) {
-    __shared__ uint32_t ck[K * IB];
-    __shared__ int ci[K * IB];
     Narrow nr;
-    nr.ck = ck;
-    nr.ci = ci;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < w.N) interact_particle(w, i, nr);

@@ -35,6 +35,8 @@ def main():
         sc, p, ext = dem_scenes.c1_chains()
     elif a.workload == "c0_settle":
         sc, p, ext = dem_scenes.c0_settle()
+    elif a.workload == "c2_impact":
+        sc, p, ext = dem_scenes.c2_impact()
     elif a.workload == "dense_bed":
         sc, p, ext = dem_scenes.dense_bed(n=a.particles or (1 << 20))
     else:
