@@ -58,6 +58,7 @@ def parse_args():
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-active", type=int, default=16 << 20)
     ap.add_argument("--serve-timeout", type=float, default=240.0)
+    ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuner's picks")
     ap.add_argument("--plain", action="store_true",
                     help="plain kernel launches instead of CUDA graphs, so that ncu can list every "
                          "launch (a profiling aid, not a bench configuration)")
@@ -484,8 +485,14 @@ def run_ours_batch(args):
     dev = torch.device("cuda", local)
     items, desc = build_batch_workload(args.scenes, args.seed + rank)
     ntot = sum(int(it[0]["radii"].shape[0]) for it in items)
-    F = args.frame
-    batch = dem.Batch(items, device=local, reorder_interval=35, plain_launches=args.plain)
+    # autotuner: cell size, list skin (re-sort interval), block size and steps
+    # per graph, picked on a sample of the scenes before anything is timed
+    knobs, tune_info = {"reorder_interval": 35}, None
+    if not args.no_tune and not args.plain:
+        knobs, tune_info = dem.autotune(items, device=local)
+    g = knobs["reorder_interval"]
+    F = args.frame if args.frame_given else g * max(1, -(-35 // g))
+    batch = dem.Batch(items, device=local, plain_launches=args.plain, **knobs)
     stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -588,7 +595,8 @@ def run_ours_batch(args):
     cfg = dict(desc)
     cfg.update({"frame_steps": F, "parallelism": "replicas" if ws > 1 else "single",
                 "l2": "inputs larger than L2 (and a %d MiB write between frames, untimed)" % (FLUSH_BYTES >> 20),
-                "graph_steps": 35, "plain_path_particle_steps_per_s": plain_value,
+                "graph_steps": g, "knobs": knobs, "autotune": tune_info,
+                "plain_path_particle_steps_per_s": plain_value,
                 "batched_over_plain": value / plain_value if plain_value else None,
                 "rebuilds": st["reorders"], "list_overflows": st["list_overflows"]})
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
@@ -738,6 +746,7 @@ def main():
         run_serve(args)
         return
     batch = args.workload == "c3_batch"
+    args.frame_given = args.frame > 0
     if args.frame <= 0:
         args.frame = 35 if batch else 105
     if args.steps <= 0:

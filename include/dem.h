@@ -91,7 +91,9 @@ typedef struct dem_ext {
     int32_t diagnostics;              /* 1: maintain data[7n] every step as the reference does */
     int32_t reorder_interval;         /* steps per captured CUDA graph; 0 = library default (35) */
     int32_t block_size;               /* threads per block for particle kernels; 0 = default */
-    float search_cell_factor;         /* search-grid cell / (2 r_max + skin); 0 = default 1.0 (minimum) */
+    float search_cell_factor;         /* search-grid cell / (2 r_max + skin), in [0.5, inf); 0 = default
+                                         1.0.  Below 1 the cell searches span 5 x 5 cells instead of
+                                         3 x 3; results do not depend on it */
     int32_t event_capacity;           /* break-event ring size; 0 = default */
     float list_skin;                  /* candidate-list skin / r_max; 0 = default 0.2.  Lists are rebuilt
                                          when a particle moves beyond half the skin; results do not
@@ -223,6 +225,34 @@ int dem_batch_set_properties(dem_batch *b, int32_t scene, int32_t *selections,
 int dem_batch_break_events(dem_batch *b, dem_break_event *buf, int32_t cap, int32_t *n);
 int dem_batch_get_stats(dem_batch *b, dem_stats *out);
 void *dem_batch_stream(dem_batch *b);
+
+/* ---- Autotuning: knobs that change speed, never results ----------------
+ * No counterpart in the reference.  dem_batch_autotune builds trial batches
+ * from a sample of the given scenes (about sample_particles particles, spread
+ * over the size range; <= 0: 2,000,000), times trial_steps steps of each
+ * (<= 0: 140) after an equal warm-up, and picks, one knob at a time from the
+ * library defaults, the search-cell factor (0.68, 0.85, 1, 1.36 x (2 r_max +
+ * skin), i.e. about 1.5 to 3 r_max), the candidate-list skin (0.1, 0.2, 0.3,
+ * 0.45 r_max: how often particles are re-sorted by cell), the particle-kernel
+ * block size (128, 256, 512) and the steps per captured graph (21, 35, 70).
+ * Copy the result's four fields into each scene's dem_ext. */
+typedef struct dem_tune_result {
+    float search_cell_factor;
+    float list_skin;
+    int32_t block_size;
+    int32_t reorder_interval;         /* steps per captured graph */
+    double ms_per_step;               /* sample, chosen values */
+    double default_ms_per_step;       /* sample, library defaults */
+    int32_t trials;
+    int32_t sample_scenes;
+    int64_t sample_particles;
+    double seconds;                   /* wall time of the tuning */
+    int32_t reserved[8];
+} dem_tune_result;
+int dem_batch_autotune(const dem_scene *const *scenes, const dem_params *params, const dem_ext *exts,
+                       int32_t n_scenes, int32_t device, int64_t sample_particles, int32_t trial_steps,
+                       dem_tune_result *out);
+const char *dem_tune_last_error(void);
 
 /* ---- Serving: continuous batching of scene requests --------------------
  * No counterpart in the reference.  A server owns device arenas sized once

@@ -16,6 +16,10 @@
 
 namespace demgb {
 
+// Particle kernels launch with the world's block size, any multiple of 32 up
+// to 1024 (the autotuner tries 128, 256 and 512).
+constexpr int PK_MAX_THREADS = 1024;
+
 // ---------------------------------------------------------------- helpers
 
 __device__ __forceinline__ float len2f(float x, float y) { return sqrtf(x * x + y * y); }
@@ -265,7 +269,7 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
 // With w.ticket the kernel's last warp sets the rebuild conditional; without
 // it (large worlds, where thousands of fenced ticket atomics cost more than a
 // launch) k_decide does it.
-__global__ void __launch_bounds__(256) k_lom(DevWorld w, int in_graph, cudaGraphConditionalHandle cond) {
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_lom(DevWorld w, int in_graph, cudaGraphConditionalHandle cond) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < w.N) lom_particle(w, i);
     if (w.ticket && last_warp(&w.tickets[0])) {
@@ -305,7 +309,7 @@ __device__ __forceinline__ bool gated_off(const int32_t *gate) {
 
 // search-cell key of every particle (zero-radius ones go to their scene's
 // dead cell) and the per-cell histogram
-__global__ void __launch_bounds__(256) k_keys(DevWorld w, const int32_t *gate) {
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_keys(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
@@ -427,7 +431,7 @@ int scan_tmp_size(int n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
 
 // scatter: slot = start + (count-1) taken by an atomic decrement, which also
 // returns every count to zero for the next histogram
-__global__ void __launch_bounds__(256) k_scatter(DevWorld w, const int32_t *gate) {
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_scatter(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
@@ -439,7 +443,7 @@ __global__ void __launch_bounds__(256) k_scatter(DevWorld w, const int32_t *gate
 
 // in-cell ordering: each cell's members sorted by scene-local particle index,
 // so the cell lists equal a stable sort of the particles by cell key
-__global__ void __launch_bounds__(256) k_cell_order(DevWorld w, const int32_t *gate) {
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_cell_order(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= w.C) return;
@@ -476,7 +480,7 @@ int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int3
 // The particle at cell-order position k (sorted[k]) moves to its scene's
 // range at the same offset: new = particle_base + (k - first position of the
 // scene's cells).  Particles of frozen scenes stay where they are.
-__global__ void __launch_bounds__(256) k_inverse(DevWorld w, const int32_t *gate) {
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_inverse(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= w.N) return;
@@ -493,7 +497,7 @@ __global__ void __launch_bounds__(256) k_inverse(DevWorld w, const int32_t *gate
     }
 }
 
-__global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o, const int32_t *gate) {
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_gather(DevWorld w, DevWorld o, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
@@ -530,7 +534,7 @@ __global__ void __launch_bounds__(256) k_gather(DevWorld w, DevWorld o, const in
 // copy the permuted arrays back, so the live arrays keep their addresses
 // (a rebuild may or may not run in a given step; addresses captured in a
 // CUDA graph must not depend on it)
-__global__ void __launch_bounds__(256) k_copy_back(DevWorld w, DevWorld o, const int32_t *gate) {
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_copy_back(DevWorld w, DevWorld o, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
@@ -566,13 +570,13 @@ void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStr
 }
 
 // ------------------------------------------------------- candidate lists
-// After the reorder, each particle collects the particles of the 3x3 search
-// cells around it whose centres lie within ra + rb + skin: a superset of
+// After the reorder, each particle collects the particles of the 3x3 (or 5x5,
+// with stencil 2) search cells around it whose centres lie within ra + rb + skin: a superset of
 // every pair the reference can accept while no particle moves more than
 // skin/2.  More than NL candidates, or one farther than an int16 offset can
 // reach: the particle searches the cell table (built in the same rebuild) at
 // every step instead.
-__global__ void __launch_bounds__(256) k_list_build(DevWorld w, const int32_t *gate) {
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_list_build(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.N) return;
@@ -594,8 +598,8 @@ __global__ void __launch_bounds__(256) k_list_build(DevWorld w, const int32_t *g
     int gx, gy;
     search_xy(P, pa.x, pa.y, gx, gy);
     w.kbuild[i] = (uint32_t)(P.cell_base + gy * P.g_w + gx);
-    const int cy0 = max(gy - 1, 0), cy1 = min(gy + 1, P.g_h - 1);
-    const int cx0 = max(gx - 1, 0), cx1 = min(gx + 1, P.g_w - 1);
+    const int cy0 = max(gy - P.stencil, 0), cy1 = min(gy + P.stencil, P.g_h - 1);
+    const int cx0 = max(gx - P.stencil, 0), cx1 = min(gx + P.stencil, P.g_w - 1);
     int cnt = 0;
     bool over = false;
     for (int cy = cy0; cy <= cy1; ++cy) {
@@ -791,8 +795,8 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             }
             const int local = (int)w.kbuild[i] - P.cell_base;
             const int gx = local % P.g_w, gy = local / P.g_w;
-            const int cy0 = max(gy - 1, 0), cy1 = min(gy + 1, P.g_h - 1);
-            const int cx0 = max(gx - 1, 0), cx1 = min(gx + 1, P.g_w - 1);
+            const int cy0 = max(gy - P.stencil, 0), cy1 = min(gy + P.stencil, P.g_h - 1);
+            const int cx0 = max(gx - P.stencil, 0), cx1 = min(gx + P.stencil, P.g_w - 1);
             for (int cy = cy0; cy <= cy1; ++cy) {
                 const int row = P.cell_base + cy * P.g_w;
                 const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
@@ -1236,7 +1240,7 @@ void launch_mark_free(const DevWorld &w, int first, int count, int free_scene, c
 
 // ------------------------------------------------------- Set_Properties
 // Set_Properties.wgsl:68-90; selections are indexed by scene-local particle.
-__global__ void __launch_bounds__(256) k_set_properties(DevWorld w, int scene,
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_set_properties(DevWorld w, int scene,
                                                         const int32_t *__restrict__ sel,
                                                         int32_t *__restrict__ sel_out,
                                                         const int32_t *__restrict__ in) {

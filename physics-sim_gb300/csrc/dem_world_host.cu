@@ -261,7 +261,11 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
     // walls (or the particles, whichever is smaller in cells)
     const dem_params &p = h.params;
     h.skin = skin_factor * rmax;
-    float reach = std::max(2.0f * rmax + h.skin, 1e-30f) * std::max(h.cell_factor, 1.0f);
+    // cell side = factor x (2 r_max + skin); below 1 the searches span 5 x 5
+    // cells (stencil 2), so the factor may go down to 0.5
+    const float factor = std::max(h.cell_factor, 0.5f);
+    const int stencil = factor < 1.0f ? 2 : 1;
+    float reach = std::max(2.0f * rmax + h.skin, 1e-30f) * factor;
     double ex0, ex1, ey0, ey1;
     if (p.round_bounds == 0) {
         ex0 = -0.5 * p.hor_bound; ex1 = 0.5 * p.hor_bound;
@@ -302,7 +306,7 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
     P.g_y0 = (float)(ey0 - reach);
     P.g_w = gw;
     P.g_h = gh;
-    P.stencil = 1;
+    P.stencil = stencil;
     return DEM_OK;
 }
 
@@ -635,7 +639,11 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     if (scenes >= MAX_SCENES) return fail(DEM_E_INVALID, "too many scene slots");
     if (particles > (1LL << 30) || cells > (1LL << 31) - 2 || bonds > (1LL << 30))
         return fail(DEM_E_INVALID, "capacity too large");
-    if (ext.block_size) block = ext.block_size;
+    if (ext.block_size) {
+        if (ext.block_size < 32 || ext.block_size > 1024 || (ext.block_size & 31))
+            return fail(DEM_E_INVALID, "block_size must be a multiple of 32 in [32, 1024]");
+        block = ext.block_size;
+    }
     if (ext.reorder_interval > 0) graph_steps = ext.reorder_interval;
     if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
     use_graphs = ext.plain_launches == 0;
@@ -964,16 +972,24 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
     if (!side) CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int kernels = 0;
+    // a launch that fails during capture invalidates it: check the capture
+    // before every use of its graph and the launch status after every group
+    auto active = [&](cudaStreamCaptureStatus cs, cudaGraph_t g) {
+        return cs == cudaStreamCaptureStatusActive && g != nullptr;
+    };
     for (int k = 0; k < R; ++k) {
         cudaStreamCaptureStatus cs;
         cudaGraph_t g = nullptr;
         CKG(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+        if (!active(cs, g)) CKG(cudaErrorStreamCaptureInvalidated);
         cudaGraphConditionalHandle h;
         CKG(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
         kernels += launch_lom(d, block, stream, true, h);
+        CKG(cudaGetLastError());
         const cudaGraphNode_t *deps = nullptr;
         size_t ndeps = 0;
         CKG(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+        if (!active(cs, g)) CKG(cudaErrorStreamCaptureInvalidated);
         cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
         np.type = cudaGraphNodeTypeConditional;
         np.conditional.handle = h;
@@ -984,10 +1000,14 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
         cudaGraph_t body = np.conditional.phGraph_out[0];
         CKG(cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         enqueue_rebuild(side, d.rebuild);
+        const cudaError_t le = cudaGetLastError();
         cudaGraph_t body_out = nullptr;
-        CKG(cudaStreamEndCapture(side, &body_out));
+        const cudaError_t ee = cudaStreamEndCapture(side, &body_out);
+        CKG(le);
+        CKG(ee);
         CKG(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
         kernels += launch_interact(d, block, stream, has_bigs);
+        CKG(cudaGetLastError());
     }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(stream, &g);
@@ -1146,7 +1166,8 @@ int World::set_properties(int s, int32_t *selections, const int32_t *props) {
     for (int i = 0; i < n; ++i) any |= selections[i] != 0;
     if (props[9] == 1 && any && !(f[23] >= 0.0f && std::isfinite(f[23])))
         return fail(DEM_E_INVALID, "radius must be finite and >= 0");
-    if (props[9] == 1 && any && f[23] > h.r_max && f[23] * 2.0f * (1.0f + 1e-3f) > h.par.g_cs)
+    if (props[9] == 1 && any && f[23] > h.r_max &&
+        (2.0f * f[23] + h.skin) * (1.0f + 1e-3f) > h.par.g_cs * h.par.stencil)
         return fail(DEM_E_UNSUPPORTED, "radius beyond the search grid's reach; create a new context");
     int32_t *dsel = nullptr, *dout = nullptr, *dprops = nullptr;
     CK(cudaMalloc(&dsel, sizeof(int32_t) * (n > 0 ? n : 1)));

@@ -97,6 +97,13 @@ class ServerStats(C.Structure):
                                          "device_bytes", "steps")]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("search_cell_factor", C.c_float), ("list_skin", C.c_float), ("block_size", C.c_int32),
+                ("reorder_interval", C.c_int32), ("ms_per_step", C.c_double),
+                ("default_ms_per_step", C.c_double), ("trials", C.c_int32), ("sample_scenes", C.c_int32),
+                ("sample_particles", C.c_int64), ("seconds", C.c_double), ("reserved", C.c_int32 * 8)]
+
+
 BREAK_DTYPE = np.dtype([("scene", "<i4"), ("step", "<i4"), ("bond", "<i4"), ("code", "<i4"),
                         ("a", "<i4"), ("b", "<i4")])
 
@@ -114,7 +121,7 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_batch_kernel_time", "dem_server_config_defaults", "dem_server_create",
            "dem_server_destroy", "dem_server_last_error", "dem_server_submit", "dem_server_advance",
            "dem_server_poll", "dem_server_fetch", "dem_server_events", "dem_server_release",
-           "dem_server_get_stats", "dem_server_stream"]
+           "dem_server_get_stats", "dem_server_stream", "dem_batch_autotune", "dem_tune_last_error"]
 
 _lib = None
 
@@ -189,6 +196,10 @@ def lib(path=None):
     L.dem_server_destroy.restype = None
     L.dem_server_last_error.argtypes = [C.c_void_p]
     L.dem_server_last_error.restype = C.c_char_p
+    L.dem_tune_last_error.argtypes = []
+    L.dem_tune_last_error.restype = C.c_char_p
+    L.dem_batch_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64,
+                                     C.c_int32, C.POINTER(TuneResult)]
     L.dem_server_submit.argtypes = [C.c_void_p, C.POINTER(Scene), C.POINTER(Params), C.POINTER(Ext),
                                     C.c_int64, C.POINTER(C.c_int64)]
     L.dem_server_advance.argtypes = [C.c_void_p, C.c_int32]
@@ -203,7 +214,8 @@ def lib(path=None):
         if name not in ("dem_destroy", "dem_ext_defaults", "dem_last_error", "dem_stream",
                         "dem_abi_version", "dem_noalloc_last_error", "dem_batch_destroy",
                         "dem_batch_last_error", "dem_batch_stream", "dem_server_config_defaults",
-                        "dem_server_destroy", "dem_server_last_error", "dem_server_stream"):
+                        "dem_server_destroy", "dem_server_last_error", "dem_server_stream",
+                        "dem_tune_last_error"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -417,6 +429,36 @@ class Context:
         _check(L, self.h, L.dem_debug_search_grid(self.h, C.byref(x0), C.byref(y0), C.byref(inv),
                                                   C.byref(gw), C.byref(gh)))
         return x0.value, y0.value, inv.value, gw.value, gh.value
+
+
+def autotune(items, *, device=-1, sample_particles=0, trial_steps=0, **world_kw):
+    """dem_batch_autotune over (scene, params, ext) items: returns (ext keyword
+    arguments to pass to Batch/Context, info dict).  The knobs it picks change
+    speed only; results are the same for every choice."""
+    L = lib()
+    keep = []
+    n = len(items)
+    scenes = (Scene * n)()
+    params = (Params * n)()
+    exts = (Ext * n)()
+    for k, (sc, p, ext) in enumerate(items):
+        kw = dict(world_kw)
+        kw.update(ext)
+        scenes[k] = make_scene(sc)
+        params[k] = make_params(p)
+        exts[k] = make_ext(keep=keep, **kw)
+    ptrs = (C.c_void_p * n)(*[C.addressof(scenes[k]) for k in range(n)])
+    res = TuneResult()
+    rc = L.dem_batch_autotune(ptrs, C.addressof(params), C.addressof(exts), n, device,
+                              C.c_int64(sample_particles), trial_steps, C.byref(res))
+    if rc != 0:
+        raise DemError(rc, (L.dem_tune_last_error() or b"").decode())
+    chosen = {"search_cell_factor": float(res.search_cell_factor), "list_skin": float(res.list_skin),
+              "block_size": int(res.block_size), "reorder_interval": int(res.reorder_interval)}
+    info = {"ms_per_step": res.ms_per_step, "default_ms_per_step": res.default_ms_per_step,
+            "trials": int(res.trials), "sample_scenes": int(res.sample_scenes),
+            "sample_particles": int(res.sample_particles), "seconds": res.seconds}
+    return chosen, info
 
 
 class Batch:

@@ -1,0 +1,65 @@
+"""Autotuner and the knobs it turns: search-cell size (3 x 3 or 5 x 5 cell
+searches), candidate-list skin (re-sort frequency), particle-kernel block
+size and steps per captured graph change speed only -- every scene's state
+and bond-break events are the same bit for bit under any setting."""
+import pytest
+
+import dem
+import dem_scenes
+from gpu_backend import assert_same_state
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import build_lib
+    build_lib.build()
+
+
+def _items():
+    specs = [(700, 0.0, 11), (1800, 0.4, 12), (3000, 0.2, 13)]
+    items = [dem_scenes.c3_mix_scene(n, f, sd) for n, f, sd in specs]
+    items.append(dem_scenes.dense_bed(1500, seed=14))
+    items.append(dem_scenes.c1_chains(chains=4, length=30, seed=15, pull_velocity=20.0))
+    items.append(dem_scenes.c2_impact(cols=32, rows=48, seed=16, projectile_radius=8.0, projectile_speed=300.0))
+    return items
+
+
+def _run(items, steps, **kw):
+    with dem.Batch(items, **kw) as b:
+        b.step(steps)
+        states = [b.download(k) for k in range(len(items))]
+        ev = b.break_events()
+    evs = sorted((int(e["scene"]), int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"]))
+                 for e in ev)
+    return states, evs
+
+
+@pytest.mark.parametrize("knobs", [
+    dict(search_cell_factor=0.68, list_skin=0.45, block_size=128, reorder_interval=21),
+    dict(search_cell_factor=1.36, list_skin=0.1, block_size=512, reorder_interval=70),
+])
+def test_knobs_do_not_change_results(knobs):
+    items = _items()
+    steps = 210
+    ref, ref_ev = _run(items, steps)
+    got, got_ev = _run(items, steps, **knobs)
+    for k in range(len(items)):
+        assert_same_state(got[k], ref[k], "scene %d: " % k)
+    assert got_ev == ref_ev
+
+
+def test_autotune_picks_listed_values_and_keeps_results():
+    items = _items()
+    chosen, info = dem.autotune(items, sample_particles=6000, trial_steps=70)
+    assert chosen["search_cell_factor"] in (pytest.approx(0.68), pytest.approx(0.85), 1.0, pytest.approx(1.36))
+    assert chosen["list_skin"] in (pytest.approx(0.1), pytest.approx(0.2), pytest.approx(0.3), pytest.approx(0.45))
+    assert chosen["block_size"] in (128, 256, 512)
+    assert chosen["reorder_interval"] in (21, 35, 70)
+    assert info["trials"] >= 10 and info["ms_per_step"] <= info["default_ms_per_step"]
+    ref, ref_ev = _run(items, 105)
+    got, got_ev = _run(items, 105, **chosen)
+    for k in range(len(items)):
+        assert_same_state(got[k], ref[k], "scene %d: " % k)
+    assert got_ev == ref_ev
