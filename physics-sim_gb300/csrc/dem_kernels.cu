@@ -737,11 +737,31 @@ __device__ __forceinline__ int nl_entry(int4 a, int4 b, int k) {
     return (k & 1) ? (v >> 16) : (int)(int16_t)(v & 0xFFFF);
 }
 
+// L1 prefetch of one line (sm_90+ PTX): the later load of the same address
+// finds it on chip instead of waiting a DRAM round trip then.
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr) {
-    // the particle's own records, issued together
+    // The particle's own records: the ones needed first are loaded now, the
+    // rest (read only after the scene, detection and slot checks resolve)
+    // are prefetched now, so the DRAM round trips overlap instead of
+    // following one another.
     const uint32_t m = w.meta[i];
     const float4 pa = w.pr[i];
     uint32_t mask = w.smask[i];
+    prefetch_l1(&w.nl[2 * (size_t)i]);
+    prefetch_l1(&w.rr[i]);
+    prefetch_l1(&w.dp[i]);
+    prefetch_l1(&w.vw[i]);
+    const int N = w.N;
+    for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
+        const int j = __ffs(left) - 1;
+        prefetch_l1(&w.s_b[j * N + i]);
+        prefetch_l1(&w.s_tf[j * N + i]);
+        if ((mask >> (BSHIFT + j)) & 1u) prefetch_l1(&w.s_bonded[j * N + i]);
+    }
     const int s = (int)meta_scene(m);
     if (!w.act[s]) return;
     const ScenePar &P = w.par[s];
@@ -749,7 +769,6 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         w.dF[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return;
     }
-    const int N = w.N;
     const uint32_t before = mask;
     const int bonds_model = P.p.bonds;
 
@@ -845,6 +864,19 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     // fields, then what they index (partner records, bond records), so a
     // slot costs two dependent memory round trips instead of five.
     const float4 da = (mask & ((1u << K) - 1u)) ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    // partners' records and bond records of every slot, requested before the
+    // first slot is evaluated
+    for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
+        const int j = __ffs(left) - 1;
+        const int b = w.s_b[j * N + i];
+        prefetch_l1(&w.pr[b]);
+        prefetch_l1(&w.dp[b]);
+        if ((mask >> (BSHIFT + j)) & 1u) {
+            const int bg = P.bond_base + w.s_bonded[j * N + i];
+            prefetch_l1(&w.b_status[bg]);
+            prefetch_l1(&w.b_length[bg]);
+        }
+    }
     float nfx = 0.0f, nfy = 0.0f, nm = 0.0f;
     Acc3 acc = {0.0f, 0.0f, 0.0f};
     for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
