@@ -190,15 +190,17 @@ __device__ __forceinline__ bool last_warp(uint32_t *ticket) {
 // a particle that moved more than half the skin since the last rebuild asks
 // for a rebuild before this step's Simulation pass.
 __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
+    // all of the particle's records requested at once (valid for any i < N)
     uint32_t m = w.meta[i];
+    float4 p = w.pr[i];
+    float4 v = w.vw[i];
+    float4 a = w.ac[i];
+    const float2 b = w.pbuild[i];
     int s = (int)meta_scene(m);
     if (!w.act[s]) return;
     const ScenePar &P = w.par[s];
-    float4 p = w.pr[i];
     if (p.z == 0.0f) return;                                       // :83
     const float dT = P.p.dT;
-    float4 v = w.vw[i];
-    float4 a = w.ac[i];
     float ivx = v.x, ivy = v.y, iw = v.z;
     if (m & M_KICK_X) ivx = ivx + (a.x * dT) * 0.5f;               // :88
     if (m & M_KICK_Y) ivy = ivy + (a.y * dT) * 0.5f;               // :89
@@ -261,7 +263,6 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     }
     w.vw[i] = make_float4(ivx, ivy, iw, v.w);                      // :151-152
     if (!ext) w.dp[i] = d;
-    const float2 b = w.pbuild[i];
     const float ex = p.x - b.x, ey = p.y - b.y;
     if (!(ex * ex + ey * ey <= P.disp_limit2)) atomicOr(w.rebuild, 1);
 }
@@ -864,19 +865,6 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     // fields, then what they index (partner records, bond records), so a
     // slot costs two dependent memory round trips instead of five.
     const float4 da = (mask & ((1u << K) - 1u)) ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    // partners' records and bond records of every slot, requested before the
-    // first slot is evaluated
-    for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
-        const int j = __ffs(left) - 1;
-        const int b = w.s_b[j * N + i];
-        prefetch_l1(&w.pr[b]);
-        prefetch_l1(&w.dp[b]);
-        if ((mask >> (BSHIFT + j)) & 1u) {
-            const int bg = P.bond_base + w.s_bonded[j * N + i];
-            prefetch_l1(&w.b_status[bg]);
-            prefetch_l1(&w.b_length[bg]);
-        }
-    }
     float nfx = 0.0f, nfy = 0.0f, nm = 0.0f;
     Acc3 acc = {0.0f, 0.0f, 0.0f};
     for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
