@@ -254,6 +254,18 @@ int dem_batch_autotune(const dem_scene *const *scenes, const dem_params *params,
                        dem_tune_result *out);
 const char *dem_tune_last_error(void);
 
+/* ---- Bond generation: State::regen_bonds (src/state.rs:291-367) on the GPU
+ * Bonds every pair closer than 1.05 (r_i + r_j), at most max_bonds per
+ * particle on its own side (pairs taken in the reference's order), numbered
+ * in the reference's creation order, each taking the first free contact slot
+ * of both particles.  pos[2n] and radii[n] are host arrays; writes
+ * bonds[3 * nb] {status 1, angle bits, length bits} (nb <= bonds_cap, else
+ * DEM_E_CAPACITY with *n_bonds = nb so the caller can size the array) and
+ * contacts[84 n] exactly as regen_bonds does.  max_bonds in [1, 14]. */
+int dem_generate_bonds(const float *pos, const float *radii, int32_t n, int32_t max_bonds, int32_t device,
+                       int32_t *bonds, int64_t bonds_cap, int64_t *n_bonds, int32_t *contacts);
+const char *dem_bondgen_last_error(void);
+
 /* ---- Serving: continuous batching of scene requests --------------------
  * No counterpart in the reference.  A server owns device arenas sized once
  * from memory_budget_bytes (and at most ~1.25 x max_active_particles

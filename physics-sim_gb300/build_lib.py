@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 INC = os.path.join(ROOT, "include")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdemgb.so")
-SOURCES = ["dem_kernels.cu", "dem_world_host.cu", "dem_api.cu", "dem_batch.cu", "dem_server.cu", "dem_noalloc.cu", "dem_tune.cu"]
+SOURCES = ["dem_kernels.cu", "dem_world_host.cu", "dem_api.cu", "dem_batch.cu", "dem_server.cu", "dem_noalloc.cu", "dem_tune.cu", "dem_bondgen.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]

@@ -464,6 +464,13 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_cell_order(DevWorld w, const
     }
 }
 
+void launch_exclusive_scan(const int32_t *in, int32_t *out, int n, int32_t *tmp, cudaStream_t st) {
+    const int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (ntiles > 0) k_scan_tiles<<<ntiles, SCAN_THREADS, 0, st>>>(in, out, n, tmp, nullptr);
+    k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(tmp, ntiles, out, n, nullptr);
+    if (ntiles > 0) k_scan_add<<<ntiles, SCAN_THREADS, 0, st>>>(out, n, tmp, nullptr);
+}
+
 int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate) {
     if (w.N == 0) return 0;
     int ntiles = (w.C + SCAN_TILE - 1) / SCAN_TILE;

@@ -195,6 +195,8 @@ int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs);
 void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
                            const int32_t *d_props, int block, cudaStream_t st);
 int scan_tmp_size(int n);
+// out[0..n) = exclusive prefix sums of in[0..n), out[n] = total; tmp holds scan_tmp_size(n) ints
+void launch_exclusive_scan(const int32_t *in, int32_t *out, int n, int32_t *tmp, cudaStream_t st);
 // mark particles [first, first + count) as unused: scene `free_scene`, radius 0
 void launch_mark_free(const DevWorld &w, int first, int count, int free_scene, cudaStream_t st);
 

@@ -121,7 +121,8 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_batch_kernel_time", "dem_server_config_defaults", "dem_server_create",
            "dem_server_destroy", "dem_server_last_error", "dem_server_submit", "dem_server_advance",
            "dem_server_poll", "dem_server_fetch", "dem_server_events", "dem_server_release",
-           "dem_server_get_stats", "dem_server_stream", "dem_batch_autotune", "dem_tune_last_error"]
+           "dem_server_get_stats", "dem_server_stream", "dem_batch_autotune", "dem_tune_last_error",
+           "dem_generate_bonds", "dem_bondgen_last_error"]
 
 _lib = None
 
@@ -198,6 +199,10 @@ def lib(path=None):
     L.dem_server_last_error.restype = C.c_char_p
     L.dem_tune_last_error.argtypes = []
     L.dem_tune_last_error.restype = C.c_char_p
+    L.dem_bondgen_last_error.argtypes = []
+    L.dem_bondgen_last_error.restype = C.c_char_p
+    L.dem_generate_bonds.argtypes = [_FP, _FP, C.c_int32, C.c_int32, C.c_int32, _IP, C.c_int64,
+                                     C.POINTER(C.c_int64), _IP]
     L.dem_batch_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64,
                                      C.c_int32, C.POINTER(TuneResult)]
     L.dem_server_submit.argtypes = [C.c_void_p, C.POINTER(Scene), C.POINTER(Params), C.POINTER(Ext),
@@ -215,7 +220,7 @@ def lib(path=None):
                         "dem_abi_version", "dem_noalloc_last_error", "dem_batch_destroy",
                         "dem_batch_last_error", "dem_batch_stream", "dem_server_config_defaults",
                         "dem_server_destroy", "dem_server_last_error", "dem_server_stream",
-                        "dem_tune_last_error"):
+                        "dem_tune_last_error", "dem_bondgen_last_error"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -429,6 +434,27 @@ class Context:
         _check(L, self.h, L.dem_debug_search_grid(self.h, C.byref(x0), C.byref(y0), C.byref(inv),
                                                   C.byref(gw), C.byref(gh)))
         return x0.value, y0.value, inv.value, gw.value, gh.value
+
+
+def generate_bonds(pos, radii, max_bonds=6, device=-1):
+    """dem_generate_bonds: regen_bonds (src/state.rs:291-367) on the GPU.
+    Returns (bonds i32[3 nb] or [-1] when there are none, contacts i32[84 n]),
+    the arrays State::regen_bonds leaves in the state."""
+    L = lib()
+    pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1)
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    n = radii.size
+    contacts = np.empty(6 * MAX_CONTACTS * n, np.int32)
+    nb = C.c_int64(0)
+    cap = max(n * max_bonds, 1)
+    bonds = np.empty(3 * cap, np.int32)
+    rc = L.dem_generate_bonds(pos.ctypes.data_as(_FP), radii.ctypes.data_as(_FP), n, max_bonds, device,
+                              bonds.ctypes.data_as(_IP), cap, C.byref(nb), contacts.ctypes.data_as(_IP))
+    if rc != 0:
+        raise DemError(rc, (L.dem_bondgen_last_error() or b"").decode())
+    if nb.value == 0:
+        return np.full(1, -1, np.int32), contacts
+    return bonds[:3 * nb.value].copy(), contacts
 
 
 def autotune(items, *, device=-1, sample_particles=0, trial_steps=0, **world_kw):
