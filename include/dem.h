@@ -202,6 +202,25 @@ int dem_get_stats(dem_ctx *ctx, dem_stats *out);
  * order their own work against the steps. */
 void *dem_stream(dem_ctx *ctx);
 
+/* Fix, Drop and Release events (src/shaders/event_handling/Fix.wgsl,
+ * Drop.wgsl, Release.wgsl) applied to the particles marked in selections[n]
+ * (the reference's State::selections; Fix and Drop rewrite the marks as the
+ * shaders do).  Release with throw_particles != 0 also sets the velocity to
+ * (del_x, del_y) / (dT * ticks), the shader's click_info[0] == 1 branch. */
+#define DEM_EVENT_FIX 1
+#define DEM_EVENT_DROP 2
+#define DEM_EVENT_RELEASE 3
+int dem_event(dem_ctx *ctx, int32_t kind, int32_t *selections, int32_t throw_particles, float del_x, float del_y,
+              int32_t ticks);
+
+/* State::get_datum (src/state.rs:708-737) on the device state: out[10] =
+ * means over the selected particles of pos.x, pos.y, data[4], data[5], rot,
+ * data[6], data[1], data[2], data[3], except out[6] = sum of |data[0]|, in the
+ * reference's order (double accumulation in index order).  Only the selected
+ * particles' fields are read back.  Returns the number selected (0: the
+ * reference's None, out untouched) or a negative DEM_E_* code. */
+int dem_get_datum(dem_ctx *ctx, const int32_t *selections, double out[10]);
+
 /* ---- Batches: many independent scenes stepped together ------------------
  * No counterpart in the reference (one scene per program there).  A batch
  * holds n_scenes scenes resident on one GPU; dem_batch_step advances every
@@ -223,6 +242,9 @@ int dem_batch_set_params(dem_batch *b, int32_t scene, const dem_params *params);
 int dem_batch_set_properties(dem_batch *b, int32_t scene, int32_t *selections,
                              const int32_t props[DEM_PROPS_WORDS]);
 int dem_batch_break_events(dem_batch *b, dem_break_event *buf, int32_t cap, int32_t *n);
+int dem_batch_event(dem_batch *b, int32_t scene, int32_t kind, int32_t *selections, int32_t throw_particles,
+                    float del_x, float del_y, int32_t ticks);
+int dem_batch_get_datum(dem_batch *b, int32_t scene, const int32_t *selections, double out[10]);
 int dem_batch_get_stats(dem_batch *b, dem_stats *out);
 void *dem_batch_stream(dem_batch *b);
 

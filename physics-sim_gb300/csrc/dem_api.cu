@@ -186,6 +186,18 @@ int dem_set_properties(dem_ctx *ctx, int32_t *selections, const int32_t props[DE
     return world_rc(ctx, ctx->world.set_properties(0, selections, props));
 }
 
+int dem_event(dem_ctx *ctx, int32_t kind, int32_t *selections, int32_t throw_particles, float del_x, float del_y,
+              int32_t ticks) {
+    CTX_GUARD(ctx);
+    return world_rc(ctx, ctx->world.fixity_event(0, kind, selections, throw_particles, del_x, del_y, ticks));
+}
+
+int dem_get_datum(dem_ctx *ctx, const int32_t *selections, double out[10]) {
+    CTX_GUARD(ctx);
+    const int rc = ctx->world.get_datum(0, selections, out);
+    return rc < 0 ? world_rc(ctx, rc) : rc;
+}
+
 int dem_break_events(dem_ctx *ctx, dem_break_event *buf, int32_t cap, int32_t *n) {
     CTX_GUARD(ctx);
     if (cap < 0 || (cap > 0 && !buf)) return set_err(ctx, DEM_E_INVALID, "bad event buffer");

@@ -123,6 +123,18 @@ int dem_batch_set_properties(dem_batch *b, int32_t scene, int32_t *selections,
     return brc(b, b->world.set_properties(scene, selections, props));
 }
 
+int dem_batch_event(dem_batch *b, int32_t scene, int32_t kind, int32_t *selections, int32_t throw_particles,
+                    float del_x, float del_y, int32_t ticks) {
+    BATCH_GUARD(b);
+    return brc(b, b->world.fixity_event(scene, kind, selections, throw_particles, del_x, del_y, ticks));
+}
+
+int dem_batch_get_datum(dem_batch *b, int32_t scene, const int32_t *selections, double out[10]) {
+    BATCH_GUARD(b);
+    const int rc = b->world.get_datum(scene, selections, out);
+    return rc < 0 ? brc(b, rc) : rc;
+}
+
 int dem_batch_break_events(dem_batch *b, dem_break_event *buf, int32_t cap, int32_t *n) {
     BATCH_GUARD(b);
     if (cap < 0 || (cap > 0 && !buf)) return bset(b, DEM_E_INVALID, "bad event buffer");

@@ -536,6 +536,7 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_gather(DevWorld w, DevWorld 
     if (w.act[ss]) {
         const ScenePar &P = w.par[ss];
         w.sorted[i - P.particle_base + w.cell_start[P.cell_base]] = i;
+        w.o2i[P.particle_base + w.orig[src]] = i;
     }
 }
 
@@ -1263,6 +1264,62 @@ __global__ void k_mark_free(DevWorld w, int first, int count, int free_scene) {
 void launch_mark_free(const DevWorld &w, int first, int count, int free_scene, cudaStream_t st) {
     if (count <= 0) return;
     k_mark_free<<<(count + 255) / 256, 256, 0, st>>>(w, first, count, free_scene);
+}
+
+// ------------------------------------------------------- Fix / Drop / Release
+__global__ void k_fixity_event(DevWorld w, int base, const int32_t *__restrict__ idx, const int32_t *__restrict__ fix3,
+                               int count, int zero_vel, int set_vel, float vx, float vy) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int i = w.o2i[base + idx[t]];
+    const int f = fix3[t];
+    const int fx = (int)(int8_t)(f & 0xFF), fy = (int)(int8_t)((f >> 8) & 0xFF), fr = (int)(int8_t)((f >> 16) & 0xFF);
+    uint32_t m = w.meta[i] & ~(M_KICK_X | M_KICK_Y | M_KICK_R | M_FIX_X | M_FIX_Y | M_FIX_R);
+    m |= (fx == 0 ? M_KICK_X : 0u) | (fy == 0 ? M_KICK_Y : 0u) | (fr == 0 ? M_KICK_R : 0u);
+    m |= (fx == 1 ? M_FIX_X : 0u) | (fy == 1 ? M_FIX_Y : 0u) | (fr == 1 ? M_FIX_R : 0u);
+    w.meta[i] = m;
+    float4 v = w.vw[i];
+    if (zero_vel) {                                                // Fix.wgsl:50-52
+        v.x = 0.0f;
+        v.y = 0.0f;
+        v.z = 0.0f;
+    }
+    if (set_vel) {                                                 // Release.wgsl:86-89
+        v.x = vx;
+        v.y = vy;
+    }
+    w.vw[i] = v;
+}
+
+void launch_fixity_event(const DevWorld &w, int base, const int32_t *d_idx, const int32_t *d_fix3, int count,
+                         int zero_vel, int set_vel, float vx, float vy, cudaStream_t st) {
+    if (count <= 0) return;
+    k_fixity_event<<<(count + 255) / 256, 256, 0, st>>>(w, base, d_idx, d_fix3, count, zero_vel, set_vel, vx, vy);
+}
+
+// per particle: pos.x, pos.y, data[4], data[5], rot, data[6], data[0], data[1], data[2]
+__global__ void k_gather_datum(DevWorld w, int base, const int32_t *__restrict__ idx, int count,
+                               float *__restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int i = w.o2i[base + idx[t]];
+    const float4 p = w.pr[i], d4 = w.d4[i], dF = w.dF[i];
+    float *o = out + 9 * (size_t)t;
+    o[0] = p.x;
+    o[1] = p.y;
+    o[2] = d4.x;
+    o[3] = d4.y;
+    o[4] = p.w;
+    o[5] = d4.z;
+    o[6] = dF.x;
+    o[7] = dF.y;
+    o[8] = dF.z;
+}
+
+void launch_gather_datum(const DevWorld &w, int base, const int32_t *d_idx, int count, float *d_out,
+                         cudaStream_t st) {
+    if (count <= 0) return;
+    k_gather_datum<<<(count + 255) / 256, 256, 0, st>>>(w, base, d_idx, count, d_out);
 }
 
 // ------------------------------------------------------- Set_Properties

@@ -115,6 +115,7 @@ struct DevWorld {
     float4 *pr, *vw, *ac, *dp, *fx, *d4, *dF;
     uint32_t *meta;
     int32_t *orig;
+    int32_t *o2i;               // [N] particle_base + scene-local index -> internal index (kept by the reorder)
     uint32_t *smask;            // bits 0-13: occupied slots; 16-29: slot's bonded field >= 0; 31: DF_ZERO
     int2 *rr;                   // reference bucket range of the AABB: {x0 | x1 << 16, y0 | y1 << 16}
     int32_t *s_b, *s_bonded;
@@ -197,6 +198,16 @@ void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, i
 int scan_tmp_size(int n);
 // out[0..n) = exclusive prefix sums of in[0..n), out[n] = total; tmp holds scan_tmp_size(n) ints
 void launch_exclusive_scan(const int32_t *in, int32_t *out, int n, int32_t *tmp, cudaStream_t st);
+// Fix / Drop / Release events (src/shaders/event_handling/{Fix,Drop,Release}.wgsl)
+// on `count` particles of the scene whose first particle is `base`, given
+// by scene-local index: the primary fixity codes become fix3[t] (three codes
+// packed 8 bits each); Fix also zeroes the velocity and rotational velocity,
+// Release with set_vel sets the velocity.
+void launch_fixity_event(const DevWorld &w, int base, const int32_t *d_idx, const int32_t *d_fix3, int count,
+                         int zero_vel, int set_vel, float vx, float vy, cudaStream_t st);
+// gather of the datum fields (state.rs:708-737) of `count` particles, 9 floats each
+void launch_gather_datum(const DevWorld &w, int base, const int32_t *d_idx, int count, float *d_out,
+                         cudaStream_t st);
 // mark particles [first, first + count) as unused: scene `free_scene`, radius 0
 void launch_mark_free(const DevWorld &w, int first, int count, int free_scene, cudaStream_t st);
 

@@ -115,6 +115,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
         x.dF = dalloc<float4>(owned, N, ok);
         x.meta = dalloc<uint32_t>(owned, N, ok);
         x.orig = dalloc<int32_t>(owned, N, ok);
+        x.o2i = dalloc<int32_t>(owned, N, ok);
         x.smask = dalloc<uint32_t>(owned, N, ok);
         x.rr = dalloc<int2>(owned, N, ok);
         x.s_b = dalloc<int32_t>(owned, (size_t)K * N, ok);
@@ -486,6 +487,11 @@ int World::stage_scene(int s, const dem_scene *sc) {
     CK(up(d.dF + base, dF));
     CK(up(d.meta + base, meta));
     CK(up(d.orig + base, orig));
+    {
+        std::vector<int32_t> o2i(n);
+        for (int i = 0; i < n; ++i) o2i[i] = base + i;
+        CK(up(d.o2i + base, o2i));
+    }
     CK(up(d.smask + base, mask));
     for (int j = 0; j < K && n > 0; ++j) {
         size_t off = (size_t)j * N + base, src = (size_t)j * n;
@@ -1197,6 +1203,100 @@ int World::set_properties(int s, int32_t *selections, const int32_t *props) {
     }
     if (any && (props[0] == 1 || props[1] == 1 || props[9] == 1)) return force_rebuild();
     return DEM_OK;
+}
+
+// Fix.wgsl:44-54 (selections == 1 -> 2, fixity all 1, velocity and
+// rotational velocity 0), Drop.wgsl:34-41 (selections == 2 -> 1, fixity all
+// 0), Release.wgsl:77-92 (selections != 0: fixity = its second triple; with
+// throw_vel, velocity = (del_x, del_y) / (dT * ticks)).  The secondary codes
+// live in the host copy of fixity, so the new primary codes are formed here
+// and the device updates the particles' flags (and velocities).
+int World::fixity_event(int s, int kind, int32_t *selections, int throw_vel, float del_x, float del_y,
+                        int ticks) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    if (!selections) return fail(DEM_E_INVALID, "selections is NULL");
+    if (kind < DEM_EVENT_FIX || kind > DEM_EVENT_RELEASE) return fail(DEM_E_INVALID, "unknown event kind");
+    SceneHost &h = sh[s];
+    std::vector<int32_t> idx, fix3;
+    for (int i = 0; i < h.n; ++i) {
+        int32_t *f = &h.fixity[6 * (size_t)i];
+        if (kind == DEM_EVENT_FIX && selections[i] == 1) {
+            selections[i] = 2;
+            for (int k = 0; k < 6; ++k) f[k] = 1;
+        } else if (kind == DEM_EVENT_DROP && selections[i] == 2) {
+            selections[i] = 1;
+            for (int k = 0; k < 6; ++k) f[k] = 0;
+        } else if (kind == DEM_EVENT_RELEASE && selections[i] != 0) {
+            f[0] = f[3];
+            f[1] = f[4];
+            f[2] = f[5];
+        } else {
+            continue;
+        }
+        idx.push_back(i);
+        fix3.push_back((f[0] & 0xFF) | ((f[1] & 0xFF) << 8) | ((f[2] & 0xFF) << 16));
+    }
+    float vx = 0.0f, vy = 0.0f;
+    const int set_vel = kind == DEM_EVENT_RELEASE && throw_vel ? 1 : 0;
+    if (set_vel) {
+        const float q = h.params.dT * (float)ticks;
+        vx = del_x / q;
+        vy = del_y / q;
+    }
+    const int k = (int)idx.size();
+    if (k == 0) return DEM_OK;
+    int32_t *dbuf = nullptr;
+    CK(cudaMalloc(&dbuf, sizeof(int32_t) * 2 * (size_t)k));
+    cudaMemcpyAsync(dbuf, idx.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(dbuf + k, fix3.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, stream);
+    launch_fixity_event(d, h.particle_base, dbuf, dbuf + k, k, kind == DEM_EVENT_FIX ? 1 : 0, set_vel, vx, vy,
+                        stream);
+    const cudaError_t e = cudaStreamSynchronize(stream);
+    cudaFree(dbuf);
+    if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("fixity event: ") + cudaGetErrorString(e));
+    return DEM_OK;
+}
+
+// State::get_datum (state.rs:708-737): means over the selected particles of
+// pos, data[4], data[5], rot, data[6], data[1..3] and the sum of |data[0]|,
+// accumulated in double in index order as the reference does; only the
+// selected particles' fields cross from the device.  Returns the count.
+int World::get_datum(int s, const int32_t *selections, double out[10]) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    if (!selections || !out) return fail(DEM_E_INVALID, "selections/out is NULL");
+    const SceneHost &h = sh[s];
+    std::vector<int32_t> idx;
+    for (int i = 0; i < h.n; ++i)
+        if (selections[i] != 0) idx.push_back(i);
+    const int k = (int)idx.size();
+    if (k == 0) return 0;
+    std::vector<float> f(9 * (size_t)k);
+    void *dbuf = nullptr;
+    CK(cudaMalloc(&dbuf, sizeof(int32_t) * (size_t)k + sizeof(float) * 9 * (size_t)k));
+    int32_t *d_idx = static_cast<int32_t *>(dbuf);
+    float *d_out = reinterpret_cast<float *>(d_idx + k);
+    cudaMemcpyAsync(d_idx, idx.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, stream);
+    launch_gather_datum(d, h.particle_base, d_idx, k, d_out, stream);
+    cudaMemcpyAsync(f.data(), d_out, sizeof(float) * 9 * (size_t)k, cudaMemcpyDeviceToHost, stream);
+    const cudaError_t e = cudaStreamSynchronize(stream);
+    cudaFree(dbuf);
+    if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("datum: ") + cudaGetErrorString(e));
+    double sums[10] = {0.0};
+    for (int t = 0; t < k; ++t) {
+        const float *g = &f[9 * (size_t)t];
+        sums[0] += (double)g[0];
+        sums[1] += (double)g[1];
+        sums[2] += (double)g[2];
+        sums[3] += (double)g[3];
+        sums[4] += (double)g[4];
+        sums[5] += (double)g[5];
+        sums[6] += std::fabs((double)g[6]);
+        sums[7] += (double)g[7];
+        sums[8] += (double)g[8];
+        sums[9] += (double)h.data3[idx[t]];
+    }
+    for (int q = 0; q < 10; ++q) out[q] = q == 6 ? sums[q] : sums[q] / (double)k;
+    return k;
 }
 
 int World::drain_events(std::vector<dem_break_event> &out) {

@@ -72,6 +72,8 @@ class World {
     int set_params(int s, const dem_params &p);
     int set_materials(int s, const float *m, int n);
     int set_properties(int s, int32_t *selections, const int32_t *props);
+    int fixity_event(int s, int kind, int32_t *selections, int throw_vel, float del_x, float del_y, int ticks);
+    int get_datum(int s, const int32_t *selections, double out[10]);
     int step(int n_steps);
     int sync();
     int drain_events(std::vector<dem_break_event> &out);

@@ -104,6 +104,8 @@ class TuneResult(C.Structure):
                 ("sample_particles", C.c_int64), ("seconds", C.c_double), ("reserved", C.c_int32 * 8)]
 
 
+EVENT_FIX, EVENT_DROP, EVENT_RELEASE = 1, 2, 3
+
 BREAK_DTYPE = np.dtype([("scene", "<i4"), ("step", "<i4"), ("bond", "<i4"), ("code", "<i4"),
                         ("a", "<i4"), ("b", "<i4")])
 
@@ -122,7 +124,8 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_server_destroy", "dem_server_last_error", "dem_server_submit", "dem_server_advance",
            "dem_server_poll", "dem_server_fetch", "dem_server_events", "dem_server_release",
            "dem_server_get_stats", "dem_server_stream", "dem_batch_autotune", "dem_tune_last_error",
-           "dem_generate_bonds", "dem_bondgen_last_error"]
+           "dem_generate_bonds", "dem_bondgen_last_error", "dem_event", "dem_get_datum",
+           "dem_batch_event", "dem_batch_get_datum"]
 
 _lib = None
 
@@ -199,6 +202,11 @@ def lib(path=None):
     L.dem_server_last_error.restype = C.c_char_p
     L.dem_tune_last_error.argtypes = []
     L.dem_tune_last_error.restype = C.c_char_p
+    L.dem_event.argtypes = [C.c_void_p, C.c_int32, _IP, C.c_int32, C.c_float, C.c_float, C.c_int32]
+    L.dem_get_datum.argtypes = [C.c_void_p, _IP, C.POINTER(C.c_double)]
+    L.dem_batch_event.argtypes = [C.c_void_p, C.c_int32, C.c_int32, _IP, C.c_int32, C.c_float, C.c_float,
+                                  C.c_int32]
+    L.dem_batch_get_datum.argtypes = [C.c_void_p, C.c_int32, _IP, C.POINTER(C.c_double)]
     L.dem_bondgen_last_error.argtypes = []
     L.dem_bondgen_last_error.restype = C.c_char_p
     L.dem_generate_bonds.argtypes = [_FP, _FP, C.c_int32, C.c_int32, C.c_int32, _IP, C.c_int64,
@@ -385,6 +393,25 @@ class Context:
         L = lib()
         cc = np.ascontiguousarray(cc, dtype=np.int32)
         _check(L, self.h, L.dem_set_control(self.h, cc.ctypes.data_as(_IP)))
+
+    def event(self, kind, selections, throw=False, del_x=0.0, del_y=0.0, ticks=1):
+        """Fix / Drop / Release (EVENT_FIX, EVENT_DROP, EVENT_RELEASE) on the
+        marked particles; `selections` (int32[n]) is updated in place."""
+        L = lib()
+        assert selections.dtype == np.int32 and selections.flags.c_contiguous
+        _check(L, self.h, L.dem_event(self.h, kind, selections.ctypes.data_as(_IP), 1 if throw else 0,
+                                      del_x, del_y, ticks))
+
+    def datum(self, selections):
+        """State::get_datum on the device state: 10 doubles, or None when
+        nothing is selected."""
+        L = lib()
+        sel = np.ascontiguousarray(selections, dtype=np.int32)
+        out = (C.c_double * 10)()
+        rc = L.dem_get_datum(self.h, sel.ctypes.data_as(_IP), out)
+        if rc < 0:
+            _check(L, self.h, rc)
+        return None if rc == 0 else np.array(out[:], np.float64)
 
     def break_events(self, cap=1 << 16):
         L = lib()

@@ -247,3 +247,21 @@ def test_zero_radius_and_empty_slots_edge_cases():
     sc["radii"][::17] = 0.0
     g, o, _, _ = run_both(sc, p, 120, chunk=30)
     assert_same_state(g, o)
+
+
+def test_checkpoint_through_a_saved_state_resumes_bit_exact():
+    """State::save -> file -> State::load -> restore (state_io + dem_upload)
+    in the middle of a run: the resumed run equals the uninterrupted one."""
+    import state_io
+    sc, p, ext = dem_scenes.dense_bed(n=1200, seed=31)
+    with dem.Context(sc, p) as a:
+        a.step(100)
+        buf = state_io.save_state(a.download(), p)
+        a.step(100)
+        ref = a.download()
+    sc2, uni, info = state_io.load_state(buf)
+    assert uni["dT"] == float(np.float32(p["dT"])) and uni["collision_interval"] == 1
+    with dem.Context(sc2, p) as b:
+        b.step(100)
+        got = b.download()
+    assert_same_state(got, ref, "resumed: ")

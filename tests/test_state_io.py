@@ -1,0 +1,111 @@
+"""FlatBuffers saved states (state_io): reading both schemas, writing the new
+one the way State::save does (src/state.rs:369-493), and the round trip."""
+import glob
+import os
+import struct
+
+import numpy as np
+import pytest
+
+import dem_scenes
+import state_io
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _same_scene(a, b):
+    for k in a:
+        if k == "grid":
+            assert a[k] == b[k]
+        else:
+            assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.bin"))), ids=os.path.basename)
+def test_golden_states_round_trip_through_the_writer(path):
+    sc, uni, info = state_io.load_state(path)
+    out = state_io.save_state(sc, uni, info)
+    sc2, uni2, info2 = state_io.load_state(out)
+    _same_scene(sc, sc2)
+    assert uni == uni2
+    # every settings byte, padding included, as the reference wrote it
+    assert info2["settings_raw"] == info["settings_raw"]
+    assert info2["scripts"] == info["scripts"]
+    assert np.array_equal(info2["groups"], info["groups"])
+    assert len(out) % 4 == 0
+
+
+def test_layouts_follow_the_flatbuffers_struct_rules():
+    names = {n: o for n, _, o in state_io.SETTINGS_NEW}
+    assert names["particles"] == 76 and names["timestep"] == 116 and names["gravity"] == 156
+    assert names["use_f64"] == 116 + 36 and names["bond_tearing"] == 156 + 24
+    old = {n: o for n, _, o in state_io.SETTINGS_OLD}
+    assert old["gravity"] == 152 and old["bond_normal_stiffness"] == 152 + 24
+    assert "use_f64" not in old and "bond_tearing" not in old
+
+
+def _write_old(scene, settings_values):
+    """A State of schema.fbs (14 vectors, then the 204-byte settings; no
+    scripts), written with the same front-to-back layout."""
+    raw = bytearray(state_io.SETTINGS_OLD_SIZE)
+    for name, kind, off in state_io.SETTINGS_OLD:
+        v = settings_values.get(name, 0)
+        if kind == "b":
+            raw[off] = 1 if v else 0
+        elif kind == "i":
+            struct.pack_into("<i", raw, off, int(v))
+        else:
+            struct.pack_into("<f", raw, off, float(v))
+    nf = 15
+    vt_pos, vt_size = 4, 4 + 2 * nf
+    table_pos = (vt_pos + vt_size + 3) // 4 * 4
+    b = state_io._Builder()
+    b.buf += struct.pack("<I", table_pos)
+    b.buf += struct.pack("<%dH" % (nf + 2), vt_size, 4 + 4 * 14 + len(raw), *[4 + 4 * i for i in range(nf)])
+    b.align()
+    b.buf += struct.pack("<i", table_pos - vt_pos) + b"\0" * (4 * 14) + bytes(raw)
+    keys = ["pos", "vel", "acc", "rot", "rot_vel", "rot_acc", "forces", "radii", "fixity", "bonds", "contacts",
+            "material_pointers", "materials"]
+    targets = [b.vector(np.asarray(scene[k])) for k in keys] + [b.vector(np.zeros(3, np.int32))]
+    for i, t in enumerate(targets):
+        fo = table_pos + 4 + 4 * i
+        struct.pack_into("<I", b.buf, fo, t - fo)
+    return bytes(b.buf)
+
+
+def test_old_schema_state_is_read():
+    sc, p, ext = dem_scenes.c1_chains(chains=2, length=10)
+    vals = {"particles": 20, "max_radius": 1.0, "timestep": 1e-4, "gen_per_frame": 105, "width": 60.0,
+            "height": 30.0, "x_timesteps": 7, "gravity": True, "g_force": 1.0, "collisions": True,
+            "collision_interval": 1, "friction_coef": 0.5, "bond": 3, "bond_normal_stiffness": 1e5,
+            "bond_shear_stiffness": 5e4, "bond_normal_strength": 5e3, "bond_shear_strength": 5e3,
+            "moment_contribution_factor": 1.0, "local_damping_alpha": 0.1}
+    buf = _write_old(sc, vals)
+    sc2, uni, info = state_io.load_state(buf)
+    assert info["schema"] == "old" and info["scripts"] == ""
+    assert info["use_f64"] is False and info["bond_tearing"] is False
+    assert info["x_timesteps"] == 7 and uni["bonds"] == 3 and uni["bonds_tear"] == 0
+    for k in ("pos", "radii", "fixity", "bonds", "contacts", "materials"):
+        assert np.array_equal(sc2[k], sc[k]), k
+    assert np.array_equal(sc2["del_pos"], sc2["vel"])
+
+
+def test_fresh_scene_saves_and_loads():
+    sc, p, ext = dem_scenes.c0_settle(n=400, seed=3)
+    buf = state_io.save_state(sc, p, use_f64=True)
+    sc2, uni, info = state_io.load_state(buf)
+    assert info["particles"] == 400 and info["use_f64"] is True
+    for k in ("pos", "radii", "vel", "fixity", "contacts", "material_pointers", "materials"):
+        assert np.array_equal(sc2[k], np.asarray(sc[k])), k
+    for k in ("dT", "hor_bound", "vert_bound", "friction_coefficient", "gravity_acc"):
+        assert uni[k] == float(np.float32(p[k])), k
+    for k in ("gravity", "planet_mode", "collisions", "collision_interval", "bonds"):
+        assert uni[k] == p[k], k
+
+
+def test_truncated_buffers_raise():
+    sc, uni, info = state_io.load_state(os.path.join(GOLDEN, "TEXPS.bin"))
+    buf = state_io.save_state(sc, uni, info)
+    for cut in (3, 40, len(buf) // 2):
+        with pytest.raises(ValueError):
+            state_io.load_state(buf[:cut])
