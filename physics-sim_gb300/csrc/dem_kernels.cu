@@ -1076,20 +1076,20 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     if (mask != before) w.smask[i] = mask;
 }
 
-// End of step, run by one warp (the last warp of k_interact, or k_end_step): breaks of this step
+// End of step, run by the last warp of k_interact or by k_end_step's block: breaks of this step
 // become visible (status = min code), the positions-set flags clear
 // (2D_Simulation.wgsl:258-261), the step counter advances, and each scene's
 // narrow-phase flag for the next step is set.
-__device__ void end_of_step(const DevWorld &w) {
-    const int lane = threadIdx.x & 31;
+template <int NT>
+__device__ void end_of_step(const DevWorld &w, int tid) {
     uint32_t n = *(volatile uint32_t *)w.pend_count;
     if (n > w.pend_cap) n = w.pend_cap;
-    for (uint32_t k = lane; k < n; k += 32) {
+    const long long next = *(volatile long long *)w.step + 1;
+    for (uint32_t k = tid; k < n; k += NT) {
         Pending p = w.pend[k];
         atomicMin(&w.b_status[p.bond], p.code);
     }
-    const long long next = *(volatile long long *)w.step + 1;
-    for (int s = lane; s < w.S; s += 32) {
+    for (int s = tid; s < w.S; s += NT) {
         w.cc3[s] = 0;
         const ScenePar &P = w.par[s];
         w.det[s] = detect_at(P.p.collision_interval, P.cc1_0, next - P.step0) ? 1 : 0;
@@ -1099,8 +1099,9 @@ __device__ void end_of_step(const DevWorld &w) {
             if (left <= 0) w.act[s] = 0;  // a served scene stops at its horizon
         }
     }
-    __syncwarp();
-    if (lane == 0) {
+    if (NT == 32) __syncwarp();
+    else __syncthreads();
+    if (tid == 0) {
         *w.pend_count = 0u;
         *w.step = next;
         w.tickets[1] = 0u;
@@ -1112,10 +1113,11 @@ __global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w) {
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < w.N) interact_particle(w, i, nr);
-    if (w.ticket && last_warp(&w.tickets[1])) end_of_step(w);
+    if (w.ticket && last_warp(&w.tickets[1])) end_of_step<32>(w, threadIdx.x & 31);
 }
 
-__global__ void k_end_step(DevWorld w) { end_of_step(w); }
+constexpr int END_THREADS = 256;
+__global__ void __launch_bounds__(END_THREADS) k_end_step(DevWorld w) { end_of_step<END_THREADS>(w, threadIdx.x); }
 
 // Narrow phase of one large particle per block (2D_Simulation.wgsl:126-170
 // with the particle's whole neighbourhood): every particle of the search
@@ -1245,7 +1247,7 @@ int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs) {
     k_interact<<<g, IB, 0, st>>>(w);
     k++;
     if (w.ticket) return k;
-    k_end_step<<<1, 32, 0, st>>>(w);
+    k_end_step<<<1, END_THREADS, 0, st>>>(w);
     return k + 1;
 }
 
