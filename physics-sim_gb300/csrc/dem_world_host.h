@@ -14,13 +14,10 @@
 namespace demgb {
 
 struct SceneHost {
-    // reference-layout copies of what the step never writes (kept for download)
-    std::vector<int32_t> fixity;       // [6n]
-    std::vector<float> forces;         // [6n]
-    std::vector<int32_t> material_ptr; // [n]
+    // reference-layout copies of what the step never writes (kept for download;
+    // fixity, forces, material pointers and data[7i+3] stay on the device)
     std::vector<float> materials;      // [6m]
     std::vector<int32_t> bond_angle;   // [B] raw bits
-    std::vector<float> data3;          // [n] data[7i+3], never written by a step
     std::vector<float> bond_sn, bond_ss;
     dem_params params;
     dem_grid_info grid;
@@ -139,6 +136,12 @@ class World {
     void drop_graph();
     DevWorld spare{};
     std::vector<void *> owned;
+    // device copy of one scene in the reference layouts (uploads, downloads)
+    RefArrays ref{};
+    void *ref_block = nullptr;
+    long long ref_cap = 0;
+    int32_t *ref_err = nullptr;
+    int ensure_ref(long long n);
     cudaGraphExec_t graph = nullptr;   // graph_steps steps
     cudaGraphExec_t graph1 = nullptr;  // one step, for remainders
     int graph_R = 0;

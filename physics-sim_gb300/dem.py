@@ -357,9 +357,11 @@ class Context:
         L = lib()
         _check(L, self.h, L.dem_synchronize(self.h))
 
-    def download(self):
+    def download(self, out=None):
+        """The scene in the reference's layouts (update_state); `out`, a scene
+        dict from an earlier download, is filled in place instead of a new one."""
         L = lib()
-        out = empty_like_scene(self._template)
+        out = empty_like_scene(self._template) if out is None else out
         st = make_scene(out)
         _check(L, self.h, L.dem_download(self.h, C.byref(st)))
         out["coll_cont"] = np.array(st.coll_cont[:], dtype=np.int32)
@@ -572,8 +574,8 @@ class Batch:
     def synchronize(self):
         self._check(lib().dem_batch_synchronize(self.h))
 
-    def download(self, scene):
-        out = empty_like_scene(self._templates[scene])
+    def download(self, scene, out=None):
+        out = empty_like_scene(self._templates[scene]) if out is None else out
         st = make_scene(out)
         self._check(lib().dem_batch_download(self.h, int(scene), C.byref(st)))
         out["coll_cont"] = np.array(st.coll_cont[:], dtype=np.int32)
