@@ -752,6 +752,12 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
+// The Simulation pass of one particle.  PART selects what runs: 0 all of it
+// (k_interact), 1 the narrow phase and slot bookkeeping (k_narrow), 2 the
+// force loop and store_forces (k_forces) -- the split form trades a second
+// read of the particle's records for two kernels with fewer registers,
+// which pays in dense scenes.
+template <int PART>
 __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr) {
     // The particle's own records: the ones needed first are loaded now, the
     // rest (read only after the scene, detection and slot checks resolve)
@@ -760,22 +766,26 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     const uint32_t m = w.meta[i];
     const float4 pa = w.pr[i];
     uint32_t mask = w.smask[i];
-    prefetch_l1(&w.nl[2 * (size_t)i]);
-    prefetch_l1(&w.rr[i]);
-    prefetch_l1(&w.dp[i]);
-    prefetch_l1(&w.vw[i]);
+    if (PART != 2) {
+        prefetch_l1(&w.nl[2 * (size_t)i]);
+        prefetch_l1(&w.rr[i]);
+    }
+    if (PART != 1) {
+        prefetch_l1(&w.dp[i]);
+        prefetch_l1(&w.vw[i]);
+    }
     const int N = w.N;
     for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
         const int j = __ffs(left) - 1;
         prefetch_l1(&w.s_b[j * N + i]);
-        prefetch_l1(&w.s_tf[j * N + i]);
+        if (PART != 1) prefetch_l1(&w.s_tf[j * N + i]);
         if ((mask >> (BSHIFT + j)) & 1u) prefetch_l1(&w.s_bonded[j * N + i]);
     }
     const int s = (int)meta_scene(m);
     if (!w.act[s]) return;
     const ScenePar &P = w.par[s];
     if (pa.z == 0.0f) {                                            // :113-118
-        w.dF[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (PART != 1) w.dF[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return;
     }
     const uint32_t before = mask;
@@ -783,7 +793,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
 
     // Loads that only some particles need (the bucket range, the second half
     // of the candidate list, del_pos) wait until the particle needs them.
-    const bool detect = P.p.collisions == 1 && w.det[s] != 0;
+    const bool detect = PART != 2 && P.p.collisions == 1 && w.det[s] != 0;
     if (detect) {                                                  // :126-228
         nr.cnt = 0;
         int ax0, ax1, ay0, ay1;
@@ -866,6 +876,11 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             w.s_b[j * N + i] = nr_ci[q * IB + t];
             w.s_tf[j * N + i] = 0.0f;
         }
+    }
+
+    if (PART == 1) {
+        if (mask != before) w.smask[i] = mask;
+        return;
     }
 
     // force loop (:230-255), slots in ascending order
@@ -1112,7 +1127,22 @@ __global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle(w, i, nr);
+    if (i < w.N) interact_particle<0>(w, i, nr);
+    if (w.ticket && last_warp(&w.tickets[1])) end_of_step<32>(w, threadIdx.x & 31);
+}
+
+__global__ void __launch_bounds__(IB, 12) k_narrow(DevWorld w) {
+    Narrow nr;
+    nr.cnt = 0;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < w.N) interact_particle<1>(w, i, nr);
+}
+
+__global__ void __launch_bounds__(IB, 8) k_forces(DevWorld w) {
+    Narrow nr;
+    nr.cnt = 0;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < w.N) interact_particle<2>(w, i, nr);
     if (w.ticket && last_warp(&w.tickets[1])) end_of_step<32>(w, threadIdx.x & 31);
 }
 
@@ -1244,8 +1274,14 @@ int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs) {
         k++;
     }
     const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
-    k_interact<<<g, IB, 0, st>>>(w);
-    k++;
+    if (w.split) {
+        k_narrow<<<g, IB, 0, st>>>(w);
+        k_forces<<<g, IB, 0, st>>>(w);
+        k += 2;
+    } else {
+        k_interact<<<g, IB, 0, st>>>(w);
+        k++;
+    }
     if (w.ticket) return k;
     k_end_step<<<1, END_THREADS, 0, st>>>(w);
     return k + 1;

@@ -154,6 +154,7 @@ struct DevWorld {
     int32_t *rebuild;           // 1 = the next rebuild body runs
     uint32_t *tickets;          // [2] last-warp counters of k_lom and k_interact
     int32_t ticket;             // 1: those kernels' last warps end the step; 0: separate one-warp kernels
+    int32_t split;              // 1: the Simulation pass as k_narrow + k_forces instead of k_interact
     int32_t *big_acc;           // [slots][16]: accepted partners of a large particle, [15] = count
     int32_t *big_scene;         // [slots] scene of each big-partner record, -1 unused
     int32_t n_big_slots;

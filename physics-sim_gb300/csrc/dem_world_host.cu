@@ -144,6 +144,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
     DevWorld &w = d;
     w.N = N; w.C = C; w.B = B; w.S = S; w.M = M; w.MP = MP;
     w.ticket = N <= TICKET_MAX_N ? 1 : 0;
+    w.split = split_narrow ? 1 : 0;
     auto particle_arrays = [&](DevWorld &x) {
         x.pr = dalloc<float4>(owned, N, ok);
         x.vw = dalloc<float4>(owned, N, ok);
@@ -552,6 +553,7 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     if (ext.list_skin < 0.0f) return fail(DEM_E_INVALID, "list_skin < 0");
     if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
     use_graphs = ext.plain_launches == 0;
+    split_narrow = ext.split_narrow != 0;
     diagnostics = ext.diagnostics != 0;
     sh.assign(S, SceneHost{});
     long long N = 0, C = 0, B = 0, M = 0, MP = 0, TB = 0;
@@ -636,6 +638,7 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     if (ext.reorder_interval > 0) graph_steps = ext.reorder_interval;
     if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
     use_graphs = ext.plain_launches == 0;
+    split_narrow = ext.split_narrow != 0;
     diagnostics = ext.diagnostics != 0;
     const int S = scenes + 1;  // the last slot owns the unused particles
     free_slot = scenes;

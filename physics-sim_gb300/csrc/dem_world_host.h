@@ -104,6 +104,7 @@ class World {
     std::vector<SceneHost> sh;
     DevWorld d{};
     bool use_graphs = true;
+    bool split_narrow = false;     // Simulation pass as two kernels (dem_ext::split_narrow)
     bool has_bigs = false;         // some scene has large particles: k_big_narrow runs each step
     long long launches = 0;
     // kernel timing (debug): event pairs per kernel kind, summed on demand

@@ -1,7 +1,8 @@
 """Autotuner and the knobs it turns: search-cell size (3 x 3 or 5 x 5 cell
 searches), candidate-list skin (re-sort frequency), particle-kernel block
-size and steps per captured graph change speed only -- every scene's state
-and bond-break events are the same bit for bit under any setting."""
+size, steps per captured graph and the one- or two-kernel Simulation pass
+change speed only -- every scene's state and bond-break events are the same
+bit for bit under any setting."""
 import pytest
 
 import dem
@@ -37,7 +38,7 @@ def _run(items, steps, **kw):
 
 
 @pytest.mark.parametrize("knobs", [
-    dict(search_cell_factor=0.68, list_skin=0.45, block_size=128, reorder_interval=21),
+    dict(search_cell_factor=0.68, list_skin=0.45, block_size=128, reorder_interval=21, split_narrow=1),
     dict(search_cell_factor=1.36, list_skin=0.1, block_size=512, reorder_interval=70),
 ])
 def test_knobs_do_not_change_results(knobs):
@@ -57,6 +58,7 @@ def test_autotune_picks_listed_values_and_keeps_results():
     assert chosen["list_skin"] in (pytest.approx(0.1), pytest.approx(0.2), pytest.approx(0.3), pytest.approx(0.45))
     assert chosen["block_size"] in (128, 256, 512)
     assert chosen["reorder_interval"] in (21, 35, 70)
+    assert chosen["split_narrow"] in (0, 1)
     assert info["trials"] >= 10 and info["ms_per_step"] <= info["default_ms_per_step"]
     ref, ref_ev = _run(items, 105)
     got, got_ev = _run(items, 105, **chosen)
