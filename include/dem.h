@@ -102,7 +102,10 @@ typedef struct dem_ext {
                                          graphs with conditional nodes) */
     int32_t split_narrow;             /* 1: narrow phase and forces as two kernels (fewer registers
                                          each; faster in dense scenes); results do not depend on it */
-    int32_t reserved[4];
+    int32_t unfused_lom;              /* 1: every step runs its own LOM kernel instead of the next
+                                         step's LOM pass running inside the Simulation kernel (the
+                                         default, fewer bytes per step); results do not depend on it */
+    int32_t reserved[3];
 } dem_ext;
 
 /* One scene in the reference's host layouts (state.rs:69-93).  Arrays hold
@@ -258,9 +261,10 @@ void *dem_batch_stream(dem_batch *b);
  * library defaults, the search-cell factor (0.68, 0.85, 1, 1.36 x (2 r_max +
  * skin), i.e. about 1.5 to 3 r_max), the candidate-list skin (0.1, 0.2, 0.3,
  * 0.45 r_max: how often particles are re-sorted by cell), the particle-kernel
- * block size (128, 256, 512), the steps per captured graph (21, 35, 70) and
- * whether the Simulation pass runs as one kernel or two (split_narrow).
- * Copy the result's five fields into each scene's dem_ext. */
+ * block size (128, 256, 512), the steps per captured graph (21, 35, 70),
+ * whether the Simulation pass runs as one kernel or two (split_narrow) and
+ * whether it carries the next step's LOM pass (unfused_lom).
+ * Copy the result's six fields into each scene's dem_ext. */
 typedef struct dem_tune_result {
     float search_cell_factor;
     float list_skin;
@@ -273,7 +277,8 @@ typedef struct dem_tune_result {
     int64_t sample_particles;
     double seconds;                   /* wall time of the tuning */
     int32_t split_narrow;
-    int32_t reserved[7];
+    int32_t unfused_lom;
+    int32_t reserved[6];
 } dem_tune_result;
 int dem_batch_autotune(const dem_scene *const *scenes, const dem_params *params, const dem_ext *exts,
                        int32_t n_scenes, int32_t device, int64_t sample_particles, int32_t trial_steps,

@@ -189,17 +189,13 @@ __device__ __forceinline__ bool last_warp(uint32_t *ticket) {
 // 2D_LOM.wgsl:80-152 per particle, plus the candidate-list validity check:
 // a particle that moved more than half the skin since the last rebuild asks
 // for a rebuild before this step's Simulation pass.
-__device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
-    // all of the particle's records requested at once (valid for any i < N)
-    uint32_t m = w.meta[i];
-    float4 p = w.pr[i];
-    float4 v = w.vw[i];
-    float4 a = w.ac[i];
-    const float2 b = w.pbuild[i];
-    int s = (int)meta_scene(m);
-    if (!w.act[s]) return;
-    const ScenePar &P = w.par[s];
-    if (p.z == 0.0f) return;                                       // :83
+// 2D_LOM.wgsl:85-152 of one particle from its records (p, v, a, flags m,
+// rebuild position b); `ext`: positions were set externally, so the
+// displacement is the stored dext.  Position, displacement and bucket range
+// go to pr_out/dp_out/rr_out, the velocities and data[4..6] to vw/d4.
+__device__ __forceinline__ void lom_core(const DevWorld &w, const ScenePar &P, int i, uint32_t m, float4 p,
+                                         float4 v, float4 a, float2 b, bool ext, float4 dext, float4 *pr_out,
+                                         float4 *dp_out, int2 *rr_out) {
     const float dT = P.p.dT;
     float ivx = v.x, ivy = v.y, iw = v.z;
     if (m & M_KICK_X) ivx = ivx + (a.x * dT) * 0.5f;               // :88
@@ -207,11 +203,10 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     if (m & M_KICK_R) iw = iw + (a.z * dT) * 0.5f;                 // :90
     w.d4[i] = make_float4(ivx, ivy, iw, 0.0f);                     // :92-94
     float4 d;
-    bool ext = w.cc3[s] != 0;
     if (!ext) {                                                    // :96-99
         d = make_float4(ivx * dT, ivy * dT, iw * dT, 0.0f);
     } else {
-        d = w.dp[i];
+        d = dext;
     }
     float r = p.z;
     float npx = p.x + d.x, npy = p.y + d.y;                        // :103
@@ -255,16 +250,31 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     p.x = p.x + d.x;                                               // :148
     p.y = p.y + d.y;
     p.w = p.w + d.z;                                               // :149
-    w.pr[i] = p;
+    pr_out[i] = p;
     {
         int x0, x1, y0, y1;                                        // 2D_LOM.wgsl:167-178
         ref_range(P, p.x, p.y, p.z, x0, x1, y0, y1);
-        w.rr[i] = pack_range(P, x0, x1, y0, y1);
+        rr_out[i] = pack_range(P, x0, x1, y0, y1);
     }
     w.vw[i] = make_float4(ivx, ivy, iw, v.w);                      // :151-152
-    if (!ext) w.dp[i] = d;
+    if (!ext) dp_out[i] = d;
     const float ex = p.x - b.x, ey = p.y - b.y;
     if (!(ex * ex + ey * ey <= P.disp_limit2)) atomicOr(w.rebuild, 1);
+}
+
+__device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
+    // all of the particle's records requested at once (valid for any i < N)
+    const uint32_t m = w.meta[i];
+    const float4 p = w.pr[i];
+    const float4 v = w.vw[i];
+    const float4 a = w.ac[i];
+    const float2 b = w.pbuild[i];
+    const int s = (int)meta_scene(m);
+    if (!w.act[s]) return;
+    const ScenePar &P = w.par[s];
+    if (p.z == 0.0f) return;                                       // :83
+    const bool ext = w.cc3[s] != 0;
+    lom_core(w, P, i, m, p, v, a, b, ext, ext ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f), w.pr, w.dp, w.rr);
 }
 
 // With w.ticket the kernel's last warp sets the rebuild conditional; without
@@ -757,7 +767,13 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // force loop and store_forces (k_forces) -- the split form trades a second
 // read of the particle's records for two kernels with fewer registers,
 // which pays in dense scenes.
-template <int PART>
+// With FUSE the particle's LOM pass of the next step follows at once
+// (2D_LOM.wgsl:85-152 with this step's accelerations and velocities, as the
+// next step's LOM would read them): its position, displacement and bucket
+// range go to the other buffers (pr_n, dp_n, rr_n), because neighbours still
+// read this step's values.  Particles that do not step on (zero radius, or a
+// served scene at its horizon) copy theirs across.
+template <int PART, bool FUSE>
 __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr) {
     // The particle's own records: the ones needed first are loaded now, the
     // rest (read only after the scene, detection and slot checks resolve)
@@ -773,6 +789,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     if (PART != 1) {
         prefetch_l1(&w.dp[i]);
         prefetch_l1(&w.vw[i]);
+        if (FUSE) prefetch_l1(&w.pbuild[i]);
     }
     const int N = w.N;
     for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
@@ -786,6 +803,11 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     const ScenePar &P = w.par[s];
     if (pa.z == 0.0f) {                                            // :113-118
         if (PART != 1) w.dF[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (FUSE) {
+            w.pr_n[i] = pa;
+            w.dp_n[i] = w.dp[i];
+            w.rr_n[i] = w.rr[i];
+        }
         return;
     }
     const uint32_t before = mask;
@@ -1082,7 +1104,17 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     if (m & M_KICK_X) v.x = v.x + (0.5f * ax) * dT;
     if (m & M_KICK_Y) v.y = v.y + (0.5f * ay) * dT;
     if (m & M_KICK_R) v.z = v.z + (0.5f * al) * dT;
-    w.vw[i] = v;
+    if (!FUSE) {
+        w.vw[i] = v;
+    } else if (w.remaining[s] > 1) {
+        lom_core(w, P, i, m, pa, v, make_float4(ax, ay, al, 0.0f), w.pbuild[i], false,
+                 make_float4(0.0f, 0.0f, 0.0f, 0.0f), w.pr_n, w.dp_n, w.rr_n);
+    } else {
+        w.vw[i] = v;
+        w.pr_n[i] = pa;
+        w.dp_n[i] = w.dp[i];
+        w.rr_n[i] = w.rr[i];
+    }
     // data[0..2]; a particle without contacts writes +0 every step, which the
     // slot word's DF_ZERO bit lets it skip
     const bool zero = (__float_as_uint(acc.d0) | __float_as_uint(acc.d1) | __float_as_uint(acc.d2)) == 0u;
@@ -1123,27 +1155,39 @@ __device__ void end_of_step(const DevWorld &w, int tid) {
     }
 }
 
-__global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w) {
+// the last warp of a Simulation kernel (small worlds): end of step, and for
+// a fused kernel in a graph the next step's rebuild condition
+__device__ __forceinline__ void interact_tail(const DevWorld &w, bool fused, int in_graph,
+                                              cudaGraphConditionalHandle cond) {
+    if (!(w.ticket && last_warp(&w.tickets[1]))) return;
+    end_of_step<32>(w, threadIdx.x & 31);
+    if (fused && in_graph && (threadIdx.x & 31) == 0)
+        cudaGraphSetConditional(cond, *(volatile int32_t *)w.rebuild != 0 ? 1u : 0u);
+}
+
+template <bool FUSE>
+__global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w, int in_graph, cudaGraphConditionalHandle cond) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle<0>(w, i, nr);
-    if (w.ticket && last_warp(&w.tickets[1])) end_of_step<32>(w, threadIdx.x & 31);
+    if (i < w.N) interact_particle<0, FUSE>(w, i, nr);
+    interact_tail(w, FUSE, in_graph, cond);
 }
 
 __global__ void __launch_bounds__(IB, 12) k_narrow(DevWorld w) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle<1>(w, i, nr);
+    if (i < w.N) interact_particle<1, false>(w, i, nr);
 }
 
-__global__ void __launch_bounds__(IB, 8) k_forces(DevWorld w) {
+template <bool FUSE>
+__global__ void __launch_bounds__(IB, 8) k_forces(DevWorld w, int in_graph, cudaGraphConditionalHandle cond) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle<2>(w, i, nr);
-    if (w.ticket && last_warp(&w.tickets[1])) end_of_step<32>(w, threadIdx.x & 31);
+    if (i < w.N) interact_particle<2, FUSE>(w, i, nr);
+    interact_tail(w, FUSE, in_graph, cond);
 }
 
 constexpr int END_THREADS = 256;
@@ -1266,7 +1310,8 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
     if (threadIdx.x == 0) out[15] = keep;
 }
 
-int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs) {
+int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool in_graph,
+                    cudaGraphConditionalHandle cond) {
     (void)block;
     int k = 0;
     if (bigs && w.n_big_slots > 0) {
@@ -1274,17 +1319,26 @@ int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs) {
         k++;
     }
     const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
+    const int ig = in_graph ? 1 : 0;
     if (w.split) {
         k_narrow<<<g, IB, 0, st>>>(w);
-        k_forces<<<g, IB, 0, st>>>(w);
+        if (fuse) k_forces<true><<<g, IB, 0, st>>>(w, ig, cond);
+        else k_forces<false><<<g, IB, 0, st>>>(w, ig, cond);
         k += 2;
     } else {
-        k_interact<<<g, IB, 0, st>>>(w);
+        if (fuse) k_interact<true><<<g, IB, 0, st>>>(w, ig, cond);
+        else k_interact<false><<<g, IB, 0, st>>>(w, ig, cond);
         k++;
     }
-    if (w.ticket) return k;
-    k_end_step<<<1, END_THREADS, 0, st>>>(w);
-    return k + 1;
+    if (!w.ticket) {
+        k_end_step<<<1, END_THREADS, 0, st>>>(w);
+        k++;
+        if (fuse && in_graph) {
+            k_decide<<<1, 32, 0, st>>>(w, cond);
+            k++;
+        }
+    }
+    return k;
 }
 
 // ------------------------------------------------------- free ranges
@@ -1294,6 +1348,7 @@ __global__ void k_mark_free(DevWorld w, int first, int count, int free_scene) {
     int i = first + k;
     w.meta[i] = (uint32_t)free_scene << 16;
     w.pr[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    w.pr_n[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     w.smask[i] = 0u;
     w.nl[2 * (size_t)i] = make_int4(0, 0, 0, 0);
     w.orig[i] = k;
@@ -1311,10 +1366,14 @@ __global__ void k_stage_particles(DevWorld w, RefArrays r, int scene, int base, 
     if (i >= n) return;
     const int g = base + i;
     const float radius = r.radii[i];
-    w.pr[g] = make_float4(r.pos[2 * i], r.pos[2 * i + 1], radius, r.rot[i]);
+    const float4 pr = make_float4(r.pos[2 * i], r.pos[2 * i + 1], radius, r.rot[i]);
+    const float4 dp = make_float4(r.del_pos[2 * i], r.del_pos[2 * i + 1], r.del_rot[i], 0.0f);
+    w.pr[g] = pr;
+    w.pr_n[g] = pr;   // both buffers: a scene that never steps must read the same from either
+    w.dp[g] = dp;
+    w.dp_n[g] = dp;
     w.vw[g] = make_float4(r.vel[2 * i], r.vel[2 * i + 1], r.rot_vel[i], 0.0f);
     w.ac[g] = make_float4(r.acc[2 * i], r.acc[2 * i + 1], r.rot_acc[i], 0.0f);
-    w.dp[g] = make_float4(r.del_pos[2 * i], r.del_pos[2 * i + 1], r.del_rot[i], 0.0f);
     const float *f = r.forces + 6 * (size_t)i;
     w.fx[g] = make_float4(f[0], f[1], f[2], 0.0f);
     float4 d4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), dF = d4;

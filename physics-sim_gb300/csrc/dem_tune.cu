@@ -3,8 +3,9 @@
 // A batch's arithmetic does not depend on the search-cell size, the
 // candidate-list skin (which sets how often the particles are re-sorted by
 // cell), the block size of the particle kernels, the number of steps per
-// captured CUDA graph or whether the Simulation pass runs as one kernel or
-// two; their best values depend on the scenes and the GPU.
+// captured CUDA graph, whether the Simulation pass runs as one kernel or
+// two, or whether it carries the next step's LOM pass; their best values
+// depend on the scenes and the GPU.
 // dem_batch_autotune times short runs of a sample of the batch's scenes with
 // candidate values, one knob at a time (coordinate descent from the library
 // defaults), and returns the fastest combination as dem_ext fields.
@@ -34,6 +35,7 @@ struct Knobs {
     int block = 256;
     int graph_steps = 35;
     int split = 0;
+    int unfused = 0;
 };
 
 // ms per step of the sample with the given knobs: warm run (graph capture,
@@ -47,6 +49,7 @@ int trial(const std::vector<const dem_scene *> &sc, const std::vector<dem_params
         e.block_size = k.block;
         e.reorder_interval = k.graph_steps;
         e.split_narrow = k.split;
+        e.unfused_lom = k.unfused;
         e.plain_launches = 0;
     }
     cudaStream_t st = nullptr;
@@ -178,12 +181,18 @@ int dem_batch_autotune(const dem_scene *const *scenes, const dem_params *params,
         k.split = 1 - best.split;
         if ((rc = try_knobs(k))) return rc;
     }
+    {
+        Knobs k = best;
+        k.unfused = 1 - best.unfused;
+        if ((rc = try_knobs(k))) return rc;
+    }
     std::memset(out, 0, sizeof *out);
     out->search_cell_factor = best.cell_factor;
     out->list_skin = best.skin;
     out->block_size = best.block;
     out->reorder_interval = best.graph_steps;
     out->split_narrow = best.split;
+    out->unfused_lom = best.unfused;
     out->ms_per_step = best_ms;
     out->default_ms_per_step = default_ms;
     out->trials = trials;

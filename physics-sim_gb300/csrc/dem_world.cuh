@@ -113,6 +113,8 @@ struct Pending {
 struct DevWorld {
     int32_t N, C, B, S, M, MP;
     float4 *pr, *vw, *ac, *dp, *fx, *d4, *dF;
+    float4 *pr_n, *dp_n;        // the other position / displacement buffers (written by fused steps)
+    int2 *rr_n;
     uint32_t *meta;
     int32_t *orig;
     int32_t *o2i;               // [N] particle_base + scene-local index -> internal index (kept by the reorder)
@@ -199,7 +201,11 @@ int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int3
 void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStream_t st,
                     const int32_t *gate);
 void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
-int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs);
+// the Simulation pass of one step; with `fuse` also the next step's LOM pass
+// (into the other pr/dp/rr buffers), whose rebuild condition is set on `cond`
+// when in a graph
+int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool in_graph,
+                    cudaGraphConditionalHandle cond);
 void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
                            const int32_t *d_props, int block, cudaStream_t st);
 int scan_tmp_size(int n);

@@ -165,6 +165,10 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
         x.s_thb = dalloc<float>(owned, (size_t)K * N, ok);
     };
     particle_arrays(w);
+    w.pr_n = dalloc<float4>(owned, N, ok);
+    w.dp_n = dalloc<float4>(owned, N, ok);
+    w.rr_n = dalloc<int2>(owned, N, ok);
+    parity = 0;
     w.b_status = dalloc<int32_t>(owned, B, ok);
     w.b_length = dalloc<float>(owned, B, ok);
     w.b_str = dalloc<float2>(owned, B, ok);
@@ -554,6 +558,7 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
     use_graphs = ext.plain_launches == 0;
     split_narrow = ext.split_narrow != 0;
+    fuse_lom = ext.unfused_lom == 0;
     diagnostics = ext.diagnostics != 0;
     sh.assign(S, SceneHost{});
     long long N = 0, C = 0, B = 0, M = 0, MP = 0, TB = 0;
@@ -639,6 +644,7 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
     use_graphs = ext.plain_launches == 0;
     split_narrow = ext.split_narrow != 0;
+    fuse_lom = ext.unfused_lom == 0;
     diagnostics = ext.diagnostics != 0;
     const int S = scenes + 1;  // the last slot owns the unused particles
     free_slot = scenes;
@@ -914,7 +920,11 @@ void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate) {
 
 // One step with plain launches; the rebuild kernels run every step and
 // return at once unless a particle moved beyond its skin.
-void World::enqueue_plain_step() {
+// One step with plain launches; the rebuild kernels run every step and
+// return at once unless a particle moved beyond its skin.  Within a call the
+// first step runs its own LOM pass; every step but the last runs the next
+// step's LOM pass inside its Simulation kernel.
+void World::enqueue_plain_step(bool first, bool last) {
     auto rec = [&](int kind, bool begin) {
         if (!timing) return;
         cudaEvent_t e;
@@ -923,25 +933,40 @@ void World::enqueue_plain_step() {
         timers[kind].ev.push_back(e);
         (void)begin;
     };
-    rec(T_LOM, true);
-    int k = launch_lom(d, block, stream, false, cudaGraphConditionalHandle{});
-    rec(T_LOM, false);
+    int k = 0;
+    if (first || !fuse_lom) {
+        rec(T_LOM, true);
+        k += launch_lom(d, block, stream, false, cudaGraphConditionalHandle{});
+        rec(T_LOM, false);
+    }
     rec(T_BROAD, true);
     enqueue_rebuild(stream, d.rebuild);
     rec(T_BROAD, false);
     rec(T_INTERACT, true);
-    k += launch_interact(d, block, stream, has_bigs);
+    const bool fuse = fuse_lom && !last;
+    k += launch_interact(d, block, stream, has_bigs, fuse, false, cudaGraphConditionalHandle{});
     rec(T_INTERACT, false);
+    if (fuse) flip();
     launches += k + rebuild_kernels;
     host_step++;
 }
 
 void World::drop_graph() {
-    if (graph) cudaGraphExecDestroy(graph);
-    if (graph1) cudaGraphExecDestroy(graph1);
-    graph = nullptr;
-    graph1 = nullptr;
-    graph_R = 0;
+    for (int p = 0; p < 2; ++p) {
+        if (graph[p]) cudaGraphExecDestroy(graph[p]);
+        if (graph1[p]) cudaGraphExecDestroy(graph1[p]);
+        graph[p] = graph1[p] = nullptr;
+        graph_R[p] = 0;
+    }
+}
+
+// the current and the other pr/dp/rr buffers trade places (a fused step
+// wrote the next step's values into the other ones)
+void World::flip() {
+    std::swap(d.pr, d.pr_n);
+    std::swap(d.dp, d.dp_n);
+    std::swap(d.rr, d.rr_n);
+    parity ^= 1;
 }
 
 #define CKG(call)                                                                         \
@@ -960,8 +985,19 @@ void World::drop_graph() {
 // whose body is the rebuild (its condition is set on the device by the LOM
 // kernel's last warp or by k_decide), and the Simulation kernel (followed by
 // k_end_step in large worlds).
+// Capture R steps as one graph: the first step's LOM kernel, then per step a
+// conditional node whose body is the rebuild (its condition set on the device
+// by the LOM pass before it) and the Simulation kernel, fused with the next
+// step's LOM pass for all but the last step (with fuse_lom; otherwise every
+// step has its own LOM kernel).  The buffer swaps of the fused
+// steps are applied to the captured launches and undone afterwards: they take
+// effect when the graph runs.
 int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
     if (!side) CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    const int parity0 = parity;
+    auto restore = [&]() {
+        while (parity != parity0) flip();
+    };
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int kernels = 0;
     // a launch that fails during capture invalidates it: check the capture
@@ -969,38 +1005,59 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
     auto active = [&](cudaStreamCaptureStatus cs, cudaGraph_t g) {
         return cs == cudaStreamCaptureStatusActive && g != nullptr;
     };
+#define CKR(call)                  \
+    do {                           \
+        cudaError_t e2_ = (call);  \
+        if (e2_ != cudaSuccess) {  \
+            restore();             \
+            CKG(e2_);              \
+        }                          \
+    } while (0)
+    cudaGraphConditionalHandle h{};
     for (int k = 0; k < R; ++k) {
         cudaStreamCaptureStatus cs;
         cudaGraph_t g = nullptr;
-        CKG(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
-        if (!active(cs, g)) CKG(cudaErrorStreamCaptureInvalidated);
-        cudaGraphConditionalHandle h;
-        CKG(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
-        kernels += launch_lom(d, block, stream, true, h);
-        CKG(cudaGetLastError());
+        if (k == 0 || !fuse_lom) {
+            CKR(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+            if (!active(cs, g)) CKR(cudaErrorStreamCaptureInvalidated);
+            CKR(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+            kernels += launch_lom(d, block, stream, true, h);
+            CKR(cudaGetLastError());
+        }
         const cudaGraphNode_t *deps = nullptr;
         size_t ndeps = 0;
-        CKG(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &ndeps));
-        if (!active(cs, g)) CKG(cudaErrorStreamCaptureInvalidated);
+        CKR(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+        if (!active(cs, g)) CKR(cudaErrorStreamCaptureInvalidated);
         cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
         np.type = cudaGraphNodeTypeConditional;
         np.conditional.handle = h;
         np.conditional.type = cudaGraphCondTypeIf;
         np.conditional.size = 1;
         cudaGraphNode_t node;
-        CKG(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np));
+        CKR(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np));
         cudaGraph_t body = np.conditional.phGraph_out[0];
-        CKG(cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        CKR(cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         enqueue_rebuild(side, d.rebuild);
         const cudaError_t le = cudaGetLastError();
         cudaGraph_t body_out = nullptr;
         const cudaError_t ee = cudaStreamEndCapture(side, &body_out);
-        CKG(le);
-        CKG(ee);
-        CKG(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-        kernels += launch_interact(d, block, stream, has_bigs);
-        CKG(cudaGetLastError());
+        CKR(le);
+        CKR(ee);
+        CKR(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        if (fuse_lom && k + 1 < R) {
+            cudaGraphConditionalHandle hn{};
+            CKR(cudaGraphConditionalHandleCreate(&hn, g, 0, cudaGraphCondAssignDefault));
+            kernels += launch_interact(d, block, stream, has_bigs, true, true, hn);
+            CKR(cudaGetLastError());
+            flip();
+            h = hn;
+        } else {
+            kernels += launch_interact(d, block, stream, has_bigs, false, true, cudaGraphConditionalHandle{});
+            CKR(cudaGetLastError());
+        }
     }
+#undef CKR
+    restore();
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(stream, &g);
     if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -1017,30 +1074,35 @@ int World::step(int n_steps) {
     if (n_steps < 0) return fail(DEM_E_INVALID, "n_steps < 0");
     int k = 0;
     if (use_graphs && !timing && n_steps > 0) {
-        if (n_steps >= graph_steps && (!graph || graph_R != graph_steps)) {
-            if (graph) cudaGraphExecDestroy(graph);
-            graph = nullptr;
-            int rc = capture_graph(graph_steps, &graph, &graph_kernels);
-            if (rc) return rc;
-            graph_R = graph_steps;
-        }
-        while (graph && n_steps - k >= graph_steps) {
-            CK(cudaGraphLaunch(graph, stream));
-            launches += graph_kernels;
+        while (n_steps - k >= graph_steps) {
+            const int p = parity;
+            if (!graph[p] || graph_R[p] != graph_steps) {
+                if (graph[p]) cudaGraphExecDestroy(graph[p]);
+                graph[p] = nullptr;
+                int rc = capture_graph(graph_steps, &graph[p], &graph_kernels[p]);
+                if (rc) return rc;
+                graph_R[p] = graph_steps;
+            }
+            CK(cudaGraphLaunch(graph[p], stream));
+            if (fuse_lom)
+                for (int f = 0; f + 1 < graph_steps; ++f) flip();
+            launches += graph_kernels[p];
             host_step += graph_steps;
             k += graph_steps;
         }
-        if (k < n_steps && !graph1) {
-            int rc = capture_graph(1, &graph1, &graph1_kernels);
-            if (rc) return rc;
-        }
         for (; k < n_steps; ++k) {
-            CK(cudaGraphLaunch(graph1, stream));
-            launches += graph1_kernels;
+            const int p = parity;
+            if (!graph1[p]) {
+                int rc = capture_graph(1, &graph1[p], &graph1_kernels[p]);
+                if (rc) return rc;
+            }
+            CK(cudaGraphLaunch(graph1[p], stream));
+            launches += graph1_kernels[p];
             host_step += 1;
         }
     }
-    for (; k < n_steps; ++k) enqueue_plain_step();
+    const int k0 = k;
+    for (; k < n_steps; ++k) enqueue_plain_step(k == k0, k + 1 == n_steps);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     return DEM_OK;

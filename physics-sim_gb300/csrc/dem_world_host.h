@@ -105,6 +105,7 @@ class World {
     DevWorld d{};
     bool use_graphs = true;
     bool split_narrow = false;     // Simulation pass as two kernels (dem_ext::split_narrow)
+    bool fuse_lom = true;          // next step's LOM pass inside the Simulation kernel (dem_ext::unfused_lom)
     bool has_bigs = false;         // some scene has large particles: k_big_narrow runs each step
     long long launches = 0;
     // kernel timing (debug): event pairs per kernel kind, summed on demand
@@ -131,7 +132,7 @@ class World {
     int push_det();
     int stage_scene(int s, const dem_scene *scene);
     int force_rebuild();
-    void enqueue_plain_step();
+    void enqueue_plain_step(bool first, bool last);
     void enqueue_rebuild(cudaStream_t st, const int32_t *gate);
     int capture_graph(int R, cudaGraphExec_t *out, int *kernels);
     void drop_graph();
@@ -143,11 +144,15 @@ class World {
     long long ref_cap = 0;
     int32_t *ref_err = nullptr;
     int ensure_ref(long long n);
-    cudaGraphExec_t graph = nullptr;   // graph_steps steps
-    cudaGraphExec_t graph1 = nullptr;  // one step, for remainders
-    int graph_R = 0;
-    int graph_kernels = 0;
-    int graph1_kernels = 0;
+    // captured graphs, one per buffer parity at their start (a graph of R
+    // steps swaps the pr/dp/rr buffers R - 1 times)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // graph_steps steps
+    cudaGraphExec_t graph1[2] = {nullptr, nullptr};  // one step, for remainders
+    int graph_R[2] = {0, 0};
+    int graph_kernels[2] = {0, 0};
+    int graph1_kernels[2] = {0, 0};
+    int parity = 0;                    // which pr/dp/rr buffers are current
+    void flip();
     int rebuild_kernels = 0;
 };
 

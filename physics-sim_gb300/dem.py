@@ -61,7 +61,8 @@ class Ext(C.Structure):
                 ("diagnostics", C.c_int32), ("reorder_interval", C.c_int32),
                 ("block_size", C.c_int32), ("search_cell_factor", C.c_float),
                 ("event_capacity", C.c_int32), ("list_skin", C.c_float),
-                ("plain_launches", C.c_int32), ("split_narrow", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("plain_launches", C.c_int32), ("split_narrow", C.c_int32), ("unfused_lom", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
 
 
 class Scene(C.Structure):
@@ -102,7 +103,7 @@ class TuneResult(C.Structure):
                 ("reorder_interval", C.c_int32), ("ms_per_step", C.c_double),
                 ("default_ms_per_step", C.c_double), ("trials", C.c_int32), ("sample_scenes", C.c_int32),
                 ("sample_particles", C.c_int64), ("seconds", C.c_double), ("split_narrow", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("unfused_lom", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 EVENT_FIX, EVENT_DROP, EVENT_RELEASE = 1, 2, 3
@@ -244,7 +245,7 @@ def make_params(d):
 
 def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnostics=True,
              reorder_interval=0, block_size=0, search_cell_factor=0.0, event_capacity=0,
-             list_skin=0.0, plain_launches=False, split_narrow=0, keep=None):
+             list_skin=0.0, plain_launches=False, split_narrow=0, unfused_lom=0, keep=None):
     e = Ext()
     lib().dem_ext_defaults(C.byref(e))
     e.use_f64 = 1 if use_f64 else 0
@@ -257,6 +258,7 @@ def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnos
     e.list_skin = list_skin
     e.plain_launches = 1 if plain_launches else 0
     e.split_narrow = 1 if split_narrow else 0
+    e.unfused_lom = 1 if unfused_lom else 0
     for attr, arr in (("bond_normal_strength", bond_sn), ("bond_shear_strength", bond_ss)):
         if arr is not None:
             a = np.ascontiguousarray(arr, dtype=np.float32)
@@ -512,7 +514,7 @@ def autotune(items, *, device=-1, sample_particles=0, trial_steps=0, **world_kw)
         raise DemError(rc, (L.dem_tune_last_error() or b"").decode())
     chosen = {"search_cell_factor": float(res.search_cell_factor), "list_skin": float(res.list_skin),
               "block_size": int(res.block_size), "reorder_interval": int(res.reorder_interval),
-              "split_narrow": int(res.split_narrow)}
+              "split_narrow": int(res.split_narrow), "unfused_lom": int(res.unfused_lom)}
     info = {"ms_per_step": res.ms_per_step, "default_ms_per_step": res.default_ms_per_step,
             "trials": int(res.trials), "sample_scenes": int(res.sample_scenes),
             "sample_particles": int(res.sample_particles), "seconds": res.seconds}

@@ -39,7 +39,7 @@ def _run(items, steps, **kw):
 
 @pytest.mark.parametrize("knobs", [
     dict(search_cell_factor=0.68, list_skin=0.45, block_size=128, reorder_interval=21, split_narrow=1),
-    dict(search_cell_factor=1.36, list_skin=0.1, block_size=512, reorder_interval=70),
+    dict(search_cell_factor=1.36, list_skin=0.1, block_size=512, reorder_interval=70, unfused_lom=1),
 ])
 def test_knobs_do_not_change_results(knobs):
     items = _items()
@@ -58,7 +58,7 @@ def test_autotune_picks_listed_values_and_keeps_results():
     assert chosen["list_skin"] in (pytest.approx(0.1), pytest.approx(0.2), pytest.approx(0.3), pytest.approx(0.45))
     assert chosen["block_size"] in (128, 256, 512)
     assert chosen["reorder_interval"] in (21, 35, 70)
-    assert chosen["split_narrow"] in (0, 1)
+    assert chosen["split_narrow"] in (0, 1) and chosen["unfused_lom"] in (0, 1)
     assert info["trials"] >= 10 and info["ms_per_step"] <= info["default_ms_per_step"]
     ref, ref_ev = _run(items, 105)
     got, got_ev = _run(items, 105, **chosen)
