@@ -601,17 +601,15 @@ def run_ours_batch(args):
     h2d = sum(scene_bytes(x) for x in states)
     outs = [batch.download(k) for k in range(len(items))]
     t0 = time.perf_counter()
-    for k in range(len(items)):
-        batch.upload(k, states[k])
+    batch.upload_many(list(enumerate(states)))
     batch.step(F)
-    for k in range(len(items)):
-        batch.download(k, outs[k])
+    batch.download_many(list(enumerate(outs)))
     barrier()
     e2e_s = time.perf_counter() - t0
     del outs
     e2e = {"value": ntot * F * ws / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": h2d,
-           "note": "dem_batch_upload of all scenes + dem_batch_step(frame) + dem_batch_download of all scenes"}
+           "note": "dem_batch_upload_many of all scenes + dem_batch_step(frame) + dem_batch_download_many of all scenes"}
 
     base = None
     if rank == 0 and ws == 1:

@@ -243,6 +243,11 @@ int dem_batch_step(dem_batch *b, int32_t n_steps);
 int dem_batch_synchronize(dem_batch *b);
 int dem_batch_download(dem_batch *b, int32_t scene, dem_scene *out);
 int dem_batch_upload(dem_batch *b, int32_t scene, const dem_scene *in);
+/* The same for n scenes at once (scene indices idx[n]): one synchronisation
+ * for all instead of several per scene.  upload_many writes nothing unless
+ * every scene passes its checks. */
+int dem_batch_upload_many(dem_batch *b, int32_t n, const int32_t *idx, const dem_scene *const *in);
+int dem_batch_download_many(dem_batch *b, int32_t n, const int32_t *idx, dem_scene *const *out);
 int dem_batch_set_params(dem_batch *b, int32_t scene, const dem_params *params);
 int dem_batch_set_properties(dem_batch *b, int32_t scene, int32_t *selections,
                              const int32_t props[DEM_PROPS_WORDS]);

@@ -111,6 +111,16 @@ int dem_batch_upload(dem_batch *b, int32_t scene, const dem_scene *in) {
     return brc(b, b->world.upload_scene(scene, in));
 }
 
+int dem_batch_upload_many(dem_batch *b, int32_t n, const int32_t *idx, const dem_scene *const *in) {
+    BATCH_GUARD(b);
+    return brc(b, b->world.upload_many(idx, in, n));
+}
+
+int dem_batch_download_many(dem_batch *b, int32_t n, const int32_t *idx, dem_scene *const *out) {
+    BATCH_GUARD(b);
+    return brc(b, b->world.download_many(idx, out, n));
+}
+
 int dem_batch_set_params(dem_batch *b, int32_t scene, const dem_params *p) {
     BATCH_GUARD(b);
     if (!p) return bset(b, DEM_E_INVALID, "params is NULL");

@@ -4,6 +4,7 @@
 #include <cstring>
 #include <climits>
 #include <limits>
+#include <thread>
 
 #include "dem_world_host.h"
 
@@ -449,46 +450,73 @@ int World::push_active(int s, bool on, long long steps) {
 }
 
 // ---- staging: reference layout -> internal layout --------------------------
-int World::stage_scene(int s, const dem_scene *sc) {
+// the staging arrays of a scene whose particles start at `off` in the block
+RefArrays World::ref_at(long long off) const {
+    RefArrays r = ref;
+    r.pos += 2 * off;
+    r.radii += off;
+    r.vel += 2 * off;
+    r.acc += 2 * off;
+    r.rot += off;
+    r.rot_vel += off;
+    r.rot_acc += off;
+    r.forces += 6 * off;
+    r.del_pos += 2 * off;
+    r.del_rot += off;
+    r.data += 7 * off;
+    r.fixity += 6 * off;
+    r.contacts += 84 * off;
+    r.material_pointers += off;
+    return r;
+}
+
+// Staging of a scene, in three phases so that many scenes can share one
+// synchronisation: copy the reference-layout arrays whole into the staging
+// block at `off` and queue their check (err word at *err); then, once the
+// checks passed, convert on the device and upload bonds and materials.
+int World::stage_copy(int s, const dem_scene *sc, long long off, int32_t *err) {
+    SceneHost &h = sh[s];
+    const int n = h.n;
+    h.materials.assign(sc->materials, sc->materials + 6 * (size_t)h.n_mat);
+    if (n <= 0) return DEM_OK;
+    const RefArrays r = ref_at(off);
+    auto up = [&](void *dst, const void *src, size_t words) {
+        return cudaMemcpyAsync(dst, src, words * 4, cudaMemcpyHostToDevice, stream);
+    };
+    const size_t un = (size_t)n;
+    CK(up(r.pos, sc->pos, 2 * un));
+    CK(up(r.radii, sc->radii, un));
+    CK(up(r.vel, sc->vel, 2 * un));
+    CK(up(r.acc, sc->acc, 2 * un));
+    CK(up(r.rot, sc->rot, un));
+    CK(up(r.rot_vel, sc->rot_vel, un));
+    CK(up(r.rot_acc, sc->rot_acc, un));
+    CK(up(r.forces, sc->forces, 6 * un));
+    CK(up(r.fixity, sc->fixity, 6 * un));
+    CK(up(r.del_pos, sc->del_pos, 2 * un));
+    CK(up(r.del_rot, sc->del_rot, un));
+    CK(up(r.contacts, sc->contacts, 84 * un));
+    CK(up(r.material_pointers, sc->material_pointers, un));
+    if (sc->data) CK(up(r.data, sc->data, 7 * un));
+    launch_stage_check(r, n, h.n_bonds, h.n_mat, err, stream);
+    return DEM_OK;
+}
+
+int World::stage_error(int32_t e) {
+    if (e & 1) return fail(DEM_E_INVALID, "material pointer out of range");
+    if (e & 2) return fail(DEM_E_INVALID, "contact bonded index beyond n_bonds");
+    if (e & 4) return fail(DEM_E_INVALID, "contact partner out of range");
+    if (e & 8) return fail(DEM_E_INVALID, "contact record's a differs from its owner");
+    return DEM_OK;
+}
+
+int World::stage_commit(int s, const dem_scene *sc, long long off) {
     SceneHost &h = sh[s];
     const int n = h.n, base = h.particle_base;
-    h.materials.assign(sc->materials, sc->materials + 6 * (size_t)h.n_mat);
-    // the reference-layout arrays go to the device whole; the conversion to
-    // the internal layout (float4 records, slot rows, flags) runs there
     if (n > 0) {
-        int rc = ensure_ref(n);
-        if (rc) return rc;
-        auto up = [&](void *dst, const void *src, size_t words) {
-            return cudaMemcpyAsync(dst, src, words * 4, cudaMemcpyHostToDevice, stream);
-        };
-        const size_t un = (size_t)n;
-        CK(up(ref.pos, sc->pos, 2 * un));
-        CK(up(ref.radii, sc->radii, un));
-        CK(up(ref.vel, sc->vel, 2 * un));
-        CK(up(ref.acc, sc->acc, 2 * un));
-        CK(up(ref.rot, sc->rot, un));
-        CK(up(ref.rot_vel, sc->rot_vel, un));
-        CK(up(ref.rot_acc, sc->rot_acc, un));
-        CK(up(ref.forces, sc->forces, 6 * un));
-        CK(up(ref.fixity, sc->fixity, 6 * un));
-        CK(up(ref.del_pos, sc->del_pos, 2 * un));
-        CK(up(ref.del_rot, sc->del_rot, un));
-        CK(up(ref.contacts, sc->contacts, 84 * un));
-        CK(up(ref.material_pointers, sc->material_pointers, un));
-        if (sc->data) CK(up(ref.data, sc->data, 7 * un));
-        CK(cudaMemsetAsync(ref_err, 0, 4, stream));
-        launch_stage_check(ref, n, h.n_bonds, h.n_mat, ref_err, stream);
-        int32_t e = 0;
-        CK(cudaMemcpyAsync(&e, ref_err, 4, cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
-        if (e & 1) return fail(DEM_E_INVALID, "material pointer out of range");
-        if (e & 2) return fail(DEM_E_INVALID, "contact bonded index beyond n_bonds");
-        if (e & 4) return fail(DEM_E_INVALID, "contact partner out of range");
-        if (e & 8) return fail(DEM_E_INVALID, "contact record's a differs from its owner");
-        launch_stage_in(d, ref, s, base, n, h.n_mat, h.r_big, sc->data ? 1 : 0, ref_err, stream);
+        launch_stage_in(d, ref_at(off), s, base, n, h.n_mat, h.r_big, sc->data ? 1 : 0, ref_err, stream);
         CK(cudaGetLastError());
     }
-    // bonds
     const int nb = h.n_bonds;
     if (nb > 0) {
         std::vector<int32_t> st(nb);
@@ -507,8 +535,24 @@ int World::stage_scene(int s, const dem_scene *sc) {
         CK(cudaMemcpyAsync(d.b_str + h.bond_base, str.data(), 8 * (size_t)nb, cudaMemcpyHostToDevice, stream));
         CK(cudaStreamSynchronize(stream));
     }
-    CK(cudaStreamSynchronize(stream));
     return push_materials(s);
+}
+
+int World::stage_scene(int s, const dem_scene *sc) {
+    const int n = sh[s].n;
+    if (n > 0) {
+        int rc = ensure_ref(n);
+        if (rc) return rc;
+    }
+    CK(cudaMemsetAsync(ref_err, 0, 4, stream));
+    int rc = stage_copy(s, sc, 0, ref_err);
+    if (rc) return rc;
+    int32_t e = 0;
+    CK(cudaMemcpyAsync(&e, ref_err, 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    rc = stage_error(e);
+    if (rc) return rc;
+    return stage_commit(s, sc, 0);
 }
 
 // material records and the material-pair stiffness table of one scene:
@@ -778,18 +822,12 @@ int World::retire(int s) {
     return force_rebuild();
 }
 
-int World::upload_scene(int s, const dem_scene *sc) {
-    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+// A re-uploaded scene keeps its cell budget and large-particle records and
+// adopts the new geometry inside them.
+int World::adopt_layout(int s, const SceneHost &probe) {
     SceneHost &h = sh[s];
-    if (!sc || sc->n_particles != h.n || sc->n_bonds != h.n_bonds || sc->n_materials != h.n_mat)
-        return fail(DEM_E_INVALID, "upload must keep particle, bond and material counts");
-    SceneHost probe = h;
-    int rc = compute_layout(probe, sc);
-    if (rc) return rc;
     if (probe.n_cells > h.n_cells)
         return fail(DEM_E_UNSUPPORTED, "uploaded scene needs a larger search grid; create a new context");
-    // keep the cell budget; adopt the new geometry inside it
-    probe.n_cells = h.n_cells;
     if (probe.n_big > h.big_cap)
         return fail(DEM_E_UNSUPPORTED, "uploaded scene has more large particles; create a new context");
     h.r_max = probe.r_max;
@@ -802,7 +840,96 @@ int World::upload_scene(int s, const dem_scene *sc) {
     h.par.g_y0 = probe.par.g_y0;
     h.par.g_w = probe.par.g_w;
     h.par.g_h = probe.par.g_h;
-    CK(cudaStreamSynchronize(stream));
+    return DEM_OK;
+}
+
+// Many scenes at once (dem_batch_upload_many): the layouts are derived on
+// host threads, every scene's arrays are copied and checked before one
+// synchronisation, then converted; one rebuild follows.  Nothing is written
+// to any scene unless every scene passes its checks.
+int World::upload_many(const int32_t *idx, const dem_scene *const *scs, int count) {
+    if (count <= 0) return DEM_OK;
+    if (!idx || !scs) return fail(DEM_E_INVALID, "scene index/pointer arrays are NULL");
+    std::vector<SceneHost> probes(count);
+    std::vector<int> rcs(count, DEM_OK);
+    std::vector<std::string> errs(count);
+    long long total = 0;
+    for (int k = 0; k < count; ++k) {
+        const int s = idx[k];
+        if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+        const SceneHost &h = sh[s];
+        const dem_scene *sc = scs[k];
+        if (!sc || sc->n_particles != h.n || sc->n_bonds != h.n_bonds || sc->n_materials != h.n_mat)
+            return fail(DEM_E_INVALID, "upload must keep particle, bond and material counts (scene " +
+                                           std::to_string(s) + ")");
+        probes[k] = h;
+        total += h.n;
+    }
+    {
+        // compute_layout touches only its probe; derive them in parallel
+        const int T = std::max(1, std::min<int>(count, (int)std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        std::vector<World> scratch(T);
+        for (int t = 0; t < T; ++t)
+            pool.emplace_back([&, t]() {
+                scratch[t].skin_factor = skin_factor;
+                for (int k = t; k < count; k += T) {
+                    rcs[k] = scratch[t].compute_layout(probes[k], scs[k]);
+                    if (rcs[k]) errs[k] = scratch[t].err;
+                }
+            });
+        for (auto &th : pool) th.join();
+    }
+    for (int k = 0; k < count; ++k)
+        if (rcs[k]) return fail(rcs[k], errs[k] + " (scene " + std::to_string(idx[k]) + ")");
+    for (int k = 0; k < count; ++k) {
+        int rc = adopt_layout(idx[k], probes[k]);
+        if (rc) return rc;
+    }
+    int rc = ensure_ref(total);
+    if (rc) return rc;
+    int32_t *d_err = nullptr;
+    CK(cudaMalloc(&d_err, sizeof(int32_t) * count));
+    std::vector<long long> off(count);
+    std::vector<int32_t> e(count, 0);
+    cudaError_t ce = cudaMemsetAsync(d_err, 0, sizeof(int32_t) * count, stream);
+    long long o = 0;
+    for (int k = 0; k < count && ce == cudaSuccess && rc == DEM_OK; ++k) {
+        off[k] = o;
+        o += sh[idx[k]].n;
+        rc = stage_copy(idx[k], scs[k], off[k], d_err + k);
+    }
+    if (ce == cudaSuccess && rc == DEM_OK)
+        ce = cudaMemcpyAsync(e.data(), d_err, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+    cudaFree(d_err);
+    if (ce != cudaSuccess) return fail(DEM_E_CUDA, cudaGetErrorString(ce));
+    if (rc) return rc;
+    for (int k = 0; k < count; ++k)
+        if (e[k]) {
+            rc = stage_error(e[k]);
+            err += " (scene " + std::to_string(idx[k]) + ")";
+            return rc;
+        }
+    for (int k = 0; k < count; ++k) {
+        rc = stage_commit(idx[k], scs[k], off[k]);
+        if (rc) return rc;
+        rc = push_par(idx[k]);
+        if (rc) return rc;
+    }
+    return force_rebuild();
+}
+
+int World::upload_scene(int s, const dem_scene *sc) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    SceneHost &h = sh[s];
+    if (!sc || sc->n_particles != h.n || sc->n_bonds != h.n_bonds || sc->n_materials != h.n_mat)
+        return fail(DEM_E_INVALID, "upload must keep particle, bond and material counts");
+    SceneHost probe = h;
+    int rc = compute_layout(probe, sc);
+    if (rc) return rc;
+    rc = adopt_layout(s, probe);
+    if (rc) return rc;
     rc = stage_scene(s, sc);
     if (rc) return rc;
     rc = push_par(s);
@@ -1116,54 +1243,43 @@ int World::sync() {
     return DEM_OK;
 }
 
-int World::download_scene(int s, dem_scene *out) {
-    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
-    if (!out) return fail(DEM_E_INVALID, "out is NULL");
+// the reference layouts of scene s into the staging block at `off`
+// (err: its check word)
+void World::unstage_launch(int s, long long off, int32_t *err) {
+    const SceneHost &h = sh[s];
+    if (h.n > 0) launch_stage_out(d, ref_at(off), h.particle_base, h.n, err, stream);
+}
+
+// staged scene -> caller's arrays; bst/blen hold the scene's bond status and
+// length words
+int World::unstage_copy(int s, long long off, dem_scene *out, const int32_t *bst, const float *blen) {
     const SceneHost &h = sh[s];
     const int n = h.n, base = h.particle_base;
-    if (out->n_particles != n) return fail(DEM_E_INVALID, "out->n_particles must match the scene");
-    CK(cudaStreamSynchronize(stream));
-    std::vector<int32_t> bst(h.n_bonds);
     if (n > 0) {
-        // the device writes the reference layouts (scene-local order), then
-        // each array comes back in one transfer straight into the caller's
-        int rc = ensure_ref(n);
-        if (rc) return rc;
-        CK(cudaMemsetAsync(ref_err, 0, 4, stream));
-        launch_stage_out(d, ref, base, n, ref_err, stream);
-        int32_t e = 0;
-        CK(cudaMemcpyAsync(&e, ref_err, 4, cudaMemcpyDeviceToHost, stream));
+        const RefArrays r = ref_at(off);
         auto dn = [&](void *dst, const void *src, size_t words) -> cudaError_t {
             if (!dst) return cudaSuccess;
             return cudaMemcpyAsync(dst, src, words * 4, cudaMemcpyDeviceToHost, stream);
         };
         const size_t un = (size_t)n;
-        CK(dn(out->pos, ref.pos, 2 * un));
-        CK(dn(out->radii, ref.radii, un));
-        CK(dn(out->rot, ref.rot, un));
-        CK(dn(out->vel, ref.vel, 2 * un));
-        CK(dn(out->rot_vel, ref.rot_vel, un));
-        CK(dn(out->acc, ref.acc, 2 * un));
-        CK(dn(out->rot_acc, ref.rot_acc, un));
-        CK(dn(out->del_pos, ref.del_pos, 2 * un));
-        CK(dn(out->del_rot, ref.del_rot, un));
-        CK(dn(out->data, ref.data, 7 * un));
-        CK(dn(out->contacts, ref.contacts, 84 * un));
+        CK(dn(out->pos, r.pos, 2 * un));
+        CK(dn(out->radii, r.radii, un));
+        CK(dn(out->rot, r.rot, un));
+        CK(dn(out->vel, r.vel, 2 * un));
+        CK(dn(out->rot_vel, r.rot_vel, un));
+        CK(dn(out->acc, r.acc, 2 * un));
+        CK(dn(out->rot_acc, r.rot_acc, un));
+        CK(dn(out->del_pos, r.del_pos, 2 * un));
+        CK(dn(out->del_rot, r.del_rot, un));
+        CK(dn(out->data, r.data, 7 * un));
+        CK(dn(out->contacts, r.contacts, 84 * un));
         CK(dn(out->fixity, d.fix_ref + 6 * (size_t)base, 6 * un));
         CK(dn(out->forces, d.force_ref + 6 * (size_t)base, 6 * un));
         CK(dn(out->material_pointers, d.matp_ref + base, un));
-        if (h.n_bonds > 0) CK(dn(bst.data(), d.b_status + h.bond_base, (size_t)h.n_bonds));
-        CK(cudaStreamSynchronize(stream));
-        if (e & 16) return fail(DEM_E_STATE, "internal particle map is corrupt");
-        if (e & 32) return fail(DEM_E_STATE, "contact partner outside its scene");
-    } else if (h.n_bonds > 0) {
-        CK(cudaMemcpy(bst.data(), d.b_status + h.bond_base, h.n_bonds * 4, cudaMemcpyDeviceToHost));
     }
     if (out->materials && out->n_materials == h.n_mat)
         std::memcpy(out->materials, h.materials.data(), h.materials.size() * 4);
     if (out->bonds && out->n_bonds == h.n_bonds) {
-        std::vector<float> blen(h.n_bonds);
-        if (h.n_bonds > 0) CK(cudaMemcpy(blen.data(), d.b_length + h.bond_base, h.n_bonds * 4, cudaMemcpyDeviceToHost));
         for (int k = 0; k < h.n_bonds; ++k) {
             out->bonds[3 * k] = bst[k];
             out->bonds[3 * k + 1] = h.bond_angle[k];
@@ -1172,6 +1288,85 @@ int World::download_scene(int s, dem_scene *out) {
     }
     control(s, out->coll_cont);
     out->grid = h.grid;
+    return DEM_OK;
+}
+
+int World::unstage_error(int32_t e) {
+    if (e & 16) return fail(DEM_E_STATE, "internal particle map is corrupt");
+    if (e & 32) return fail(DEM_E_STATE, "contact partner outside its scene");
+    return DEM_OK;
+}
+
+int World::download_scene(int s, dem_scene *out) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    if (!out) return fail(DEM_E_INVALID, "out is NULL");
+    const SceneHost &h = sh[s];
+    if (out->n_particles != h.n) return fail(DEM_E_INVALID, "out->n_particles must match the scene");
+    int rc = ensure_ref(h.n);
+    if (rc) return rc;
+    std::vector<int32_t> bst(h.n_bonds);
+    std::vector<float> blen(h.n_bonds);
+    CK(cudaMemsetAsync(ref_err, 0, 4, stream));
+    unstage_launch(s, 0, ref_err);
+    int32_t e = 0;
+    CK(cudaMemcpyAsync(&e, ref_err, 4, cudaMemcpyDeviceToHost, stream));
+    if (h.n_bonds > 0) {
+        CK(cudaMemcpyAsync(bst.data(), d.b_status + h.bond_base, 4 * (size_t)h.n_bonds, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(blen.data(), d.b_length + h.bond_base, 4 * (size_t)h.n_bonds, cudaMemcpyDeviceToHost, stream));
+    }
+    CK(cudaStreamSynchronize(stream));
+    rc = unstage_error(e);
+    if (rc) return rc;
+    rc = unstage_copy(s, 0, out, bst.data(), blen.data());
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(stream));
+    return DEM_OK;
+}
+
+// Many scenes at once (dem_batch_download_many): every scene is converted
+// into the staging block before one synchronisation, then copied out.
+int World::download_many(const int32_t *idx, dem_scene *const *outs, int count) {
+    if (count <= 0) return DEM_OK;
+    if (!idx || !outs) return fail(DEM_E_INVALID, "scene index/pointer arrays are NULL");
+    long long total = 0;
+    for (int k = 0; k < count; ++k) {
+        const int s = idx[k];
+        if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+        if (!outs[k] || outs[k]->n_particles != sh[s].n)
+            return fail(DEM_E_INVALID, "out->n_particles must match the scene (scene " + std::to_string(s) + ")");
+        total += sh[s].n;
+    }
+    int rc = ensure_ref(total);
+    if (rc) return rc;
+    int32_t *d_err = nullptr;
+    CK(cudaMalloc(&d_err, sizeof(int32_t) * count));
+    std::vector<long long> off(count);
+    std::vector<int32_t> e(count, 0);
+    std::vector<int32_t> bst(d.B > 0 ? d.B : 1);
+    std::vector<float> blen(d.B > 0 ? d.B : 1);
+    cudaError_t ce = cudaMemsetAsync(d_err, 0, sizeof(int32_t) * count, stream);
+    long long o = 0;
+    for (int k = 0; k < count; ++k) {
+        off[k] = o;
+        o += sh[idx[k]].n;
+        unstage_launch(idx[k], off[k], d_err + k);
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(e.data(), d_err, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, stream);
+    if (ce == cudaSuccess && d.B > 0)
+        ce = cudaMemcpyAsync(bst.data(), d.b_status, 4 * (size_t)d.B, cudaMemcpyDeviceToHost, stream);
+    if (ce == cudaSuccess && d.B > 0)
+        ce = cudaMemcpyAsync(blen.data(), d.b_length, 4 * (size_t)d.B, cudaMemcpyDeviceToHost, stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+    cudaFree(d_err);
+    if (ce != cudaSuccess) return fail(DEM_E_CUDA, cudaGetErrorString(ce));
+    for (int k = 0; k < count; ++k)
+        if (e[k]) return unstage_error(e[k]);
+    for (int k = 0; k < count; ++k) {
+        const SceneHost &h = sh[idx[k]];
+        rc = unstage_copy(idx[k], off[k], outs[k], bst.data() + h.bond_base, blen.data() + h.bond_base);
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(stream));
     return DEM_OK;
 }
 

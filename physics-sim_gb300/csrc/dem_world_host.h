@@ -66,6 +66,8 @@ class World {
     // Replace one scene's state in place (same particle/bond/material counts).
     int upload_scene(int s, const dem_scene *scene);
     int download_scene(int s, dem_scene *out);
+    int upload_many(const int32_t *idx, const dem_scene *const *scenes, int count);
+    int download_many(const int32_t *idx, dem_scene *const *outs, int count);
     int set_params(int s, const dem_params &p);
     int set_materials(int s, const float *m, int n);
     int set_properties(int s, int32_t *selections, const int32_t *props);
@@ -144,6 +146,14 @@ class World {
     long long ref_cap = 0;
     int32_t *ref_err = nullptr;
     int ensure_ref(long long n);
+    RefArrays ref_at(long long off) const;
+    int stage_copy(int s, const dem_scene *sc, long long off, int32_t *err);
+    int stage_error(int32_t e);
+    int stage_commit(int s, const dem_scene *sc, long long off);
+    int adopt_layout(int s, const SceneHost &probe);
+    void unstage_launch(int s, long long off, int32_t *err);
+    int unstage_copy(int s, long long off, dem_scene *out, const int32_t *bst, const float *blen);
+    int unstage_error(int32_t e);
     // captured graphs, one per buffer parity at their start (a graph of R
     // steps swaps the pr/dp/rr buffers R - 1 times)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};   // graph_steps steps

@@ -127,7 +127,7 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_server_poll", "dem_server_fetch", "dem_server_events", "dem_server_release",
            "dem_server_get_stats", "dem_server_stream", "dem_batch_autotune", "dem_tune_last_error",
            "dem_generate_bonds", "dem_bondgen_last_error", "dem_event", "dem_get_datum",
-           "dem_batch_event", "dem_batch_get_datum"]
+           "dem_batch_event", "dem_batch_get_datum", "dem_batch_upload_many", "dem_batch_download_many"]
 
 _lib = None
 
@@ -589,6 +589,24 @@ class Batch:
     def upload(self, scene, sc):
         st = make_scene(sc)
         self._check(lib().dem_batch_upload(self.h, int(scene), C.byref(st)))
+
+    def upload_many(self, pairs):
+        """[(scene index, scene dict), ...] in one call (dem_batch_upload_many)."""
+        n = len(pairs)
+        structs = [make_scene(sc) for _, sc in pairs]
+        idx = (C.c_int32 * n)(*[int(k) for k, _ in pairs])
+        ptrs = (C.c_void_p * n)(*[C.addressof(st) for st in structs])
+        self._check(lib().dem_batch_upload_many(self.h, n, idx, ptrs))
+
+    def download_many(self, pairs):
+        """[(scene index, scene dict to fill), ...] in one call (dem_batch_download_many)."""
+        n = len(pairs)
+        structs = [make_scene(out) for _, out in pairs]
+        idx = (C.c_int32 * n)(*[int(k) for k, _ in pairs])
+        ptrs = (C.c_void_p * n)(*[C.addressof(st) for st in structs])
+        self._check(lib().dem_batch_download_many(self.h, n, idx, ptrs))
+        for (_, out), st in zip(pairs, structs):
+            out["coll_cont"] = np.array(st.coll_cont[:], dtype=np.int32)
 
     def break_events(self, cap=1 << 18):
         buf = np.zeros(cap, dtype=BREAK_DTYPE)

@@ -81,3 +81,49 @@ def test_batch_upload_replaces_one_scene_only():
     for k in (0, 1, 3):
         assert_same_state(after[k], before[k], "scene %d: " % k)
     assert np.array_equal(after[2]["pos"], items[2][0]["pos"])
+
+
+def test_bulk_upload_and_download_equal_per_scene_calls():
+    items = _items()
+    with dem.Batch(items) as b:
+        b.step(70)
+        per = [b.download(k) for k in range(len(items))]
+        bulk = [b.download(k) for k in range(len(items))]
+        for x in bulk:
+            for key in ("pos", "vel", "contacts", "data"):
+                x[key][:] = 0
+        b.download_many(list(enumerate(bulk)))
+        for k in range(len(items)):
+            assert_same_state(bulk[k], per[k], "download_many scene %d: " % k)
+            assert np.array_equal(bulk[k]["fixity"], per[k]["fixity"])
+            assert np.array_equal(bulk[k]["coll_cont"], per[k]["coll_cont"])
+        # restore every scene in one call and step on: equal to per-scene restores
+        b.upload_many(list(enumerate(per)))
+        b.step(35)
+        got = [b.download(k) for k in range(len(items))]
+    with dem.Batch(items) as c:
+        c.step(70)
+        for k in range(len(items)):
+            c.upload(k, per[k])
+        c.step(35)
+        ref = [c.download(k) for k in range(len(items))]
+    for k in range(len(items)):
+        assert_same_state(got[k], ref[k], "upload_many scene %d: " % k)
+
+
+def test_bulk_upload_rejects_a_bad_scene_and_writes_nothing():
+    items = _items()[:3]
+    with dem.Batch(items) as b:
+        b.step(35)
+        before = [b.download(k) for k in range(3)]
+        bad = copy_scene(before[2])
+        bad["contacts"] = bad["contacts"].copy()
+        c = bad["contacts"].reshape(-1, 14, 6)
+        c[0, 0, 1] = 10 ** 6          # partner out of range
+        good = copy_scene(before[0])
+        good["vel"] = good["vel"] + np.float32(1.0)
+        with pytest.raises(dem.DemError):
+            b.upload_many([(0, good), (2, bad)])
+        after = [b.download(k) for k in range(3)]
+    for k in range(3):
+        assert_same_state(after[k], before[k], "scene %d: " % k)
