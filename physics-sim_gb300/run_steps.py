@@ -22,10 +22,13 @@ def main():
     ap.add_argument("--particles", type=int, default=0, help="particles (dense_bed) or scenes (c3_batch)")
     ap.add_argument("--graph-steps", type=int, default=35)
     ap.add_argument("--plain", action="store_true", help="no CUDA graphs (for ncu)")
+    ap.add_argument("--split", action="store_true", help="Simulation pass as k_narrow + k_forces")
+    ap.add_argument("--unfused", action="store_true", help="every step its own LOM kernel")
     a = ap.parse_args()
+    knobs = {"split_narrow": int(a.split), "unfused_lom": int(a.unfused)}
     if a.workload == "c3_batch":
         items = dem_scenes.c3_batch(n_scenes=a.particles or 512)
-        with dem.Batch(items, reorder_interval=a.graph_steps, plain_launches=a.plain) as b:
+        with dem.Batch(items, reorder_interval=a.graph_steps, plain_launches=a.plain, **knobs) as b:
             b.step(a.steps)
             b.synchronize()
             print("ok", a.workload, len(items), "scenes", sum(len(x[0]["radii"]) for x in items),
@@ -41,7 +44,7 @@ def main():
         sc, p, ext = dem_scenes.dense_bed(n=a.particles or (1 << 20))
     else:
         raise SystemExit("unknown workload")
-    with dem.Context(sc, p, reorder_interval=a.graph_steps, plain_launches=a.plain, **ext) as ctx:
+    with dem.Context(sc, p, reorder_interval=a.graph_steps, plain_launches=a.plain, **knobs, **ext) as ctx:
         ctx.step(a.steps)
         ctx.synchronize()
         print("ok", a.workload, len(sc["radii"]), "particles", a.steps, "steps", ctx.stats())
