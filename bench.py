@@ -600,14 +600,22 @@ def run_ours_batch(args):
     # (host arrays are the caller's, allocated once, as State owns its vectors)
     h2d = sum(scene_bytes(x) for x in states)
     outs = [batch.download(k) for k in range(len(items))]
-    t0 = time.perf_counter()
+    # one untimed cycle first: it allocates the page-locked staging the
+    # bulk calls keep, as the warm-up steps do for the device buffers
     batch.upload_many(list(enumerate(states)))
     batch.step(F)
     batch.download_many(list(enumerate(outs)))
     barrier()
+    e2e_n = max(1, args.e2e_steps)
+    t0 = time.perf_counter()
+    for _ in range(e2e_n):
+        batch.upload_many(list(enumerate(states)))
+        batch.step(F)
+        batch.download_many(list(enumerate(outs)))
+    barrier()
     e2e_s = time.perf_counter() - t0
     del outs
-    e2e = {"value": ntot * F * ws / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+    e2e = {"value": ntot * F * e2e_n * ws / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": h2d,
            "note": "dem_batch_upload_many of all scenes + dem_batch_step(frame) + dem_batch_download_many of all scenes"}
 

@@ -243,9 +243,14 @@ int dem_batch_step(dem_batch *b, int32_t n_steps);
 int dem_batch_synchronize(dem_batch *b);
 int dem_batch_download(dem_batch *b, int32_t scene, dem_scene *out);
 int dem_batch_upload(dem_batch *b, int32_t scene, const dem_scene *in);
-/* The same for n scenes at once (scene indices idx[n]): one synchronisation
- * for all instead of several per scene.  upload_many writes nothing unless
- * every scene passes its checks. */
+/* The same for n scenes at once (scene indices idx[n]): a few large
+ * transfers, one conversion launch and one check for all of them, with host
+ * threads copying the callers' arrays through a page-locked block that the
+ * batch keeps (its size: 468 bytes a particle of the largest transfer, plus
+ * the world's bond, material and per-particle reference words).
+ * upload_many writes nothing unless every scene passes its checks, and a
+ * scene may appear in idx only once; download_many writes no caller's array
+ * unless every scene's conversion passed. */
 int dem_batch_upload_many(dem_batch *b, int32_t n, const int32_t *idx, const dem_scene *const *in);
 int dem_batch_download_many(dem_batch *b, int32_t n, const int32_t *idx, dem_scene *const *out);
 int dem_batch_set_params(dem_batch *b, int32_t scene, const dem_params *params);

@@ -1360,31 +1360,128 @@ void launch_mark_free(const DevWorld &w, int first, int count, int free_scene, c
 }
 
 // ------------------------------------------------------- layout conversion
-__global__ void k_stage_particles(DevWorld w, RefArrays r, int scene, int base, int n, int n_mat, float r_big,
-                                  int has_data, int32_t *err) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int g = base + i;
-    const float radius = r.radii[i];
-    const float4 pr = make_float4(r.pos[2 * i], r.pos[2 * i + 1], radius, r.rot[i]);
-    const float4 dp = make_float4(r.del_pos[2 * i], r.del_pos[2 * i + 1], r.del_rot[i], 0.0f);
+// Every item of a transfer in one launch.  The contact records (84 words a
+// particle, 72% of the bytes) are moved whole through shared memory: a tile
+// of ST_P particles is read or written as contiguous 16-byte words on the
+// reference side and as 32-particle rows on the slot side, so both sides
+// are coalesced.
+constexpr int ST_P = 64, ST_THREADS = 128, ST_REC = 6 * K, ST_REC4 = ST_REC / 4;
+static_assert(ST_REC % 4 == 0, "contact record is a whole number of 16-byte words");
+
+// item holding staged particle t, walking forward from item k (items are
+// packed and sorted by off)
+__device__ __forceinline__ int item_from(const StageItem *it, int count, int k, long long t) {
+    while (k + 1 < count && it[k + 1].off <= t) ++k;
+    return k;
+}
+
+__device__ __forceinline__ int item_search(const StageItem *it, int count, long long t) {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (it[mid].off <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// one thread per (particle, slot); a block's first item found by search,
+// the rest by walking
+__global__ void k_stage_check(RefArrays r, const StageItem *__restrict__ it, int count, long long total,
+                              int32_t *err) {
+    __shared__ int s_k0;
+    const long long u0 = (long long)blockIdx.x * blockDim.x;
+    if (threadIdx.x == 0) s_k0 = item_search(it, count, u0 / K);
+    __syncthreads();
+    const long long u = u0 + threadIdx.x;
+    if (u >= total * K) return;
+    const long long t = u / K;
+    const int k = item_from(it, count, s_k0, t);
+    const int n = it[k].n, i = (int)(t - it[k].off);
+    const int32_t *c = r.contacts + u * 6;
+    int e = 0;
+    if (c[5] >= it[k].n_bonds) e |= 2;
+    if (c[1] != -1) {
+        if (c[1] < 0 || c[1] >= n) e |= 4;
+        if (c[0] != i) e |= 8;
+    }
+    if (u % K == 0) {
+        const int mp = r.material_pointers[t];
+        if (mp < 0 || mp >= it[k].n_mat) e |= 1;
+    }
+    if (e) atomicOr(err + k, e);
+}
+
+void launch_stage_check(const RefArrays &r, const StageItem *items, int count, long long total, int32_t *err,
+                        cudaStream_t st) {
+    if (total <= 0 || count <= 0) return;
+    const long long t = total * K;
+    k_stage_check<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(r, items, count, total, err);
+}
+
+// tile of ST_P staged particles: their items and world indices
+__device__ __forceinline__ void tile_items(const StageItem *it, int count, long long t0, int np, int *s_item,
+                                           int *s_g) {
+    __shared__ int s_k0;
+    if (threadIdx.x == 0) s_k0 = item_search(it, count, t0);
+    __syncthreads();
+    if (threadIdx.x < np) {
+        const long long t = t0 + threadIdx.x;
+        const int k = item_from(it, count, s_k0, t);
+        s_item[threadIdx.x] = k;
+        s_g[threadIdx.x] = it[k].base + (int)(t - it[k].off);
+    }
+}
+
+__global__ void __launch_bounds__(ST_THREADS) k_stage_in(DevWorld w, RefArrays r, const StageItem *__restrict__ it,
+                                                          int count, long long total) {
+    __shared__ __align__(16) int32_t cont[ST_P * ST_REC];
+    __shared__ int s_item[ST_P], s_g[ST_P];
+    const long long t0 = (long long)blockIdx.x * ST_P;
+    const int np = (int)min((long long)ST_P, total - t0);
+    const int4 *src = reinterpret_cast<const int4 *>(r.contacts + t0 * ST_REC);
+    int4 *c4 = reinterpret_cast<int4 *>(cont);
+    for (int v = threadIdx.x; v < np * ST_REC4; v += ST_THREADS) c4[v] = src[v];
+    tile_items(it, count, t0, np, s_item, s_g);
+    __syncthreads();
+    // slot rows (slot j, particle p), p fastest
+    for (int q = threadIdx.x; q < K * ST_P; q += ST_THREADS) {
+        const int j = q / ST_P, p = q % ST_P;
+        if (p >= np) continue;
+        const int32_t *c = cont + p * ST_REC + 6 * j;
+        const size_t at = (size_t)j * w.N + s_g[p];
+        const int b = c[1];
+        w.s_b[at] = b != -1 ? it[s_item[p]].base + b : -1;
+        w.s_tf[at] = __int_as_float(c[2]);
+        w.s_btf[at] = __int_as_float(c[3]);
+        w.s_thb[at] = __int_as_float(c[4]);
+        w.s_bonded[at] = c[5];
+    }
+    if (threadIdx.x >= np) return;
+    const int p = threadIdx.x;
+    const StageItem I = it[s_item[p]];
+    const long long t = t0 + p;
+    const int g = s_g[p], i = (int)(t - I.off);
+    const float radius = r.radii[t];
+    const float4 pr = make_float4(r.pos[2 * t], r.pos[2 * t + 1], radius, r.rot[t]);
+    const float4 dp = make_float4(r.del_pos[2 * t], r.del_pos[2 * t + 1], r.del_rot[t], 0.0f);
     w.pr[g] = pr;
     w.pr_n[g] = pr;   // both buffers: a scene that never steps must read the same from either
     w.dp[g] = dp;
     w.dp_n[g] = dp;
-    w.vw[g] = make_float4(r.vel[2 * i], r.vel[2 * i + 1], r.rot_vel[i], 0.0f);
-    w.ac[g] = make_float4(r.acc[2 * i], r.acc[2 * i + 1], r.rot_acc[i], 0.0f);
-    const float *f = r.forces + 6 * (size_t)i;
+    w.vw[g] = make_float4(r.vel[2 * t], r.vel[2 * t + 1], r.rot_vel[t], 0.0f);
+    w.ac[g] = make_float4(r.acc[2 * t], r.acc[2 * t + 1], r.rot_acc[t], 0.0f);
+    const float *f = r.forces + 6 * t;
     w.fx[g] = make_float4(f[0], f[1], f[2], 0.0f);
     float4 d4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), dF = d4;
-    if (has_data) {
-        const float *dd = r.data + 7 * (size_t)i;
+    if (I.has_data) {
+        const float *dd = r.data + 7 * t;
         d4 = make_float4(dd[4], dd[5], dd[6], 0.0f);
         dF = make_float4(dd[0], dd[1], dd[2], 0.0f);
     }
     w.d4[g] = d4;
     w.dF[g] = dF;
-    const int32_t *fix = r.fixity + 6 * (size_t)i;
+    const int32_t *fix = r.fixity + 6 * t;
     uint32_t m = 0;
     m |= fix[0] == 0 ? M_KICK_X : 0u;
     m |= fix[1] == 0 ? M_KICK_Y : 0u;
@@ -1393,22 +1490,21 @@ __global__ void k_stage_particles(DevWorld w, RefArrays r, int scene, int base, 
     m |= fix[1] == 1 ? M_FIX_Y : 0u;
     m |= fix[2] == 1 ? M_FIX_R : 0u;
     if (f[0] != 0.0f || f[1] != 0.0f || f[2] != 0.0f) m |= M_FEXT;
-    const int mp = r.material_pointers[i];
-    if (mp < 0 || mp >= n_mat) atomicOr(err, 1);
+    const int mp = r.material_pointers[t];   // range checked before the launch
     m |= ((uint32_t)mp & 0xFFu) << 8;
     for (int k = 0; k < 6; ++k) {
         w.fix_ref[6 * (size_t)g + k] = fix[k];
         w.force_ref[6 * (size_t)g + k] = f[k];
     }
     w.matp_ref[g] = mp;
-    w.data3[g] = has_data ? r.data[7 * (size_t)i + 3] : 0.0f;
-    m |= (uint32_t)scene << 16;
-    if (radius > r_big) m |= M_BIG;
+    w.data3[g] = I.has_data ? r.data[7 * t + 3] : 0.0f;
+    m |= (uint32_t)I.scene << 16;
+    if (radius > I.r_big) m |= M_BIG;
     w.meta[g] = m;
     w.orig[g] = i;
     w.o2i[g] = g;
     uint32_t mk = 0;
-    const int32_t *c = r.contacts + (size_t)i * K * 6;
+    const int32_t *c = cont + p * ST_REC;
     for (int j = 0; j < K; ++j) {
         if (c[6 * j + 5] >= 0) mk |= 1u << (BSHIFT + j);
         if (c[6 * j + 1] != -1) mk |= 1u << j;
@@ -1417,67 +1513,80 @@ __global__ void k_stage_particles(DevWorld w, RefArrays r, int scene, int base, 
     w.smask[g] = mk;
 }
 
-// one thread per (slot, particle), slot-major: the slot arrays are written
-// row by row
-__global__ void k_stage_slots(DevWorld w, RefArrays r, int base, int n) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)n * K) return;
-    const int j = (int)(t / n), i = (int)(t % n);
-    const int32_t *c = r.contacts + ((size_t)i * K + j) * 6;
-    const size_t at = (size_t)j * w.N + base + i;
-    const int b = c[1];
-    w.s_b[at] = b != -1 ? base + b : -1;
-    w.s_tf[at] = __int_as_float(c[2]);
-    w.s_btf[at] = __int_as_float(c[3]);
-    w.s_thb[at] = __int_as_float(c[4]);
-    w.s_bonded[at] = c[5];
+void launch_stage_in(const DevWorld &w, const RefArrays &r, const StageItem *items, int count, long long total,
+                     cudaStream_t st) {
+    if (total <= 0 || count <= 0) return;
+    k_stage_in<<<(unsigned)((total + ST_P - 1) / ST_P), ST_THREADS, 0, st>>>(w, r, items, count, total);
 }
 
-// the reference-layout arrays checked before anything is written
-__global__ void k_stage_check(RefArrays r, int n, int n_bonds, int n_mat, int32_t *err) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)n * K) return;
-    const int i = (int)(t / K);
-    const int32_t *c = r.contacts + t * 6;
-    if (c[5] >= n_bonds) atomicOr(err, 2);
-    if (c[1] != -1) {
-        if (c[1] < 0 || c[1] >= n) atomicOr(err, 4);
-        if (c[0] != i) atomicOr(err, 8);
+// The world's particles of every item, in world order, to the reference
+// layout in original order (orig[g]); the per-particle reference mirrors
+// (fixity, forces, material pointers, data[3]) are indexed by original index
+// and read by the host directly.
+__global__ void __launch_bounds__(ST_THREADS) k_stage_out(DevWorld w, RefArrays r, const StageItem *__restrict__ it,
+                                                           int count, long long total, int32_t *err) {
+    __shared__ __align__(16) int32_t cont[ST_P * ST_REC];
+    __shared__ int s_item[ST_P], s_g[ST_P], s_o[ST_P];
+    __shared__ uint32_t s_mask[ST_P];
+    const long long t0 = (long long)blockIdx.x * ST_P;
+    const int np = (int)min((long long)ST_P, total - t0);
+    tile_items(it, count, t0, np, s_item, s_g);
+    if (threadIdx.x < np) {
+        const int k = s_item[threadIdx.x], g = s_g[threadIdx.x];
+        const int o = w.orig[g];
+        if (o < 0 || o >= it[k].n) {
+            atomicOr(err + k, 16);
+            s_o[threadIdx.x] = -1;
+        } else {
+            s_o[threadIdx.x] = o;
+        }
+        s_mask[threadIdx.x] = w.smask[g];
     }
-    if (t % K == 0) {
-        const int mp = r.material_pointers[i];
-        if (mp < 0 || mp >= n_mat) atomicOr(err, 1);
+    __syncthreads();
+    for (int q = threadIdx.x; q < K * ST_P; q += ST_THREADS) {
+        const int j = q / ST_P, p = q % ST_P;
+        if (p >= np || s_o[p] < 0) continue;
+        const int g = s_g[p];
+        const size_t at = (size_t)j * w.N + g;
+        int32_t *c = cont + p * ST_REC + 6 * j;
+        if ((s_mask[p] >> j) & 1u) {
+            const int pb = w.s_b[at];
+            const int base = it[s_item[p]].base, n = it[s_item[p]].n;
+            if (pb < base || pb >= base + n) {
+                atomicOr(err + s_item[p], 32);
+                c[0] = -1;
+                c[1] = -1;
+            } else {
+                c[0] = s_o[p];
+                c[1] = w.orig[pb];
+            }
+        } else {
+            c[0] = -1;
+            c[1] = -1;
+        }
+        c[2] = __float_as_int(w.s_tf[at]);
+        c[3] = __float_as_int(w.s_btf[at]);
+        c[4] = __float_as_int(w.s_thb[at]);
+        c[5] = w.s_bonded[at];
     }
-}
-
-void launch_stage_check(const RefArrays &r, int n, int n_bonds, int n_mat, int32_t *err, cudaStream_t st) {
-    if (n <= 0) return;
-    const long long t = (long long)n * K;
-    k_stage_check<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(r, n, n_bonds, n_mat, err);
-}
-
-void launch_stage_in(const DevWorld &w, const RefArrays &r, int scene, int base, int n, int n_mat, float r_big,
-                     int has_data, int32_t *err, cudaStream_t st) {
-    if (n <= 0) return;
-    k_stage_particles<<<(n + 255) / 256, 256, 0, st>>>(w, r, scene, base, n, n_mat, r_big, has_data, err);
-    const long long t = (long long)n * K;
-    k_stage_slots<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(w, r, base, n);
-}
-
-__global__ void k_stage_out(DevWorld w, RefArrays r, int base, int n, int32_t *err) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const int g = base + k;
-    const int o = w.orig[g];
-    if (o < 0 || o >= n) {
-        atomicOr(err, 16);
-        return;
+    __syncthreads();
+    // whole records to their original positions
+    const int4 *c4 = reinterpret_cast<const int4 *>(cont);
+    for (int v = threadIdx.x; v < np * ST_REC4; v += ST_THREADS) {
+        const int p = v / ST_REC4, q = v % ST_REC4;
+        if (s_o[p] < 0) continue;
+        const long long dst = it[s_item[p]].off + s_o[p];
+        reinterpret_cast<int4 *>(r.contacts + dst * ST_REC)[q] = c4[v];
     }
-    const float4 p = w.pr[g], v = w.vw[g], a = w.ac[g], d = w.dp[g], d4 = w.d4[g], dF = w.dF[g];
-    r.pos[2 * o] = p.x;
-    r.pos[2 * o + 1] = p.y;
-    r.radii[o] = p.z;
-    r.rot[o] = p.w;
+    if (threadIdx.x >= np || s_o[threadIdx.x] < 0) return;
+    const int p = threadIdx.x, g = s_g[p];
+    const StageItem I = it[s_item[p]];
+    const long long o = I.off + s_o[p];
+    const float4 pp = w.pr[g], v = w.vw[g], a = w.ac[g], d = w.dp[g], d4 = w.d4[g], dF = w.dF[g];
+    r.pos[2 * o] = pp.x;
+    r.pos[2 * o + 1] = pp.y;
+    r.radii[o] = pp.z;
+    r.rot[o] = pp.w;
     r.vel[2 * o] = v.x;
     r.vel[2 * o + 1] = v.y;
     r.rot_vel[o] = v.z;
@@ -1487,42 +1596,20 @@ __global__ void k_stage_out(DevWorld w, RefArrays r, int base, int n, int32_t *e
     r.del_pos[2 * o] = d.x;
     r.del_pos[2 * o + 1] = d.y;
     r.del_rot[o] = d.z;
-    float *dd = r.data + 7 * (size_t)o;
+    float *dd = r.data + 7 * o;
     dd[0] = dF.x;
     dd[1] = dF.y;
     dd[2] = dF.z;
-    dd[3] = w.data3[base + o];
+    dd[3] = w.data3[I.base + s_o[p]];
     dd[4] = d4.x;
     dd[5] = d4.y;
     dd[6] = d4.z;
-    const uint32_t mask = w.smask[g];
-    int32_t *c = r.contacts + (size_t)o * K * 6;
-    for (int j = 0; j < K; ++j) {
-        const size_t at = (size_t)j * w.N + g;
-        if ((mask >> j) & 1u) {
-            const int pb = w.s_b[at];
-            if (pb < base || pb >= base + n) {
-                atomicOr(err, 32);
-                c[6 * j] = -1;
-                c[6 * j + 1] = -1;
-            } else {
-                c[6 * j] = o;
-                c[6 * j + 1] = w.orig[pb];
-            }
-        } else {
-            c[6 * j] = -1;
-            c[6 * j + 1] = -1;
-        }
-        c[6 * j + 2] = __float_as_int(w.s_tf[at]);
-        c[6 * j + 3] = __float_as_int(w.s_btf[at]);
-        c[6 * j + 4] = __float_as_int(w.s_thb[at]);
-        c[6 * j + 5] = w.s_bonded[at];
-    }
 }
 
-void launch_stage_out(const DevWorld &w, const RefArrays &r, int base, int n, int32_t *err, cudaStream_t st) {
-    if (n <= 0) return;
-    k_stage_out<<<(n + 255) / 256, 256, 0, st>>>(w, r, base, n, err);
+void launch_stage_out(const DevWorld &w, const RefArrays &r, const StageItem *items, int count, long long total,
+                      int32_t *err, cudaStream_t st) {
+    if (total <= 0 || count <= 0) return;
+    k_stage_out<<<(unsigned)((total + ST_P - 1) / ST_P), ST_THREADS, 0, st>>>(w, r, items, count, total, err);
 }
 
 // ------------------------------------------------------- Fix / Drop / Release

@@ -218,16 +218,28 @@ struct RefArrays {
     float *pos, *radii, *vel, *acc, *rot, *rot_vel, *rot_acc, *forces, *del_pos, *del_rot, *data;
     int32_t *fixity, *contacts, *material_pointers;
 };
-// validation of the staged arrays; failures OR bits into *err: 1 material
-// pointer, 2 bonded index >= n_bonds, 4 partner out of range, 8 record's a
-// differs from its owner
-void launch_stage_check(const RefArrays &r, int n, int n_bonds, int n_mat, int32_t *err, cudaStream_t st);
-// reference layout -> internal layout of scene `scene` (n particles at `base`)
-void launch_stage_in(const DevWorld &w, const RefArrays &r, int scene, int base, int n, int n_mat, float r_big,
-                     int has_data, int32_t *err, cudaStream_t st);
-// internal layout -> reference layout (data[7i+3] is left to the host);
-// *err bits: 16 internal map corrupt, 32 contact partner outside the scene
-void launch_stage_out(const DevWorld &w, const RefArrays &r, int base, int n, int32_t *err, cudaStream_t st);
+// One scene of a staging transfer: particles [off, off + n) of the staging
+// block are particles [base, base + n) of the world, which hold scene `scene`.
+// A transfer's items are packed: off of item k+1 = off + n of item k, n > 0.
+struct StageItem {
+    long long off;
+    int base, n, scene, n_mat, n_bonds, has_data;
+    float r_big;
+    int pad;
+};
+// validation of the staged arrays (items in device memory, `total` staged
+// particles); failures OR bits into err[k] of item k: 1 material pointer,
+// 2 bonded index >= n_bonds, 4 partner out of range, 8 record's a differs
+// from its owner
+void launch_stage_check(const RefArrays &r, const StageItem *items, int count, long long total, int32_t *err,
+                        cudaStream_t st);
+// reference layout -> internal layout of every item's scene
+void launch_stage_in(const DevWorld &w, const RefArrays &r, const StageItem *items, int count, long long total,
+                     cudaStream_t st);
+// internal layout -> reference layout; err[k] bits: 16 internal map corrupt,
+// 32 contact partner outside the scene
+void launch_stage_out(const DevWorld &w, const RefArrays &r, const StageItem *items, int count, long long total,
+                      int32_t *err, cudaStream_t st);
 
 // Fix / Drop / Release events (src/shaders/event_handling/{Fix,Drop,Release}.wgsl)
 // on `count` particles of the scene whose first particle is `base`, given

@@ -1,9 +1,13 @@
 // dem_world_host.cu -- host owner of the device world (see dem_world_host.h).
+#include <sched.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <climits>
 #include <limits>
+#include <memory>
 #include <thread>
 
 #include "dem_world_host.h"
@@ -72,6 +76,9 @@ World::~World() {
     set_timing(false);
     release();
     if (ref_block) cudaFree(ref_block);
+    if (pin) cudaFreeHost(pin);
+    if (d_items) cudaFree(d_items);
+    for (auto e : xfer_ev) cudaEventDestroy(e);
     if (side) cudaStreamDestroy(side);
 }
 
@@ -108,8 +115,245 @@ int World::ensure_ref(long long n) {
     ref.fixity = reinterpret_cast<int32_t *>(take(6));
     ref.contacts = reinterpret_cast<int32_t *>(take(84));
     ref.material_pointers = reinterpret_cast<int32_t *>(take(1));
-    ref_err = reinterpret_cast<int32_t *>(f);
     ref_cap = cap;
+    return DEM_OK;
+}
+
+// The staging block's fields in order: words per particle and the scene
+// array each one mirrors (the device block and the pinned host block share
+// this layout, field f at base * cap words).
+namespace {
+struct RefField {
+    int per;
+    size_t base;  // words per particle before this field
+};
+constexpr int N_REF_FIELDS = 14, F_CONTACTS = 12, REF_WORDS = 117;
+constexpr RefField REF_FIELDS[N_REF_FIELDS] = {
+    {2, 0}, {1, 2}, {2, 3}, {2, 5}, {1, 7}, {1, 8}, {1, 9}, {6, 10}, {2, 16}, {1, 18}, {7, 19}, {6, 26}, {84, 32}, {1, 116}};
+// the fields k_stage_out writes (fixity, forces and material pointers are
+// read from the world's reference mirrors instead)
+constexpr bool OUT_FIELD[N_REF_FIELDS] = {true, true, true, true, true, true, true,
+                                          false, true, true, true, false, true, false};
+const void *scene_field(const dem_scene *sc, int f) {
+    switch (f) {
+        case 0: return sc->pos;
+        case 1: return sc->radii;
+        case 2: return sc->vel;
+        case 3: return sc->acc;
+        case 4: return sc->rot;
+        case 5: return sc->rot_vel;
+        case 6: return sc->rot_acc;
+        case 7: return sc->forces;
+        case 8: return sc->del_pos;
+        case 9: return sc->del_rot;
+        case 10: return sc->data;
+        case 11: return sc->fixity;
+        case 12: return sc->contacts;
+        default: return sc->material_pointers;
+    }
+}
+
+// cores this process may run on
+int host_threads() {
+    static const int n = [] {
+        int c = (int)std::thread::hardware_concurrency();
+        cpu_set_t set;
+        CPU_ZERO(&set);
+        if (sched_getaffinity(0, sizeof set, &set) == 0) c = CPU_COUNT(&set);
+        return std::max(1, c);
+    }();
+    return n;
+}
+
+// run fn(k) for k in [0, count) on up to host_threads() threads
+template <class F>
+void par_for(int count, F fn) {
+    const int T = std::max(1, std::min(count, host_threads()));
+    if (T == 1) {
+        for (int k = 0; k < count; ++k) fn(k);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < T; ++t)
+        pool.emplace_back([&, t]() {
+            for (int k = t; k < count; k += T) fn(k);
+        });
+    for (auto &th : pool) th.join();
+}
+
+// Host copying beside the transfers.  Chunk c holds units [cum[c], cum[c+1]);
+// threads take units in order.  A unit of chunk c starts once the chunk is
+// released (downloads release a chunk when its copy has landed; uploads
+// start with every chunk released) and wait_chunk(c) returns once all of
+// chunk c's units have run (uploads then issue its copy).
+class HostPipe {
+  public:
+    HostPipe(const std::vector<long long> &sizes, bool gated)
+        : n_chunks((int)sizes.size()),
+          cum(sizes.size() + 1, 0),
+          ready(new std::atomic<int>[sizes.size() + 1]),
+          left(new std::atomic<long long>[sizes.size() + 1]) {
+        for (int c = 0; c < n_chunks; ++c) {
+            cum[c + 1] = cum[c] + sizes[c];
+            ready[c].store(gated ? 0 : 1);
+            left[c].store(sizes[c]);
+        }
+    }
+    ~HostPipe() {
+        cancel();
+        join();
+    }
+    template <class F>
+    void start(F unit) {
+        const int T = (int)std::max(1LL, std::min<long long>(cum[n_chunks], host_threads()));
+        for (int t = 0; t < T; ++t)
+            pool.emplace_back([this, unit]() {
+                for (;;) {
+                    const long long u = next.fetch_add(1);
+                    if (u >= cum[n_chunks]) return;
+                    const int c = (int)(std::upper_bound(cum.begin(), cum.end(), u) - cum.begin()) - 1;
+                    while (!ready[c].load(std::memory_order_acquire)) {
+                        if (stop.load()) return;
+                        std::this_thread::yield();
+                    }
+                    if (stop.load()) return;
+                    unit(c, u - cum[c]);
+                    left[c].fetch_sub(1, std::memory_order_acq_rel);
+                }
+            });
+    }
+    void wait_chunk(int c) {
+        while (left[c].load(std::memory_order_acquire) > 0) std::this_thread::yield();
+    }
+    void release(int c) { ready[c].store(1, std::memory_order_release); }
+    void cancel() { stop.store(1); }
+    void join() {
+        for (auto &th : pool) th.join();
+        pool.clear();
+    }
+
+  private:
+    int n_chunks;
+    std::vector<long long> cum;
+    std::unique_ptr<std::atomic<int>[]> ready;
+    std::unique_ptr<std::atomic<long long>[]> left;
+    std::atomic<long long> next{0};
+    std::atomic<int> stop{0};
+    std::vector<std::thread> pool;
+};
+
+// byte offsets of the regions of one pinned transfer block (16-byte aligned)
+struct PinMap {
+    size_t bytes = 0;
+    size_t take(size_t n) {
+        const size_t at = bytes;
+        bytes += (n + 15) & ~(size_t)15;
+        return at;
+    }
+};
+
+// [start, start + len) ranges of one array, sorted and merged where they touch
+std::vector<std::pair<long long, long long>> merge_runs(std::vector<std::pair<long long, long long>> r) {
+    std::sort(r.begin(), r.end());
+    std::vector<std::pair<long long, long long>> out;
+    for (const auto &x : r) {
+        if (x.second <= 0) continue;
+        if (!out.empty() && out.back().first + out.back().second == x.first) out.back().second += x.second;
+        else out.push_back(x);
+    }
+    return out;
+}
+
+// table items [0, count) in up to `groups` consecutive ranges of about equal
+// particle counts
+std::vector<std::pair<int, int>> split_items(const std::vector<StageItem> &tab, int groups) {
+    std::vector<std::pair<int, int>> g;
+    long long total = 0;
+    for (const auto &it : tab) total += it.n;
+    int i0 = 0;
+    long long acc = 0;
+    for (int i = 0; i < (int)tab.size(); ++i) {
+        acc += tab[i].n;
+        if (acc * groups >= total * ((long long)g.size() + 1) || i + 1 == (int)tab.size()) {
+            g.emplace_back(i0, i + 1);
+            i0 = i + 1;
+        }
+    }
+    return g;
+}
+
+// material records and the material-pair stiffness table of one scene:
+// 1/(1/k_a + 1/k_b) for normal and shear stiffness (2D_Simulation.wgsl:345-346),
+// in float arithmetic, division correctly rounded
+void material_tables(const float *materials, int M, Mat *mats, float2 *pair) {
+    for (int k = 0; k < M; ++k) {
+        const float *mm = materials + 6 * k;
+        mats[k] = Mat{mm[3], mm[4], mm[5], 0.0f};
+    }
+    for (int a = 0; a < M; ++a)
+        for (int b = 0; b < M; ++b) {
+            volatile float kna = mats[a].kn, knb = mats[b].kn, ksa = mats[a].ks, ksb = mats[b].ks;
+            volatile float ia = 1.0f / kna, ib = 1.0f / knb;
+            volatile float sum = ia + ib;
+            volatile float kn = 1.0f / sum;
+            volatile float ja = 1.0f / ksa, jb = 1.0f / ksb;
+            volatile float sum2 = ja + jb;
+            volatile float ks = 1.0f / sum2;
+            pair[(size_t)a * M + b] = make_float2(kn, ks);
+        }
+}
+
+// a scene's bond records [status, angle, length bits] split into the
+// device arrays' words (strengths from the scene's per-bond values, else 0)
+void split_bonds(const SceneHost &h, const int32_t *bonds, int32_t *st, float *len, float2 *str, int32_t *ang) {
+    for (int k = 0; k < h.n_bonds; ++k) {
+        st[k] = bonds[3 * k];
+        ang[k] = bonds[3 * k + 1];
+        len[k] = bits2f(bonds[3 * k + 2]);
+        str[k] = make_float2(h.bond_sn.empty() ? 0.0f : h.bond_sn[k], h.bond_ss.empty() ? 0.0f : h.bond_ss[k]);
+    }
+}
+}  // namespace
+
+// page-locked host staging of the bulk transfers (grows, kept)
+int World::ensure_pin(size_t bytes) {
+    if (bytes <= pin_bytes && pin) return DEM_OK;
+    if (pin) cudaFreeHost(pin);
+    pin = nullptr;
+    pin_bytes = 0;
+    if (cudaHostAlloc(&pin, bytes, cudaHostAllocDefault) != cudaSuccess) {
+        pin = nullptr;
+        return fail(DEM_E_OOM, "pinned staging allocation failed");
+    }
+    pin_bytes = bytes;
+    return DEM_OK;
+}
+
+// device table of a transfer's items and their check words (grows, kept)
+int World::ensure_items(int count) {
+    if (count <= items_cap && d_items) return DEM_OK;
+    if (d_items) cudaFree(d_items);
+    d_items = nullptr;
+    d_item_err = nullptr;
+    items_cap = 0;
+    const int cap = std::max(count, 64);
+    void *p = nullptr;
+    if (cudaMalloc(&p, (size_t)cap * (sizeof(StageItem) + 4)) != cudaSuccess)
+        return fail(DEM_E_OOM, "staging table allocation failed");
+    d_items = static_cast<StageItem *>(p);
+    d_item_err = reinterpret_cast<int32_t *>(d_items + cap);
+    items_cap = cap;
+    return DEM_OK;
+}
+
+// one event per pipelined transfer chunk (created once, kept)
+int World::ensure_events(int count) {
+    while ((int)xfer_ev.size() < count) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return fail(DEM_E_CUDA, "event creation failed");
+        xfer_ev.push_back(e);
+    }
     return DEM_OK;
 }
 
@@ -470,38 +714,6 @@ RefArrays World::ref_at(long long off) const {
     return r;
 }
 
-// Staging of a scene, in three phases so that many scenes can share one
-// synchronisation: copy the reference-layout arrays whole into the staging
-// block at `off` and queue their check (err word at *err); then, once the
-// checks passed, convert on the device and upload bonds and materials.
-int World::stage_copy(int s, const dem_scene *sc, long long off, int32_t *err) {
-    SceneHost &h = sh[s];
-    const int n = h.n;
-    h.materials.assign(sc->materials, sc->materials + 6 * (size_t)h.n_mat);
-    if (n <= 0) return DEM_OK;
-    const RefArrays r = ref_at(off);
-    auto up = [&](void *dst, const void *src, size_t words) {
-        return cudaMemcpyAsync(dst, src, words * 4, cudaMemcpyHostToDevice, stream);
-    };
-    const size_t un = (size_t)n;
-    CK(up(r.pos, sc->pos, 2 * un));
-    CK(up(r.radii, sc->radii, un));
-    CK(up(r.vel, sc->vel, 2 * un));
-    CK(up(r.acc, sc->acc, 2 * un));
-    CK(up(r.rot, sc->rot, un));
-    CK(up(r.rot_vel, sc->rot_vel, un));
-    CK(up(r.rot_acc, sc->rot_acc, un));
-    CK(up(r.forces, sc->forces, 6 * un));
-    CK(up(r.fixity, sc->fixity, 6 * un));
-    CK(up(r.del_pos, sc->del_pos, 2 * un));
-    CK(up(r.del_rot, sc->del_rot, un));
-    CK(up(r.contacts, sc->contacts, 84 * un));
-    CK(up(r.material_pointers, sc->material_pointers, un));
-    if (sc->data) CK(up(r.data, sc->data, 7 * un));
-    launch_stage_check(r, n, h.n_bonds, h.n_mat, err, stream);
-    return DEM_OK;
-}
-
 int World::stage_error(int32_t e) {
     if (e & 1) return fail(DEM_E_INVALID, "material pointer out of range");
     if (e & 2) return fail(DEM_E_INVALID, "contact bonded index beyond n_bonds");
@@ -510,11 +722,41 @@ int World::stage_error(int32_t e) {
     return DEM_OK;
 }
 
-int World::stage_commit(int s, const dem_scene *sc, long long off) {
+// One scene, its arrays copied straight from the caller's memory into the
+// staging block and checked there; only then (probe: a re-upload's new
+// layout) is anything of the scene changed, and the block converted.
+int World::stage_scene(int s, const dem_scene *sc, const SceneHost *probe) {
     SceneHost &h = sh[s];
-    const int n = h.n, base = h.particle_base;
+    const int n = h.n;
     if (n > 0) {
-        launch_stage_in(d, ref_at(off), s, base, n, h.n_mat, h.r_big, sc->data ? 1 : 0, ref_err, stream);
+        int rc = ensure_ref(n);
+        if (rc) return rc;
+        rc = ensure_items(1);
+        if (rc) return rc;
+        const StageItem it{0, h.particle_base, n, s, h.n_mat, h.n_bonds, sc->data ? 1 : 0,
+                           probe ? probe->r_big : h.r_big, 0};
+        float *dp0 = static_cast<float *>(ref_block);
+        for (int f = 0; f < N_REF_FIELDS; ++f) {
+            const void *src = scene_field(sc, f);
+            if (!src) continue;
+            const RefField &F = REF_FIELDS[f];
+            CK(cudaMemcpyAsync(dp0 + F.base * ref_cap, src, sizeof(float) * F.per * (size_t)n, cudaMemcpyHostToDevice,
+                               stream));
+        }
+        CK(cudaMemcpyAsync(d_items, &it, sizeof it, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemsetAsync(d_item_err, 0, 4, stream));
+        launch_stage_check(ref, d_items, 1, n, d_item_err, stream);
+        CK(cudaGetLastError());
+        int32_t e = 0;
+        CK(cudaMemcpyAsync(&e, d_item_err, 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        rc = stage_error(e);
+        if (rc) return rc;
+    }
+    if (probe) apply_layout(s, *probe);
+    h.materials.assign(sc->materials, sc->materials + 6 * (size_t)h.n_mat);
+    if (n > 0) {
+        launch_stage_in(d, ref, d_items, 1, n, stream);
         CK(cudaGetLastError());
     }
     const int nb = h.n_bonds;
@@ -523,13 +765,7 @@ int World::stage_commit(int s, const dem_scene *sc, long long off) {
         std::vector<float> len(nb);
         std::vector<float2> str(nb);
         h.bond_angle.resize(nb);
-        for (int k = 0; k < nb; ++k) {
-            st[k] = sc->bonds[3 * k];
-            h.bond_angle[k] = sc->bonds[3 * k + 1];
-            len[k] = bits2f(sc->bonds[3 * k + 2]);
-            str[k] = make_float2(h.bond_sn.empty() ? 0.0f : h.bond_sn[k],
-                                 h.bond_ss.empty() ? 0.0f : h.bond_ss[k]);
-        }
+        split_bonds(h, sc->bonds, st.data(), len.data(), str.data(), h.bond_angle.data());
         CK(cudaMemcpyAsync(d.b_status + h.bond_base, st.data(), 4 * (size_t)nb, cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync(d.b_length + h.bond_base, len.data(), 4 * (size_t)nb, cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync(d.b_str + h.bond_base, str.data(), 8 * (size_t)nb, cudaMemcpyHostToDevice, stream));
@@ -538,46 +774,12 @@ int World::stage_commit(int s, const dem_scene *sc, long long off) {
     return push_materials(s);
 }
 
-int World::stage_scene(int s, const dem_scene *sc) {
-    const int n = sh[s].n;
-    if (n > 0) {
-        int rc = ensure_ref(n);
-        if (rc) return rc;
-    }
-    CK(cudaMemsetAsync(ref_err, 0, 4, stream));
-    int rc = stage_copy(s, sc, 0, ref_err);
-    if (rc) return rc;
-    int32_t e = 0;
-    CK(cudaMemcpyAsync(&e, ref_err, 4, cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    rc = stage_error(e);
-    if (rc) return rc;
-    return stage_commit(s, sc, 0);
-}
-
-// material records and the material-pair stiffness table of one scene:
-// 1/(1/k_a + 1/k_b) for normal and shear stiffness (2D_Simulation.wgsl:345-346),
-// in float arithmetic, division correctly rounded
 int World::push_materials(int s) {
     SceneHost &h = sh[s];
     const int M = h.n_mat;
     std::vector<Mat> mats(M);
     std::vector<float2> pair((size_t)M * M);
-    for (int k = 0; k < M; ++k) {
-        const float *mm = h.materials.data() + 6 * k;
-        mats[k] = Mat{mm[3], mm[4], mm[5], 0.0f};
-    }
-    for (int a = 0; a < M; ++a)
-        for (int b = 0; b < M; ++b) {
-            volatile float kna = mats[a].kn, knb = mats[b].kn, ksa = mats[a].ks, ksb = mats[b].ks;
-            volatile float ia = 1.0f / kna, ib = 1.0f / knb;
-            volatile float sum = ia + ib;
-            volatile float kn = 1.0f / sum;
-            volatile float ja = 1.0f / ksa, jb = 1.0f / ksb;
-            volatile float sum2 = ja + jb;
-            volatile float ks = 1.0f / sum2;
-            pair[(size_t)a * M + b] = make_float2(kn, ks);
-        }
+    material_tables(h.materials.data(), M, mats.data(), pair.data());
     CK(cudaMemcpyAsync(d.mats + h.mat_base, mats.data(), M * sizeof(Mat), cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d.pair + h.pair_base, pair.data(), pair.size() * sizeof(float2),
                        cudaMemcpyHostToDevice, stream));
@@ -649,7 +851,7 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     if (rc) return rc;
     update_has_bigs();
     for (int s = 0; s < S; ++s) {
-        rc = stage_scene(s, scenes[s]);
+        rc = stage_scene(s, scenes[s], nullptr);
         if (rc) return rc;
         rc = push_bigs(s, s);
         if (rc) return rc;
@@ -780,7 +982,7 @@ int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e
     h.cc2_0 = sc->coll_cont[2];
     h.active = true;
     sh[s] = h;
-    rc = stage_scene(s, sc);
+    rc = stage_scene(s, sc, nullptr);
     if (rc == DEM_OK) rc = push_bigs(s, s);
     if (rc == DEM_OK) rc = push_par(s);
     if (rc == DEM_OK) {
@@ -823,13 +1025,18 @@ int World::retire(int s) {
 }
 
 // A re-uploaded scene keeps its cell budget and large-particle records and
-// adopts the new geometry inside them.
-int World::adopt_layout(int s, const SceneHost &probe) {
-    SceneHost &h = sh[s];
+// adopts the new geometry inside them: layout_fits checks, apply_layout adopts.
+int World::layout_fits(int s, const SceneHost &probe) {
+    const SceneHost &h = sh[s];
     if (probe.n_cells > h.n_cells)
         return fail(DEM_E_UNSUPPORTED, "uploaded scene needs a larger search grid; create a new context");
     if (probe.n_big > h.big_cap)
         return fail(DEM_E_UNSUPPORTED, "uploaded scene has more large particles; create a new context");
+    return DEM_OK;
+}
+
+void World::apply_layout(int s, const SceneHost &probe) {
+    SceneHost &h = sh[s];
     h.r_max = probe.r_max;
     h.r_big = probe.r_big;
     h.n_big = probe.n_big;
@@ -840,34 +1047,35 @@ int World::adopt_layout(int s, const SceneHost &probe) {
     h.par.g_y0 = probe.par.g_y0;
     h.par.g_w = probe.par.g_w;
     h.par.g_h = probe.par.g_h;
-    return DEM_OK;
 }
 
-// Many scenes at once (dem_batch_upload_many): the layouts are derived on
-// host threads, every scene's arrays are copied and checked before one
-// synchronisation, then converted; one rebuild follows.  Nothing is written
-// to any scene unless every scene passes its checks.
+// Many scenes at once (dem_batch_upload_many).  The layouts are derived on
+// host threads; host threads copy every scene into a page-locked block laid
+// out like the staging block while the block goes to the device one field
+// at a time; one launch checks every scene.  Nothing of any scene changes
+// unless every scene passes; then one launch converts them all and the
+// bonds, materials and scene parameters follow in merged transfers.
 int World::upload_many(const int32_t *idx, const dem_scene *const *scs, int count) {
     if (count <= 0) return DEM_OK;
     if (!idx || !scs) return fail(DEM_E_INVALID, "scene index/pointer arrays are NULL");
     std::vector<SceneHost> probes(count);
     std::vector<int> rcs(count, DEM_OK);
     std::vector<std::string> errs(count);
-    long long total = 0;
+    std::vector<char> seen(sh.size(), 0);
     for (int k = 0; k < count; ++k) {
         const int s = idx[k];
         if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+        if (seen[s]++) return fail(DEM_E_INVALID, "scene " + std::to_string(s) + " listed twice");
         const SceneHost &h = sh[s];
         const dem_scene *sc = scs[k];
         if (!sc || sc->n_particles != h.n || sc->n_bonds != h.n_bonds || sc->n_materials != h.n_mat)
             return fail(DEM_E_INVALID, "upload must keep particle, bond and material counts (scene " +
                                            std::to_string(s) + ")");
         probes[k] = h;
-        total += h.n;
     }
     {
         // compute_layout touches only its probe; derive them in parallel
-        const int T = std::max(1, std::min<int>(count, (int)std::thread::hardware_concurrency()));
+        const int T = std::max(1, std::min(count, host_threads()));
         std::vector<std::thread> pool;
         std::vector<World> scratch(T);
         for (int t = 0; t < T; ++t)
@@ -883,40 +1091,146 @@ int World::upload_many(const int32_t *idx, const dem_scene *const *scs, int coun
     for (int k = 0; k < count; ++k)
         if (rcs[k]) return fail(rcs[k], errs[k] + " (scene " + std::to_string(idx[k]) + ")");
     for (int k = 0; k < count; ++k) {
-        int rc = adopt_layout(idx[k], probes[k]);
-        if (rc) return rc;
-    }
-    int rc = ensure_ref(total);
-    if (rc) return rc;
-    int32_t *d_err = nullptr;
-    CK(cudaMalloc(&d_err, sizeof(int32_t) * count));
-    std::vector<long long> off(count);
-    std::vector<int32_t> e(count, 0);
-    cudaError_t ce = cudaMemsetAsync(d_err, 0, sizeof(int32_t) * count, stream);
-    long long o = 0;
-    for (int k = 0; k < count && ce == cudaSuccess && rc == DEM_OK; ++k) {
-        off[k] = o;
-        o += sh[idx[k]].n;
-        rc = stage_copy(idx[k], scs[k], off[k], d_err + k);
-    }
-    if (ce == cudaSuccess && rc == DEM_OK)
-        ce = cudaMemcpyAsync(e.data(), d_err, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, stream);
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
-    cudaFree(d_err);
-    if (ce != cudaSuccess) return fail(DEM_E_CUDA, cudaGetErrorString(ce));
-    if (rc) return rc;
-    for (int k = 0; k < count; ++k)
-        if (e[k]) {
-            rc = stage_error(e[k]);
+        int rc = layout_fits(idx[k], probes[k]);
+        if (rc) {
             err += " (scene " + std::to_string(idx[k]) + ")";
             return rc;
         }
-    for (int k = 0; k < count; ++k) {
-        rc = stage_commit(idx[k], scs[k], off[k]);
-        if (rc) return rc;
-        rc = push_par(idx[k]);
-        if (rc) return rc;
     }
+    // the transfer's items: scenes with particles, packed in call order
+    std::vector<StageItem> tab;
+    std::vector<int> tab_k;
+    long long total = 0;
+    for (int k = 0; k < count; ++k) {
+        const SceneHost &h = sh[idx[k]];
+        if (h.n <= 0) continue;
+        tab.push_back(StageItem{total, h.particle_base, h.n, idx[k], h.n_mat, h.n_bonds, scs[k]->data ? 1 : 0,
+                                probes[k].r_big, 0});
+        tab_k.push_back(k);
+        total += h.n;
+    }
+    const int nt = (int)tab.size();
+    int rc = ensure_ref(std::max(total, 1LL));
+    if (rc) return rc;
+    rc = ensure_items(std::max(nt, 1));
+    if (rc) return rc;
+    PinMap pm;
+    const size_t o_fields = pm.take((size_t)ref_cap * REF_WORDS * 4);
+    const size_t o_items = pm.take(sizeof(StageItem) * (size_t)std::max(nt, 1));
+    const size_t o_err = pm.take(4 * (size_t)std::max(nt, 1));
+    const size_t o_bst = pm.take(4 * (size_t)d.B), o_blen = pm.take(4 * (size_t)d.B);
+    const size_t o_bstr = pm.take(8 * (size_t)d.B), o_bang = pm.take(4 * (size_t)d.B);
+    const size_t o_mats = pm.take(sizeof(Mat) * (size_t)d.M), o_pair = pm.take(8 * (size_t)d.MP);
+    const size_t o_par = pm.take(sizeof(ScenePar) * sh.size());
+    rc = ensure_pin(pm.bytes);
+    if (rc) return rc;
+    char *pb = static_cast<char *>(pin);
+    float *hp = reinterpret_cast<float *>(pb + o_fields);
+    std::memcpy(pb + o_items, tab.data(), sizeof(StageItem) * nt);
+    int32_t *h_err = reinterpret_cast<int32_t *>(pb + o_err);
+    int32_t *h_bst = reinterpret_cast<int32_t *>(pb + o_bst);
+    float *h_blen = reinterpret_cast<float *>(pb + o_blen);
+    float2 *h_bstr = reinterpret_cast<float2 *>(pb + o_bstr);
+    int32_t *h_bang = reinterpret_cast<int32_t *>(pb + o_bang);
+    Mat *h_mats = reinterpret_cast<Mat *>(pb + o_mats);
+    float2 *h_pair = reinterpret_cast<float2 *>(pb + o_pair);
+    ScenePar *h_par = reinterpret_cast<ScenePar *>(pb + o_par);
+
+    // chunks: each field over all items (contacts in 8 groups), then the
+    // bonds and materials of every scene
+    struct Chunk {
+        int f, i0, i1;
+    };
+    std::vector<Chunk> chunks;
+    std::vector<long long> sizes;
+    for (int f = 0; f < N_REF_FIELDS && nt > 0; ++f)
+        for (const auto &g : split_items(tab, f == F_CONTACTS ? 8 : 1)) {
+            chunks.push_back(Chunk{f, g.first, g.second});
+            sizes.push_back(g.second - g.first);
+        }
+    chunks.push_back(Chunk{-1, 0, count});
+    sizes.push_back(count);
+    HostPipe pipe(sizes, false);
+    pipe.start([&](int c, long long u) {
+        const Chunk &ch = chunks[c];
+        if (ch.f >= 0) {
+            const int i = ch.i0 + (int)u;
+            const void *src = scene_field(scs[tab_k[i]], ch.f);
+            if (!src) return;
+            const RefField &F = REF_FIELDS[ch.f];
+            std::memcpy(hp + F.base * ref_cap + F.per * tab[i].off, src, sizeof(float) * F.per * (size_t)tab[i].n);
+            return;
+        }
+        const int k = (int)u;
+        const SceneHost &h = sh[idx[k]];
+        if (h.n_bonds > 0)
+            split_bonds(h, scs[k]->bonds, h_bst + h.bond_base, h_blen + h.bond_base, h_bstr + h.bond_base,
+                        h_bang + h.bond_base);
+        material_tables(scs[k]->materials, h.n_mat, h_mats + h.mat_base, h_pair + h.pair_base);
+    });
+    float *dp0 = static_cast<float *>(ref_block);
+    cudaError_t ce = cudaSuccess;
+    for (int c = 0; c < (int)chunks.size(); ++c) {
+        pipe.wait_chunk(c);
+        const Chunk &ch = chunks[c];
+        if (ch.f < 0 || ce != cudaSuccess) continue;
+        const RefField &F = REF_FIELDS[ch.f];
+        const long long o0 = tab[ch.i0].off, o1 = tab[ch.i1 - 1].off + tab[ch.i1 - 1].n;
+        ce = cudaMemcpyAsync(dp0 + F.base * ref_cap + F.per * o0, hp + F.base * ref_cap + F.per * o0,
+                             sizeof(float) * F.per * (size_t)(o1 - o0), cudaMemcpyHostToDevice, stream);
+    }
+    pipe.join();
+    if (ce == cudaSuccess && nt > 0) {
+        ce = cudaMemcpyAsync(d_items, pb + o_items, sizeof(StageItem) * nt, cudaMemcpyHostToDevice, stream);
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(d_item_err, 0, 4 * (size_t)nt, stream);
+        if (ce == cudaSuccess) {
+            launch_stage_check(ref, d_items, nt, total, d_item_err, stream);
+            ce = cudaGetLastError();
+        }
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(h_err, d_item_err, 4 * (size_t)nt, cudaMemcpyDeviceToHost, stream);
+    }
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+    if (ce != cudaSuccess) return fail(DEM_E_CUDA, cudaGetErrorString(ce));
+    for (int i = 0; i < nt; ++i)
+        if (h_err[i]) {
+            rc = stage_error(h_err[i]);
+            err += " (scene " + std::to_string(tab[i].scene) + ")";
+            return rc;
+        }
+    // every scene passed: adopt, convert, and send bonds, materials, parameters
+    std::vector<std::pair<long long, long long>> rb, rm, rp, rs;
+    for (int k = 0; k < count; ++k) {
+        const int s = idx[k];
+        SceneHost &h = sh[s];
+        apply_layout(s, probes[k]);
+        h.materials.assign(scs[k]->materials, scs[k]->materials + 6 * (size_t)h.n_mat);
+        h.bond_angle.assign(h_bang + h.bond_base, h_bang + h.bond_base + h.n_bonds);
+        fill_par(h);
+        h_par[s] = h.par;
+        rb.emplace_back(h.bond_base, h.n_bonds);
+        rm.emplace_back(h.mat_base, h.n_mat);
+        rp.emplace_back(h.pair_base, (long long)h.n_mat * h.n_mat);
+        rs.emplace_back(s, 1);
+    }
+    launch_stage_in(d, ref, d_items, nt, total, stream);
+    CK(cudaGetLastError());
+    auto send = [&](void *dst, const void *src, size_t elem, const std::vector<std::pair<long long, long long>> &r) {
+        for (const auto &x : merge_runs(r)) {
+            cudaError_t e2 = cudaMemcpyAsync(static_cast<char *>(dst) + elem * x.first,
+                                             static_cast<const char *>(src) + elem * x.first, elem * x.second,
+                                             cudaMemcpyHostToDevice, stream);
+            if (e2 != cudaSuccess) return e2;
+        }
+        return cudaSuccess;
+    };
+    CK(send(d.b_status, h_bst, 4, rb));
+    CK(send(d.b_length, h_blen, 4, rb));
+    CK(send(d.b_str, h_bstr, 8, rb));
+    CK(send(d.mats, h_mats, sizeof(Mat), rm));
+    CK(send(d.pair, h_pair, 8, rp));
+    CK(send(d.par, h_par, sizeof(ScenePar), rs));
+    CK(cudaStreamSynchronize(stream));  // the pinned block is reused by the next transfer
     return force_rebuild();
 }
 
@@ -928,9 +1242,9 @@ int World::upload_scene(int s, const dem_scene *sc) {
     SceneHost probe = h;
     int rc = compute_layout(probe, sc);
     if (rc) return rc;
-    rc = adopt_layout(s, probe);
+    rc = layout_fits(s, probe);
     if (rc) return rc;
-    rc = stage_scene(s, sc);
+    rc = stage_scene(s, sc, &probe);
     if (rc) return rc;
     rc = push_par(s);
     if (rc) return rc;
@@ -1243,130 +1557,176 @@ int World::sync() {
     return DEM_OK;
 }
 
-// the reference layouts of scene s into the staging block at `off`
-// (err: its check word)
-void World::unstage_launch(int s, long long off, int32_t *err) {
-    const SceneHost &h = sh[s];
-    if (h.n > 0) launch_stage_out(d, ref_at(off), h.particle_base, h.n, err, stream);
-}
-
-// staged scene -> caller's arrays; bst/blen hold the scene's bond status and
-// length words
-int World::unstage_copy(int s, long long off, dem_scene *out, const int32_t *bst, const float *blen) {
-    const SceneHost &h = sh[s];
-    const int n = h.n, base = h.particle_base;
-    if (n > 0) {
-        const RefArrays r = ref_at(off);
-        auto dn = [&](void *dst, const void *src, size_t words) -> cudaError_t {
-            if (!dst) return cudaSuccess;
-            return cudaMemcpyAsync(dst, src, words * 4, cudaMemcpyDeviceToHost, stream);
-        };
-        const size_t un = (size_t)n;
-        CK(dn(out->pos, r.pos, 2 * un));
-        CK(dn(out->radii, r.radii, un));
-        CK(dn(out->rot, r.rot, un));
-        CK(dn(out->vel, r.vel, 2 * un));
-        CK(dn(out->rot_vel, r.rot_vel, un));
-        CK(dn(out->acc, r.acc, 2 * un));
-        CK(dn(out->rot_acc, r.rot_acc, un));
-        CK(dn(out->del_pos, r.del_pos, 2 * un));
-        CK(dn(out->del_rot, r.del_rot, un));
-        CK(dn(out->data, r.data, 7 * un));
-        CK(dn(out->contacts, r.contacts, 84 * un));
-        CK(dn(out->fixity, d.fix_ref + 6 * (size_t)base, 6 * un));
-        CK(dn(out->forces, d.force_ref + 6 * (size_t)base, 6 * un));
-        CK(dn(out->material_pointers, d.matp_ref + base, un));
-    }
-    if (out->materials && out->n_materials == h.n_mat)
-        std::memcpy(out->materials, h.materials.data(), h.materials.size() * 4);
-    if (out->bonds && out->n_bonds == h.n_bonds) {
-        for (int k = 0; k < h.n_bonds; ++k) {
-            out->bonds[3 * k] = bst[k];
-            out->bonds[3 * k + 1] = h.bond_angle[k];
-            out->bonds[3 * k + 2] = f2bits(blen[k]);
-        }
-    }
-    control(s, out->coll_cont);
-    out->grid = h.grid;
-    return DEM_OK;
-}
-
 int World::unstage_error(int32_t e) {
     if (e & 16) return fail(DEM_E_STATE, "internal particle map is corrupt");
     if (e & 32) return fail(DEM_E_STATE, "contact partner outside its scene");
     return DEM_OK;
 }
 
+// One scene: converted into the staging block, then copied straight into
+// the caller's arrays.
 int World::download_scene(int s, dem_scene *out) {
     if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
     if (!out) return fail(DEM_E_INVALID, "out is NULL");
-    const SceneHost &h = sh[s];
-    if (out->n_particles != h.n) return fail(DEM_E_INVALID, "out->n_particles must match the scene");
-    int rc = ensure_ref(h.n);
-    if (rc) return rc;
-    std::vector<int32_t> bst(h.n_bonds);
-    std::vector<float> blen(h.n_bonds);
-    CK(cudaMemsetAsync(ref_err, 0, 4, stream));
-    unstage_launch(s, 0, ref_err);
-    int32_t e = 0;
-    CK(cudaMemcpyAsync(&e, ref_err, 4, cudaMemcpyDeviceToHost, stream));
-    if (h.n_bonds > 0) {
-        CK(cudaMemcpyAsync(bst.data(), d.b_status + h.bond_base, 4 * (size_t)h.n_bonds, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(blen.data(), d.b_length + h.bond_base, 4 * (size_t)h.n_bonds, cudaMemcpyDeviceToHost, stream));
-    }
-    CK(cudaStreamSynchronize(stream));
-    rc = unstage_error(e);
-    if (rc) return rc;
-    rc = unstage_copy(s, 0, out, bst.data(), blen.data());
-    if (rc) return rc;
-    CK(cudaStreamSynchronize(stream));
-    return DEM_OK;
+    const int32_t one = s;
+    return download_many(&one, &out, 1);
 }
 
-// Many scenes at once (dem_batch_download_many): every scene is converted
-// into the staging block before one synchronisation, then copied out.
+// Many scenes at once (dem_batch_download_many).  One launch converts every
+// scene into the staging block; the block comes back one field at a time
+// into a page-locked block, and host threads copy each field into the
+// callers' arrays as soon as it has landed.  The callers' arrays are written
+// only if every scene's check passed.
 int World::download_many(const int32_t *idx, dem_scene *const *outs, int count) {
     if (count <= 0) return DEM_OK;
     if (!idx || !outs) return fail(DEM_E_INVALID, "scene index/pointer arrays are NULL");
+    std::vector<StageItem> tab;
+    std::vector<int> tab_k;
     long long total = 0;
     for (int k = 0; k < count; ++k) {
         const int s = idx[k];
         if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
-        if (!outs[k] || outs[k]->n_particles != sh[s].n)
+        if (!outs[k]) return fail(DEM_E_INVALID, "out is NULL");
+        const SceneHost &h = sh[s];
+        if (outs[k]->n_particles != h.n)
             return fail(DEM_E_INVALID, "out->n_particles must match the scene (scene " + std::to_string(s) + ")");
-        total += sh[s].n;
+        if (h.n <= 0) continue;
+        tab.push_back(StageItem{total, h.particle_base, h.n, s, h.n_mat, h.n_bonds, 0, h.r_big, 0});
+        tab_k.push_back(k);
+        total += h.n;
     }
-    int rc = ensure_ref(total);
+    const int nt = (int)tab.size();
+    int rc = ensure_ref(std::max(total, 1LL));
     if (rc) return rc;
-    int32_t *d_err = nullptr;
-    CK(cudaMalloc(&d_err, sizeof(int32_t) * count));
-    std::vector<long long> off(count);
-    std::vector<int32_t> e(count, 0);
-    std::vector<int32_t> bst(d.B > 0 ? d.B : 1);
-    std::vector<float> blen(d.B > 0 ? d.B : 1);
-    cudaError_t ce = cudaMemsetAsync(d_err, 0, sizeof(int32_t) * count, stream);
-    long long o = 0;
-    for (int k = 0; k < count; ++k) {
-        off[k] = o;
-        o += sh[idx[k]].n;
-        unstage_launch(idx[k], off[k], d_err + k);
+    rc = ensure_items(std::max(nt, 1));
+    if (rc) return rc;
+    const size_t N = (size_t)d.N;
+    PinMap pm;
+    const size_t o_fields = pm.take((size_t)ref_cap * REF_WORDS * 4);
+    const size_t o_items = pm.take(sizeof(StageItem) * (size_t)std::max(nt, 1));
+    const size_t o_err = pm.take(4 * (size_t)std::max(nt, 1));
+    const size_t o_fix = pm.take(24 * N), o_force = pm.take(24 * N), o_matp = pm.take(4 * N);
+    const size_t o_bst = pm.take(4 * (size_t)d.B), o_blen = pm.take(4 * (size_t)d.B);
+    rc = ensure_pin(pm.bytes);
+    if (rc) return rc;
+    char *pb = static_cast<char *>(pin);
+    float *hp = reinterpret_cast<float *>(pb + o_fields);
+    std::memcpy(pb + o_items, tab.data(), sizeof(StageItem) * nt);
+    const int32_t *h_err = reinterpret_cast<const int32_t *>(pb + o_err);
+    const int32_t *h_fix = reinterpret_cast<const int32_t *>(pb + o_fix);
+    const float *h_force = reinterpret_cast<const float *>(pb + o_force);
+    const int32_t *h_matp = reinterpret_cast<const int32_t *>(pb + o_matp);
+    const int32_t *h_bst = reinterpret_cast<const int32_t *>(pb + o_bst);
+    const float *h_blen = reinterpret_cast<const float *>(pb + o_blen);
+
+    struct Chunk {
+        int f, i0, i1;
+    };
+    std::vector<Chunk> chunks;
+    std::vector<long long> sizes;
+    for (int f = 0; f < N_REF_FIELDS && nt > 0; ++f) {
+        if (!OUT_FIELD[f]) continue;
+        for (const auto &g : split_items(tab, f == F_CONTACTS ? 8 : 1)) {
+            chunks.push_back(Chunk{f, g.first, g.second});
+            sizes.push_back(g.second - g.first);
+        }
     }
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(e.data(), d_err, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, stream);
-    if (ce == cudaSuccess && d.B > 0)
-        ce = cudaMemcpyAsync(bst.data(), d.b_status, 4 * (size_t)d.B, cudaMemcpyDeviceToHost, stream);
-    if (ce == cudaSuccess && d.B > 0)
-        ce = cudaMemcpyAsync(blen.data(), d.b_length, 4 * (size_t)d.B, cudaMemcpyDeviceToHost, stream);
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
-    cudaFree(d_err);
-    if (ce != cudaSuccess) return fail(DEM_E_CUDA, cudaGetErrorString(ce));
-    for (int k = 0; k < count; ++k)
-        if (e[k]) return unstage_error(e[k]);
+    chunks.push_back(Chunk{-1, 0, count});
+    sizes.push_back(count);
+    rc = ensure_events((int)chunks.size());
+    if (rc) return rc;
+
+    // the conversion and its check words, then every chunk's copy and event
+    if (nt > 0) {
+        CK(cudaMemcpyAsync(d_items, pb + o_items, sizeof(StageItem) * nt, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemsetAsync(d_item_err, 0, 4 * (size_t)nt, stream));
+        launch_stage_out(d, ref, d_items, nt, total, d_item_err, stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(pb + o_err, d_item_err, 4 * (size_t)nt, cudaMemcpyDeviceToHost, stream));
+    }
+    float *dp0 = static_cast<float *>(ref_block);
+    std::vector<std::pair<long long, long long>> rn, rb;
     for (int k = 0; k < count; ++k) {
         const SceneHost &h = sh[idx[k]];
-        rc = unstage_copy(idx[k], off[k], outs[k], bst.data() + h.bond_base, blen.data() + h.bond_base);
-        if (rc) return rc;
+        rn.emplace_back(h.particle_base, h.n);
+        rb.emplace_back(h.bond_base, h.n_bonds);
     }
-    CK(cudaStreamSynchronize(stream));
+    rn = merge_runs(rn);
+    rb = merge_runs(rb);
+    for (int c = 0; c < (int)chunks.size(); ++c) {
+        const Chunk &ch = chunks[c];
+        if (ch.f >= 0) {
+            const RefField &F = REF_FIELDS[ch.f];
+            const long long o0 = tab[ch.i0].off, o1 = tab[ch.i1 - 1].off + tab[ch.i1 - 1].n;
+            CK(cudaMemcpyAsync(hp + F.base * ref_cap + F.per * o0, dp0 + F.base * ref_cap + F.per * o0,
+                               sizeof(float) * F.per * (size_t)(o1 - o0), cudaMemcpyDeviceToHost, stream));
+        } else {
+            for (const auto &x : rn) {
+                CK(cudaMemcpyAsync(pb + o_fix + 24 * x.first, d.fix_ref + 6 * x.first, 24 * x.second,
+                                   cudaMemcpyDeviceToHost, stream));
+                CK(cudaMemcpyAsync(pb + o_force + 24 * x.first, d.force_ref + 6 * x.first, 24 * x.second,
+                                   cudaMemcpyDeviceToHost, stream));
+                CK(cudaMemcpyAsync(pb + o_matp + 4 * x.first, d.matp_ref + x.first, 4 * x.second,
+                                   cudaMemcpyDeviceToHost, stream));
+            }
+            for (const auto &x : rb) {
+                CK(cudaMemcpyAsync(pb + o_bst + 4 * x.first, d.b_status + x.first, 4 * x.second,
+                                   cudaMemcpyDeviceToHost, stream));
+                CK(cudaMemcpyAsync(pb + o_blen + 4 * x.first, d.b_length + x.first, 4 * x.second,
+                                   cudaMemcpyDeviceToHost, stream));
+            }
+        }
+        CK(cudaEventRecord(xfer_ev[c], stream));
+    }
+    HostPipe pipe(sizes, true);
+    pipe.start([&](int c, long long u) {
+        const Chunk &ch = chunks[c];
+        if (ch.f >= 0) {
+            const int i = ch.i0 + (int)u;
+            dem_scene *out = outs[tab_k[i]];
+            void *dst = const_cast<void *>(scene_field(out, ch.f));
+            if (!dst) return;
+            const RefField &F = REF_FIELDS[ch.f];
+            std::memcpy(dst, hp + F.base * ref_cap + F.per * tab[i].off, sizeof(float) * F.per * (size_t)tab[i].n);
+            return;
+        }
+        const int k = (int)u, s = idx[k];
+        const SceneHost &h = sh[s];
+        dem_scene *out = outs[k];
+        const size_t n = (size_t)h.n, base = (size_t)h.particle_base;
+        if (out->fixity && n) std::memcpy(out->fixity, h_fix + 6 * base, 24 * n);
+        if (out->forces && n) std::memcpy(out->forces, h_force + 6 * base, 24 * n);
+        if (out->material_pointers && n) std::memcpy(out->material_pointers, h_matp + base, 4 * n);
+        if (out->materials && out->n_materials == h.n_mat)
+            std::memcpy(out->materials, h.materials.data(), h.materials.size() * 4);
+        if (out->bonds && out->n_bonds == h.n_bonds)
+            for (int q = 0; q < h.n_bonds; ++q) {
+                out->bonds[3 * q] = h_bst[h.bond_base + q];
+                out->bonds[3 * q + 1] = h.bond_angle[q];
+                out->bonds[3 * q + 2] = f2bits(h_blen[h.bond_base + q]);
+            }
+        control(s, out->coll_cont);
+        out->grid = h.grid;
+    });
+    for (int c = 0; c < (int)chunks.size(); ++c) {
+        const cudaError_t ce = cudaEventSynchronize(xfer_ev[c]);
+        if (ce != cudaSuccess) {
+            pipe.cancel();
+            pipe.join();
+            return fail(DEM_E_CUDA, cudaGetErrorString(ce));
+        }
+        if (c == 0)
+            for (int i = 0; i < nt; ++i)
+                if (h_err[i]) {
+                    pipe.cancel();
+                    pipe.join();
+                    rc = unstage_error(h_err[i]);
+                    err += " (scene " + std::to_string(tab[i].scene) + ")";
+                    return rc;
+                }
+        pipe.release(c);
+    }
+    pipe.join();
     return DEM_OK;
 }
 

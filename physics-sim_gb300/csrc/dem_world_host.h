@@ -132,7 +132,7 @@ class World {
     void fill_par(SceneHost &h);
     int push_par(int s);
     int push_det();
-    int stage_scene(int s, const dem_scene *scene);
+    int stage_scene(int s, const dem_scene *scene, const SceneHost *probe);
     int force_rebuild();
     void enqueue_plain_step(bool first, bool last);
     void enqueue_rebuild(cudaStream_t st, const int32_t *gate);
@@ -144,15 +144,21 @@ class World {
     RefArrays ref{};
     void *ref_block = nullptr;
     long long ref_cap = 0;
-    int32_t *ref_err = nullptr;
     int ensure_ref(long long n);
+    void *pin = nullptr;               // page-locked staging of the bulk transfers
+    size_t pin_bytes = 0;
+    int ensure_pin(size_t bytes);
+    // the item table of a staging transfer and one check word per item
+    StageItem *d_items = nullptr;
+    int32_t *d_item_err = nullptr;
+    int items_cap = 0;
+    int ensure_items(int count);
+    std::vector<cudaEvent_t> xfer_ev;  // one per chunk of a pipelined download
+    int ensure_events(int count);
     RefArrays ref_at(long long off) const;
-    int stage_copy(int s, const dem_scene *sc, long long off, int32_t *err);
     int stage_error(int32_t e);
-    int stage_commit(int s, const dem_scene *sc, long long off);
-    int adopt_layout(int s, const SceneHost &probe);
-    void unstage_launch(int s, long long off, int32_t *err);
-    int unstage_copy(int s, long long off, dem_scene *out, const int32_t *bst, const float *blen);
+    int layout_fits(int s, const SceneHost &probe);
+    void apply_layout(int s, const SceneHost &probe);
     int unstage_error(int32_t e);
     // captured graphs, one per buffer parity at their start (a graph of R
     // steps swaps the pr/dp/rr buffers R - 1 times)

@@ -66,11 +66,15 @@ class Ext(C.Structure):
 
 
 class Scene(C.Structure):
+    # array fields are plain addresses (float* / int32_t* in dem.h): setting
+    # an int is several times cheaper than building a ctypes pointer, which
+    # matters when hundreds of scenes are marshalled per call
     _fields_ = [("n_particles", C.c_int32), ("n_bonds", C.c_int32), ("n_materials", C.c_int32),
-                ("pos", _FP), ("radii", _FP), ("vel", _FP), ("acc", _FP), ("rot", _FP),
-                ("rot_vel", _FP), ("rot_acc", _FP), ("forces", _FP), ("fixity", _IP),
-                ("del_pos", _FP), ("del_rot", _FP), ("bonds", _IP), ("contacts", _IP),
-                ("material_pointers", _IP), ("materials", _FP), ("data", _FP),
+                ("pos", C.c_void_p), ("radii", C.c_void_p), ("vel", C.c_void_p), ("acc", C.c_void_p),
+                ("rot", C.c_void_p), ("rot_vel", C.c_void_p), ("rot_acc", C.c_void_p),
+                ("forces", C.c_void_p), ("fixity", C.c_void_p), ("del_pos", C.c_void_p),
+                ("del_rot", C.c_void_p), ("bonds", C.c_void_p), ("contacts", C.c_void_p),
+                ("material_pointers", C.c_void_p), ("materials", C.c_void_p), ("data", C.c_void_p),
                 ("coll_cont", C.c_int32 * 4), ("grid", GridInfo)]
 
 
@@ -289,11 +293,10 @@ def make_scene(sc):
     s.n_bonds = int(sc["bonds"].shape[0] // 3)
     s.n_materials = int(sc["materials"].shape[0] // 6)
     for k in F32_KEYS:
-        setattr(s, k, sc[k].ctypes.data_as(_FP))
+        setattr(s, k, sc[k].__array_interface__["data"][0])
     for k in I32_KEYS:
-        setattr(s, k, sc[k].ctypes.data_as(_IP))
-    for i in range(4):
-        s.coll_cont[i] = int(sc["coll_cont"][i])
+        setattr(s, k, sc[k].__array_interface__["data"][0])
+    s.coll_cont[:] = [int(v) for v in sc["coll_cont"]]
     cs, cap, w, h = sc["grid"]
     s.grid.cell_size = float(cs)
     s.grid.cell_cap = int(cap)
