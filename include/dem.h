@@ -105,7 +105,11 @@ typedef struct dem_ext {
     int32_t unfused_lom;              /* 1: every step runs its own LOM kernel instead of the next
                                          step's LOM pass running inside the Simulation kernel (the
                                          default, fewer bytes per step); results do not depend on it */
-    int32_t reserved[3];
+    int32_t host_copies;              /* 0: transfers read and write the caller's arrays directly from the
+                                         device where it reaches pageable host memory through the host's
+                                         page tables (Grace), else through a page-locked block; 1: always
+                                         through the page-locked block */
+    int32_t reserved[2];
 } dem_ext;
 
 /* One scene in the reference's host layouts (state.rs:69-93).  Arrays hold

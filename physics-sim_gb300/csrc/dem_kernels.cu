@@ -1397,7 +1397,9 @@ __global__ void k_stage_check(RefArrays r, const StageItem *__restrict__ it, int
     if (u >= total * K) return;
     const long long t = u / K;
     const int k = item_from(it, count, s_k0, t);
-    const int n = it[k].n, i = (int)(t - it[k].off);
+    const int n = it[k].n;
+    const long long i = t - it[k].off;
+    if (i < 0 || i >= n) return;  // padding between items
     const int32_t *c = r.contacts + u * 6;
     int e = 0;
     if (c[5] >= it[k].n_bonds) e |= 2;
@@ -1428,8 +1430,9 @@ __device__ __forceinline__ void tile_items(const StageItem *it, int count, long 
     if (threadIdx.x < np) {
         const long long t = t0 + threadIdx.x;
         const int k = item_from(it, count, s_k0, t);
+        const long long i = t - it[k].off;
         s_item[threadIdx.x] = k;
-        s_g[threadIdx.x] = it[k].base + (int)(t - it[k].off);
+        s_g[threadIdx.x] = (i >= 0 && i < it[k].n) ? it[k].base + (int)i : -1;  // -1: padding
     }
 }
 
@@ -1447,7 +1450,7 @@ __global__ void __launch_bounds__(ST_THREADS) k_stage_in(DevWorld w, RefArrays r
     // slot rows (slot j, particle p), p fastest
     for (int q = threadIdx.x; q < K * ST_P; q += ST_THREADS) {
         const int j = q / ST_P, p = q % ST_P;
-        if (p >= np) continue;
+        if (p >= np || s_g[p] < 0) continue;
         const int32_t *c = cont + p * ST_REC + 6 * j;
         const size_t at = (size_t)j * w.N + s_g[p];
         const int b = c[1];
@@ -1457,7 +1460,7 @@ __global__ void __launch_bounds__(ST_THREADS) k_stage_in(DevWorld w, RefArrays r
         w.s_thb[at] = __int_as_float(c[4]);
         w.s_bonded[at] = c[5];
     }
-    if (threadIdx.x >= np) return;
+    if (threadIdx.x >= np || s_g[threadIdx.x] < 0) return;
     const int p = threadIdx.x;
     const StageItem I = it[s_item[p]];
     const long long t = t0 + p;
@@ -1533,14 +1536,17 @@ __global__ void __launch_bounds__(ST_THREADS) k_stage_out(DevWorld w, RefArrays 
     tile_items(it, count, t0, np, s_item, s_g);
     if (threadIdx.x < np) {
         const int k = s_item[threadIdx.x], g = s_g[threadIdx.x];
-        const int o = w.orig[g];
-        if (o < 0 || o >= it[k].n) {
+        const int o = g < 0 ? -1 : w.orig[g];
+        if (g < 0) {
+            s_o[threadIdx.x] = -1;  // padding
+        } else if (o < 0 || o >= it[k].n) {
             atomicOr(err + k, 16);
+            atomicOr(err + count, 16);
             s_o[threadIdx.x] = -1;
         } else {
             s_o[threadIdx.x] = o;
         }
-        s_mask[threadIdx.x] = w.smask[g];
+        s_mask[threadIdx.x] = g < 0 ? 0u : w.smask[g];
     }
     __syncthreads();
     for (int q = threadIdx.x; q < K * ST_P; q += ST_THREADS) {
@@ -1554,6 +1560,7 @@ __global__ void __launch_bounds__(ST_THREADS) k_stage_out(DevWorld w, RefArrays 
             const int base = it[s_item[p]].base, n = it[s_item[p]].n;
             if (pb < base || pb >= base + n) {
                 atomicOr(err + s_item[p], 32);
+                atomicOr(err + count, 32);
                 c[0] = -1;
                 c[1] = -1;
             } else {
@@ -1610,6 +1617,52 @@ void launch_stage_out(const DevWorld &w, const RefArrays &r, const StageItem *it
                       int32_t *err, cudaStream_t st) {
     if (total <= 0 || count <= 0) return;
     k_stage_out<<<(unsigned)((total + ST_P - 1) / ST_P), ST_THREADS, 0, st>>>(w, r, items, count, total, err);
+}
+
+// one block per piece; 16-byte words where both ends allow, else 4-byte
+// words, both coalesced
+constexpr int COPY_THREADS = 256;
+__global__ void __launch_bounds__(COPY_THREADS) k_copies(const HostCopy *__restrict__ c, int n,
+                                                          const int32_t *guard) {
+    if (guard && *guard) return;
+    __shared__ int s_k;
+    const long long b = blockIdx.x;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = n - 1;  // last copy with piece0 <= b
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (c[mid].piece0 <= b) lo = mid;
+            else hi = mid - 1;
+        }
+        s_k = lo;
+    }
+    __syncthreads();
+    const HostCopy C = c[s_k];
+    const long long at = (b - C.piece0) * COPY_PIECE;
+    const long long len = min(COPY_PIECE, C.bytes - at);
+    if (len <= 0) return;
+    const char *src = C.src + at;
+    char *dst = C.dst + at;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+        const int n16 = (int)(len >> 4);
+        const int4 *s4 = reinterpret_cast<const int4 *>(src);
+        int4 *d4 = reinterpret_cast<int4 *>(dst);
+#pragma unroll 4
+        for (int i = threadIdx.x; i < n16; i += COPY_THREADS) d4[i] = s4[i];
+        for (long long i = ((long long)n16 << 4) + 4 * threadIdx.x; i < len; i += 4 * COPY_THREADS)
+            *reinterpret_cast<int32_t *>(dst + i) = *reinterpret_cast<const int32_t *>(src + i);
+    } else {
+        const int n4 = (int)(len >> 2);
+        const int32_t *s1 = reinterpret_cast<const int32_t *>(src);
+        int32_t *d1 = reinterpret_cast<int32_t *>(dst);
+#pragma unroll 4
+        for (int i = threadIdx.x; i < n4; i += COPY_THREADS) d1[i] = s1[i];
+    }
+}
+
+void launch_copies(const HostCopy *c, int n, long long pieces, const int32_t *guard, cudaStream_t st) {
+    if (n <= 0 || pieces <= 0) return;
+    k_copies<<<(unsigned)pieces, COPY_THREADS, 0, st>>>(c, n, guard);
 }
 
 // ------------------------------------------------------- Fix / Drop / Release

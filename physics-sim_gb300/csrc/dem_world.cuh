@@ -220,7 +220,8 @@ struct RefArrays {
 };
 // One scene of a staging transfer: particles [off, off + n) of the staging
 // block are particles [base, base + n) of the world, which hold scene `scene`.
-// A transfer's items are packed: off of item k+1 = off + n of item k, n > 0.
+// A transfer's items are sorted by off and do not overlap; n > 0.  Staged
+// positions between items (padding) belong to no item and are skipped.
 struct StageItem {
     long long off;
     int base, n, scene, n_mat, n_bonds, has_data;
@@ -237,9 +238,24 @@ void launch_stage_check(const RefArrays &r, const StageItem *items, int count, l
 void launch_stage_in(const DevWorld &w, const RefArrays &r, const StageItem *items, int count, long long total,
                      cudaStream_t st);
 // internal layout -> reference layout; err[k] bits: 16 internal map corrupt,
-// 32 contact partner outside the scene
+// 32 contact partner outside the scene; err[count] = OR of all
 void launch_stage_out(const DevWorld &w, const RefArrays &r, const StageItem *items, int count, long long total,
                       int32_t *err, cudaStream_t st);
+
+// One contiguous copy of a transfer, between the caller's host memory and
+// the device (through the device's access to pageable host memory) or
+// within the device; bytes a multiple of 4, both ends 4-byte aligned.  It
+// runs as pieces of COPY_PIECE bytes; piece0 = pieces of the copies before.
+constexpr long long COPY_PIECE = 65536;
+struct HostCopy {
+    const char *src;
+    char *dst;
+    long long bytes;
+    long long piece0;
+};
+// every piece of copies c[0..n) (`pieces` in all); nothing if guard != NULL
+// and *guard != 0
+void launch_copies(const HostCopy *c, int n, long long pieces, const int32_t *guard, cudaStream_t st);
 
 // Fix / Drop / Release events (src/shaders/event_handling/{Fix,Drop,Release}.wgsl)
 // on `count` particles of the scene whose first particle is `base`, given

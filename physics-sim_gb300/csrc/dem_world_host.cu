@@ -78,6 +78,7 @@ World::~World() {
     if (ref_block) cudaFree(ref_block);
     if (pin) cudaFreeHost(pin);
     if (d_items) cudaFree(d_items);
+    if (d_copies) cudaFree(d_copies);
     for (auto e : xfer_ev) cudaEventDestroy(e);
     if (side) cudaStreamDestroy(side);
 }
@@ -89,7 +90,7 @@ int World::ensure_ref(long long n) {
     if (ref_block) cudaFree(ref_block);
     ref_block = nullptr;
     ref_cap = 0;
-    const long long cap = std::max(n, 1024LL);
+    const long long cap = (std::max(n, 1024LL) + 63) & ~63LL;  // every field 256-byte aligned
     const size_t words = (size_t)cap * 117 + 64;
     if (cudaMalloc(&ref_block, words * 4) != cudaSuccess) {
         ref_block = nullptr;
@@ -151,6 +152,17 @@ const void *scene_field(const dem_scene *sc, int f) {
         case 12: return sc->contacts;
         default: return sc->material_pointers;
     }
+}
+
+// the device reads and writes pageable host memory through the host's page
+// tables (hardware-coherent hosts such as Grace)
+bool device_reads_pageable() {
+    int dev = 0, a = 0, b = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess)
+        return false;
+    return a == 1 && b == 1;
 }
 
 // cores this process may run on
@@ -303,6 +315,30 @@ void material_tables(const float *materials, int M, Mat *mats, float2 *pair) {
         }
 }
 
+// appends one copy of `bytes` to a direct transfer's table; returns the
+// pieces so far
+long long add_copy(HostCopy *tab, int &n, const void *src, void *dst, long long bytes, long long pieces) {
+    if (bytes <= 0 || !src || !dst) return pieces;
+    tab[n++] = HostCopy{static_cast<const char *>(src), static_cast<char *>(dst), bytes, pieces};
+    return pieces + (bytes + COPY_PIECE - 1) / COPY_PIECE;
+}
+
+// a transfer's items: the scenes with particles in call order, each starting
+// on a multiple of 4 particles (every field of every item 16-byte aligned)
+long long pack_items(const std::vector<SceneHost> &sh, const int32_t *idx, int count, std::vector<StageItem> &tab,
+                     std::vector<int> &tab_k) {
+    long long total = 0;
+    for (int k = 0; k < count; ++k) {
+        const SceneHost &h = sh[idx[k]];
+        if (h.n <= 0) continue;
+        const long long off = (total + 3) & ~3LL;
+        tab.push_back(StageItem{off, h.particle_base, h.n, idx[k], h.n_mat, h.n_bonds, 0, h.r_big, 0});
+        tab_k.push_back(k);
+        total = off + h.n;
+    }
+    return total;
+}
+
 // a scene's bond records [status, angle, length bits] split into the
 // device arrays' words (strengths from the scene's per-bond values, else 0)
 void split_bonds(const SceneHost &h, const int32_t *bonds, int32_t *st, float *len, float2 *str, int32_t *ang) {
@@ -329,20 +365,33 @@ int World::ensure_pin(size_t bytes) {
     return DEM_OK;
 }
 
-// device table of a transfer's items and their check words (grows, kept)
-int World::ensure_items(int count) {
-    if (count <= items_cap && d_items) return DEM_OK;
-    if (d_items) cudaFree(d_items);
-    d_items = nullptr;
-    d_item_err = nullptr;
-    items_cap = 0;
-    const int cap = std::max(count, 64);
-    void *p = nullptr;
-    if (cudaMalloc(&p, (size_t)cap * (sizeof(StageItem) + 4)) != cudaSuccess)
-        return fail(DEM_E_OOM, "staging table allocation failed");
-    d_items = static_cast<StageItem *>(p);
-    d_item_err = reinterpret_cast<int32_t *>(d_items + cap);
-    items_cap = cap;
+// device tables of a transfer: its items with one check word each (plus
+// their OR), and its direct copies (grow, kept)
+int World::ensure_tables(int items, int copies) {
+    if (items > items_cap || !d_items) {
+        if (d_items) cudaFree(d_items);
+        d_items = nullptr;
+        d_item_err = nullptr;
+        items_cap = 0;
+        const int cap = std::max(items, 64);
+        void *p = nullptr;
+        if (cudaMalloc(&p, (size_t)cap * (sizeof(StageItem) + 4)) != cudaSuccess)
+            return fail(DEM_E_OOM, "staging table allocation failed");
+        d_items = static_cast<StageItem *>(p);
+        d_item_err = reinterpret_cast<int32_t *>(d_items + cap);
+        items_cap = cap;
+    }
+    if (copies > copies_cap || !d_copies) {
+        if (d_copies) cudaFree(d_copies);
+        d_copies = nullptr;
+        copies_cap = 0;
+        const int cap = std::max(copies, 1024);
+        if (cudaMalloc(&d_copies, (size_t)cap * sizeof(HostCopy)) != cudaSuccess) {
+            d_copies = nullptr;
+            return fail(DEM_E_OOM, "copy table allocation failed");
+        }
+        copies_cap = cap;
+    }
     return DEM_OK;
 }
 
@@ -722,56 +771,167 @@ int World::stage_error(int32_t e) {
     return DEM_OK;
 }
 
-// One scene, its arrays copied straight from the caller's memory into the
-// staging block and checked there; only then (probe: a re-upload's new
-// layout) is anything of the scene changed, and the block converted.
-int World::stage_scene(int s, const dem_scene *sc, const SceneHost *probe) {
-    SceneHost &h = sh[s];
-    const int n = h.n;
-    if (n > 0) {
-        int rc = ensure_ref(n);
-        if (rc) return rc;
-        rc = ensure_items(1);
-        if (rc) return rc;
-        const StageItem it{0, h.particle_base, n, s, h.n_mat, h.n_bonds, sc->data ? 1 : 0,
-                           probe ? probe->r_big : h.r_big, 0};
-        float *dp0 = static_cast<float *>(ref_block);
-        for (int f = 0; f < N_REF_FIELDS; ++f) {
-            const void *src = scene_field(sc, f);
-            if (!src) continue;
-            const RefField &F = REF_FIELDS[f];
-            CK(cudaMemcpyAsync(dp0 + F.base * ref_cap, src, sizeof(float) * F.per * (size_t)n, cudaMemcpyHostToDevice,
-                               stream));
+// Staging of `count` scenes (idx[k] from scs[k]).  Every scene's arrays go
+// into the staging block -- read by the device straight from the caller's
+// memory (host_direct), else copied by host threads into the page-locked
+// block as it is sent one field at a time -- and one launch checks them
+// all.  `layouts` runs on the host meanwhile (before, on the page-locked
+// route) and fills probes[k] with re-uploads' new layouts; a failure there
+// or in a check ends the transfer before any scene changed.  Then the
+// layouts are adopted, one launch converts every scene, and the bonds,
+// materials and scene parameters follow in merged transfers.
+int World::stage_many(const int32_t *idx, const dem_scene *const *scs, int count, const SceneHost *probes,
+                      const std::function<int()> &layouts) {
+    std::vector<StageItem> tab;
+    std::vector<int> tab_k;
+    const long long total = pack_items(sh, idx, count, tab, tab_k);
+    const int nt = (int)tab.size();
+    for (int i = 0; i < nt; ++i) tab[i].has_data = scs[tab_k[i]]->data ? 1 : 0;
+    int rc = ensure_ref(std::max(total, 1LL));
+    if (rc) return rc;
+    rc = ensure_tables(nt + 1, N_REF_FIELDS * nt + 1);
+    if (rc) return rc;
+    PinMap pm;
+    const size_t o_fields = host_direct ? 0 : pm.take((size_t)ref_cap * REF_WORDS * 4);
+    const size_t o_copies = pm.take(sizeof(HostCopy) * ((size_t)N_REF_FIELDS * nt + 1));
+    const size_t o_items = pm.take(sizeof(StageItem) * (size_t)(nt + 1));
+    const size_t o_err = pm.take(4 * (size_t)(nt + 1));
+    const size_t o_bst = pm.take(4 * (size_t)d.B), o_blen = pm.take(4 * (size_t)d.B);
+    const size_t o_bstr = pm.take(8 * (size_t)d.B), o_bang = pm.take(4 * (size_t)d.B);
+    const size_t o_mats = pm.take(sizeof(Mat) * (size_t)d.M), o_pair = pm.take(8 * (size_t)d.MP);
+    const size_t o_par = pm.take(sizeof(ScenePar) * sh.size());
+    rc = ensure_pin(pm.bytes);
+    if (rc) return rc;
+    char *pb = static_cast<char *>(pin);
+    float *hp = reinterpret_cast<float *>(pb + o_fields);
+    int32_t *h_err = reinterpret_cast<int32_t *>(pb + o_err);
+    int32_t *h_bst = reinterpret_cast<int32_t *>(pb + o_bst);
+    float *h_blen = reinterpret_cast<float *>(pb + o_blen);
+    float2 *h_bstr = reinterpret_cast<float2 *>(pb + o_bstr);
+    int32_t *h_bang = reinterpret_cast<int32_t *>(pb + o_bang);
+    Mat *h_mats = reinterpret_cast<Mat *>(pb + o_mats);
+    float2 *h_pair = reinterpret_cast<float2 *>(pb + o_pair);
+    ScenePar *h_par = reinterpret_cast<ScenePar *>(pb + o_par);
+    float *dp0 = static_cast<float *>(ref_block);
+    cudaError_t ce = cudaSuccess;
+    if (host_direct) {
+        HostCopy *hc = reinterpret_cast<HostCopy *>(pb + o_copies);
+        int nc = 0;
+        long long pieces = 0;
+        for (int i = 0; i < nt; ++i)
+            for (int f = 0; f < N_REF_FIELDS; ++f) {
+                const RefField &F = REF_FIELDS[f];
+                pieces = add_copy(hc, nc, scene_field(scs[tab_k[i]], f), dp0 + F.base * ref_cap + F.per * tab[i].off,
+                                  4LL * F.per * tab[i].n, pieces);
+            }
+        if (nc > 0) {
+            ce = cudaMemcpyAsync(d_copies, hc, sizeof(HostCopy) * nc, cudaMemcpyHostToDevice, stream);
+            if (ce == cudaSuccess) {
+                launch_copies(d_copies, nc, pieces, nullptr, stream);
+                ce = cudaGetLastError();
+            }
         }
-        CK(cudaMemcpyAsync(d_items, &it, sizeof it, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemsetAsync(d_item_err, 0, 4, stream));
-        launch_stage_check(ref, d_items, 1, n, d_item_err, stream);
-        CK(cudaGetLastError());
-        int32_t e = 0;
-        CK(cudaMemcpyAsync(&e, d_item_err, 4, cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
-        rc = stage_error(e);
+        rc = layouts ? layouts() : DEM_OK;
+        if (rc != DEM_OK || ce != cudaSuccess) {
+            cudaStreamSynchronize(stream);  // the tables in the page-locked block are in use until then
+            return ce != cudaSuccess ? fail(DEM_E_CUDA, cudaGetErrorString(ce)) : rc;
+        }
+    } else {
+        rc = layouts ? layouts() : DEM_OK;
         if (rc) return rc;
+        struct Chunk {
+            int f, i0, i1;
+        };
+        std::vector<Chunk> chunks;
+        std::vector<long long> sizes;
+        for (int f = 0; f < N_REF_FIELDS && nt > 0; ++f)
+            for (const auto &g : split_items(tab, f == F_CONTACTS ? 8 : 1)) {
+                chunks.push_back(Chunk{f, g.first, g.second});
+                sizes.push_back(g.second - g.first);
+            }
+        HostPipe pipe(sizes, false);
+        pipe.start([&](int c, long long u) {
+            const Chunk &ch = chunks[c];
+            const int i = ch.i0 + (int)u;
+            const void *src = scene_field(scs[tab_k[i]], ch.f);
+            if (!src) return;
+            const RefField &F = REF_FIELDS[ch.f];
+            std::memcpy(hp + F.base * ref_cap + F.per * tab[i].off, src, sizeof(float) * F.per * (size_t)tab[i].n);
+        });
+        for (int c = 0; c < (int)chunks.size(); ++c) {
+            pipe.wait_chunk(c);
+            const Chunk &ch = chunks[c];
+            if (ce != cudaSuccess) continue;
+            const RefField &F = REF_FIELDS[ch.f];
+            const long long o0 = tab[ch.i0].off, o1 = tab[ch.i1 - 1].off + tab[ch.i1 - 1].n;
+            ce = cudaMemcpyAsync(dp0 + F.base * ref_cap + F.per * o0, hp + F.base * ref_cap + F.per * o0,
+                                 sizeof(float) * F.per * (size_t)(o1 - o0), cudaMemcpyHostToDevice, stream);
+        }
+        pipe.join();
     }
-    if (probe) apply_layout(s, *probe);
-    h.materials.assign(sc->materials, sc->materials + 6 * (size_t)h.n_mat);
-    if (n > 0) {
-        launch_stage_in(d, ref, d_items, 1, n, stream);
-        CK(cudaGetLastError());
+    // bonds and material tables of every scene into the page-locked block
+    par_for(count, [&](int k) {
+        const SceneHost &h = sh[idx[k]];
+        if (h.n_bonds > 0)
+            split_bonds(h, scs[k]->bonds, h_bst + h.bond_base, h_blen + h.bond_base, h_bstr + h.bond_base,
+                        h_bang + h.bond_base);
+        material_tables(scs[k]->materials, h.n_mat, h_mats + h.mat_base, h_pair + h.pair_base);
+    });
+    // the items with their (new) large-particle thresholds; one check launch
+    for (int i = 0; i < nt; ++i) tab[i].r_big = probes ? probes[tab_k[i]].r_big : sh[tab[i].scene].r_big;
+    std::memcpy(pb + o_items, tab.data(), sizeof(StageItem) * nt);
+    if (ce == cudaSuccess && nt > 0) {
+        ce = cudaMemcpyAsync(d_items, pb + o_items, sizeof(StageItem) * nt, cudaMemcpyHostToDevice, stream);
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(d_item_err, 0, 4 * (size_t)(nt + 1), stream);
+        if (ce == cudaSuccess) {
+            launch_stage_check(ref, d_items, nt, total, d_item_err, stream);
+            ce = cudaGetLastError();
+        }
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(h_err, d_item_err, 4 * (size_t)nt, cudaMemcpyDeviceToHost, stream);
     }
-    const int nb = h.n_bonds;
-    if (nb > 0) {
-        std::vector<int32_t> st(nb);
-        std::vector<float> len(nb);
-        std::vector<float2> str(nb);
-        h.bond_angle.resize(nb);
-        split_bonds(h, sc->bonds, st.data(), len.data(), str.data(), h.bond_angle.data());
-        CK(cudaMemcpyAsync(d.b_status + h.bond_base, st.data(), 4 * (size_t)nb, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemcpyAsync(d.b_length + h.bond_base, len.data(), 4 * (size_t)nb, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemcpyAsync(d.b_str + h.bond_base, str.data(), 8 * (size_t)nb, cudaMemcpyHostToDevice, stream));
-        CK(cudaStreamSynchronize(stream));
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+    if (ce != cudaSuccess) return fail(DEM_E_CUDA, cudaGetErrorString(ce));
+    for (int i = 0; i < nt; ++i)
+        if (h_err[i]) {
+            rc = stage_error(h_err[i]);
+            err += " (scene " + std::to_string(tab[i].scene) + ")";
+            return rc;
+        }
+    // every scene passed: adopt, convert, and send bonds, materials, parameters
+    std::vector<std::pair<long long, long long>> rb, rm, rp, rs;
+    for (int k = 0; k < count; ++k) {
+        const int s = idx[k];
+        SceneHost &h = sh[s];
+        if (probes) apply_layout(s, probes[k]);
+        h.materials.assign(scs[k]->materials, scs[k]->materials + 6 * (size_t)h.n_mat);
+        h.bond_angle.assign(h_bang + h.bond_base, h_bang + h.bond_base + h.n_bonds);
+        fill_par(h);
+        h_par[s] = h.par;
+        rb.emplace_back(h.bond_base, h.n_bonds);
+        rm.emplace_back(h.mat_base, h.n_mat);
+        rp.emplace_back(h.pair_base, (long long)h.n_mat * h.n_mat);
+        rs.emplace_back(s, 1);
     }
-    return push_materials(s);
+    launch_stage_in(d, ref, d_items, nt, total, stream);
+    CK(cudaGetLastError());
+    auto send = [&](void *dst, const void *src, size_t elem, const std::vector<std::pair<long long, long long>> &r) {
+        for (const auto &x : merge_runs(r)) {
+            cudaError_t e2 = cudaMemcpyAsync(static_cast<char *>(dst) + elem * x.first,
+                                             static_cast<const char *>(src) + elem * x.first, elem * x.second,
+                                             cudaMemcpyHostToDevice, stream);
+            if (e2 != cudaSuccess) return e2;
+        }
+        return cudaSuccess;
+    };
+    CK(send(d.b_status, h_bst, 4, rb));
+    CK(send(d.b_length, h_blen, 4, rb));
+    CK(send(d.b_str, h_bstr, 8, rb));
+    CK(send(d.mats, h_mats, sizeof(Mat), rm));
+    CK(send(d.pair, h_pair, 8, rp));
+    CK(send(d.par, h_par, sizeof(ScenePar), rs));
+    CK(cudaStreamSynchronize(stream));  // the page-locked block is reused by the next transfer
+    return DEM_OK;
 }
 
 int World::push_materials(int s) {
@@ -805,6 +965,7 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     use_graphs = ext.plain_launches == 0;
     split_narrow = ext.split_narrow != 0;
     fuse_lom = ext.unfused_lom == 0;
+    host_direct = ext.host_copies == 0 && device_reads_pageable();
     diagnostics = ext.diagnostics != 0;
     sh.assign(S, SceneHost{});
     long long N = 0, C = 0, B = 0, M = 0, MP = 0, TB = 0;
@@ -850,9 +1011,13 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     int rc = alloc((int)N, (int)C, (int)B, S, (int)M, (int)MP, (int)TB, ev_cap);
     if (rc) return rc;
     update_has_bigs();
-    for (int s = 0; s < S; ++s) {
-        rc = stage_scene(s, scenes[s], nullptr);
+    {
+        std::vector<int32_t> all(S);
+        for (int s = 0; s < S; ++s) all[s] = s;
+        rc = stage_many(all.data(), scenes.data(), S, nullptr, nullptr);
         if (rc) return rc;
+    }
+    for (int s = 0; s < S; ++s) {
         rc = push_bigs(s, s);
         if (rc) return rc;
         rc = push_par(s);
@@ -891,6 +1056,7 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     use_graphs = ext.plain_launches == 0;
     split_narrow = ext.split_narrow != 0;
     fuse_lom = ext.unfused_lom == 0;
+    host_direct = ext.host_copies == 0 && device_reads_pageable();
     diagnostics = ext.diagnostics != 0;
     const int S = scenes + 1;  // the last slot owns the unused particles
     free_slot = scenes;
@@ -982,7 +1148,10 @@ int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e
     h.cc2_0 = sc->coll_cont[2];
     h.active = true;
     sh[s] = h;
-    rc = stage_scene(s, sc, nullptr);
+    {
+        const int32_t one = s;
+        rc = stage_many(&one, &sc, 1, nullptr, nullptr);
+    }
     if (rc == DEM_OK) rc = push_bigs(s, s);
     if (rc == DEM_OK) rc = push_par(s);
     if (rc == DEM_OK) {
@@ -1049,18 +1218,13 @@ void World::apply_layout(int s, const SceneHost &probe) {
     h.par.g_h = probe.par.g_h;
 }
 
-// Many scenes at once (dem_batch_upload_many).  The layouts are derived on
-// host threads; host threads copy every scene into a page-locked block laid
-// out like the staging block while the block goes to the device one field
-// at a time; one launch checks every scene.  Nothing of any scene changes
-// unless every scene passes; then one launch converts them all and the
-// bonds, materials and scene parameters follow in merged transfers.
+// Many scenes at once (dem_batch_upload_many): the new layouts are derived
+// on host threads while the arrays travel; nothing of any scene changes
+// unless every scene passes.
 int World::upload_many(const int32_t *idx, const dem_scene *const *scs, int count) {
     if (count <= 0) return DEM_OK;
     if (!idx || !scs) return fail(DEM_E_INVALID, "scene index/pointer arrays are NULL");
     std::vector<SceneHost> probes(count);
-    std::vector<int> rcs(count, DEM_OK);
-    std::vector<std::string> errs(count);
     std::vector<char> seen(sh.size(), 0);
     for (int k = 0; k < count; ++k) {
         const int s = idx[k];
@@ -1073,8 +1237,10 @@ int World::upload_many(const int32_t *idx, const dem_scene *const *scs, int coun
                                            std::to_string(s) + ")");
         probes[k] = h;
     }
-    {
+    auto layouts = [&]() -> int {
         // compute_layout touches only its probe; derive them in parallel
+        std::vector<int> rcs(count, DEM_OK);
+        std::vector<std::string> errs(count);
         const int T = std::max(1, std::min(count, host_threads()));
         std::vector<std::thread> pool;
         std::vector<World> scratch(T);
@@ -1087,168 +1253,26 @@ int World::upload_many(const int32_t *idx, const dem_scene *const *scs, int coun
                 }
             });
         for (auto &th : pool) th.join();
-    }
-    for (int k = 0; k < count; ++k)
-        if (rcs[k]) return fail(rcs[k], errs[k] + " (scene " + std::to_string(idx[k]) + ")");
-    for (int k = 0; k < count; ++k) {
-        int rc = layout_fits(idx[k], probes[k]);
-        if (rc) {
-            err += " (scene " + std::to_string(idx[k]) + ")";
-            return rc;
+        for (int k = 0; k < count; ++k)
+            if (rcs[k]) return fail(rcs[k], errs[k] + " (scene " + std::to_string(idx[k]) + ")");
+        for (int k = 0; k < count; ++k) {
+            const int rc = layout_fits(idx[k], probes[k]);
+            if (rc) {
+                err += " (scene " + std::to_string(idx[k]) + ")";
+                return rc;
+            }
         }
-    }
-    // the transfer's items: scenes with particles, packed in call order
-    std::vector<StageItem> tab;
-    std::vector<int> tab_k;
-    long long total = 0;
-    for (int k = 0; k < count; ++k) {
-        const SceneHost &h = sh[idx[k]];
-        if (h.n <= 0) continue;
-        tab.push_back(StageItem{total, h.particle_base, h.n, idx[k], h.n_mat, h.n_bonds, scs[k]->data ? 1 : 0,
-                                probes[k].r_big, 0});
-        tab_k.push_back(k);
-        total += h.n;
-    }
-    const int nt = (int)tab.size();
-    int rc = ensure_ref(std::max(total, 1LL));
-    if (rc) return rc;
-    rc = ensure_items(std::max(nt, 1));
-    if (rc) return rc;
-    PinMap pm;
-    const size_t o_fields = pm.take((size_t)ref_cap * REF_WORDS * 4);
-    const size_t o_items = pm.take(sizeof(StageItem) * (size_t)std::max(nt, 1));
-    const size_t o_err = pm.take(4 * (size_t)std::max(nt, 1));
-    const size_t o_bst = pm.take(4 * (size_t)d.B), o_blen = pm.take(4 * (size_t)d.B);
-    const size_t o_bstr = pm.take(8 * (size_t)d.B), o_bang = pm.take(4 * (size_t)d.B);
-    const size_t o_mats = pm.take(sizeof(Mat) * (size_t)d.M), o_pair = pm.take(8 * (size_t)d.MP);
-    const size_t o_par = pm.take(sizeof(ScenePar) * sh.size());
-    rc = ensure_pin(pm.bytes);
-    if (rc) return rc;
-    char *pb = static_cast<char *>(pin);
-    float *hp = reinterpret_cast<float *>(pb + o_fields);
-    std::memcpy(pb + o_items, tab.data(), sizeof(StageItem) * nt);
-    int32_t *h_err = reinterpret_cast<int32_t *>(pb + o_err);
-    int32_t *h_bst = reinterpret_cast<int32_t *>(pb + o_bst);
-    float *h_blen = reinterpret_cast<float *>(pb + o_blen);
-    float2 *h_bstr = reinterpret_cast<float2 *>(pb + o_bstr);
-    int32_t *h_bang = reinterpret_cast<int32_t *>(pb + o_bang);
-    Mat *h_mats = reinterpret_cast<Mat *>(pb + o_mats);
-    float2 *h_pair = reinterpret_cast<float2 *>(pb + o_pair);
-    ScenePar *h_par = reinterpret_cast<ScenePar *>(pb + o_par);
-
-    // chunks: each field over all items (contacts in 8 groups), then the
-    // bonds and materials of every scene
-    struct Chunk {
-        int f, i0, i1;
+        return DEM_OK;
     };
-    std::vector<Chunk> chunks;
-    std::vector<long long> sizes;
-    for (int f = 0; f < N_REF_FIELDS && nt > 0; ++f)
-        for (const auto &g : split_items(tab, f == F_CONTACTS ? 8 : 1)) {
-            chunks.push_back(Chunk{f, g.first, g.second});
-            sizes.push_back(g.second - g.first);
-        }
-    chunks.push_back(Chunk{-1, 0, count});
-    sizes.push_back(count);
-    HostPipe pipe(sizes, false);
-    pipe.start([&](int c, long long u) {
-        const Chunk &ch = chunks[c];
-        if (ch.f >= 0) {
-            const int i = ch.i0 + (int)u;
-            const void *src = scene_field(scs[tab_k[i]], ch.f);
-            if (!src) return;
-            const RefField &F = REF_FIELDS[ch.f];
-            std::memcpy(hp + F.base * ref_cap + F.per * tab[i].off, src, sizeof(float) * F.per * (size_t)tab[i].n);
-            return;
-        }
-        const int k = (int)u;
-        const SceneHost &h = sh[idx[k]];
-        if (h.n_bonds > 0)
-            split_bonds(h, scs[k]->bonds, h_bst + h.bond_base, h_blen + h.bond_base, h_bstr + h.bond_base,
-                        h_bang + h.bond_base);
-        material_tables(scs[k]->materials, h.n_mat, h_mats + h.mat_base, h_pair + h.pair_base);
-    });
-    float *dp0 = static_cast<float *>(ref_block);
-    cudaError_t ce = cudaSuccess;
-    for (int c = 0; c < (int)chunks.size(); ++c) {
-        pipe.wait_chunk(c);
-        const Chunk &ch = chunks[c];
-        if (ch.f < 0 || ce != cudaSuccess) continue;
-        const RefField &F = REF_FIELDS[ch.f];
-        const long long o0 = tab[ch.i0].off, o1 = tab[ch.i1 - 1].off + tab[ch.i1 - 1].n;
-        ce = cudaMemcpyAsync(dp0 + F.base * ref_cap + F.per * o0, hp + F.base * ref_cap + F.per * o0,
-                             sizeof(float) * F.per * (size_t)(o1 - o0), cudaMemcpyHostToDevice, stream);
-    }
-    pipe.join();
-    if (ce == cudaSuccess && nt > 0) {
-        ce = cudaMemcpyAsync(d_items, pb + o_items, sizeof(StageItem) * nt, cudaMemcpyHostToDevice, stream);
-        if (ce == cudaSuccess) ce = cudaMemsetAsync(d_item_err, 0, 4 * (size_t)nt, stream);
-        if (ce == cudaSuccess) {
-            launch_stage_check(ref, d_items, nt, total, d_item_err, stream);
-            ce = cudaGetLastError();
-        }
-        if (ce == cudaSuccess)
-            ce = cudaMemcpyAsync(h_err, d_item_err, 4 * (size_t)nt, cudaMemcpyDeviceToHost, stream);
-    }
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
-    if (ce != cudaSuccess) return fail(DEM_E_CUDA, cudaGetErrorString(ce));
-    for (int i = 0; i < nt; ++i)
-        if (h_err[i]) {
-            rc = stage_error(h_err[i]);
-            err += " (scene " + std::to_string(tab[i].scene) + ")";
-            return rc;
-        }
-    // every scene passed: adopt, convert, and send bonds, materials, parameters
-    std::vector<std::pair<long long, long long>> rb, rm, rp, rs;
-    for (int k = 0; k < count; ++k) {
-        const int s = idx[k];
-        SceneHost &h = sh[s];
-        apply_layout(s, probes[k]);
-        h.materials.assign(scs[k]->materials, scs[k]->materials + 6 * (size_t)h.n_mat);
-        h.bond_angle.assign(h_bang + h.bond_base, h_bang + h.bond_base + h.n_bonds);
-        fill_par(h);
-        h_par[s] = h.par;
-        rb.emplace_back(h.bond_base, h.n_bonds);
-        rm.emplace_back(h.mat_base, h.n_mat);
-        rp.emplace_back(h.pair_base, (long long)h.n_mat * h.n_mat);
-        rs.emplace_back(s, 1);
-    }
-    launch_stage_in(d, ref, d_items, nt, total, stream);
-    CK(cudaGetLastError());
-    auto send = [&](void *dst, const void *src, size_t elem, const std::vector<std::pair<long long, long long>> &r) {
-        for (const auto &x : merge_runs(r)) {
-            cudaError_t e2 = cudaMemcpyAsync(static_cast<char *>(dst) + elem * x.first,
-                                             static_cast<const char *>(src) + elem * x.first, elem * x.second,
-                                             cudaMemcpyHostToDevice, stream);
-            if (e2 != cudaSuccess) return e2;
-        }
-        return cudaSuccess;
-    };
-    CK(send(d.b_status, h_bst, 4, rb));
-    CK(send(d.b_length, h_blen, 4, rb));
-    CK(send(d.b_str, h_bstr, 8, rb));
-    CK(send(d.mats, h_mats, sizeof(Mat), rm));
-    CK(send(d.pair, h_pair, 8, rp));
-    CK(send(d.par, h_par, sizeof(ScenePar), rs));
-    CK(cudaStreamSynchronize(stream));  // the pinned block is reused by the next transfer
+    int rc = stage_many(idx, scs, count, probes.data(), layouts);
+    if (rc) return rc;
     return force_rebuild();
 }
 
 int World::upload_scene(int s, const dem_scene *sc) {
     if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
-    SceneHost &h = sh[s];
-    if (!sc || sc->n_particles != h.n || sc->n_bonds != h.n_bonds || sc->n_materials != h.n_mat)
-        return fail(DEM_E_INVALID, "upload must keep particle, bond and material counts");
-    SceneHost probe = h;
-    int rc = compute_layout(probe, sc);
-    if (rc) return rc;
-    rc = layout_fits(s, probe);
-    if (rc) return rc;
-    rc = stage_scene(s, sc, &probe);
-    if (rc) return rc;
-    rc = push_par(s);
-    if (rc) return rc;
-    return force_rebuild();
+    const int32_t one = s;
+    return upload_many(&one, &sc, 1);
 }
 
 int World::set_params(int s, const dem_params &p) {
@@ -1573,39 +1597,39 @@ int World::download_scene(int s, dem_scene *out) {
 }
 
 // Many scenes at once (dem_batch_download_many).  One launch converts every
-// scene into the staging block; the block comes back one field at a time
-// into a page-locked block, and host threads copy each field into the
-// callers' arrays as soon as it has landed.  The callers' arrays are written
-// only if every scene's check passed.
+// scene into the staging block.  With host_direct one copy launch writes
+// the block and the per-particle reference mirrors straight into the
+// callers' arrays, skipped on the device if any conversion failed; else the
+// block comes back one field at a time into the page-locked block and host
+// threads copy each field out as soon as it has landed.  The callers'
+// arrays are written only if every scene's conversion passed.
 int World::download_many(const int32_t *idx, dem_scene *const *outs, int count) {
     if (count <= 0) return DEM_OK;
     if (!idx || !outs) return fail(DEM_E_INVALID, "scene index/pointer arrays are NULL");
-    std::vector<StageItem> tab;
-    std::vector<int> tab_k;
-    long long total = 0;
     for (int k = 0; k < count; ++k) {
         const int s = idx[k];
         if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
         if (!outs[k]) return fail(DEM_E_INVALID, "out is NULL");
-        const SceneHost &h = sh[s];
-        if (outs[k]->n_particles != h.n)
+        if (outs[k]->n_particles != sh[s].n)
             return fail(DEM_E_INVALID, "out->n_particles must match the scene (scene " + std::to_string(s) + ")");
-        if (h.n <= 0) continue;
-        tab.push_back(StageItem{total, h.particle_base, h.n, s, h.n_mat, h.n_bonds, 0, h.r_big, 0});
-        tab_k.push_back(k);
-        total += h.n;
     }
+    std::vector<StageItem> tab;
+    std::vector<int> tab_k;
+    const long long total = pack_items(sh, idx, count, tab, tab_k);
     const int nt = (int)tab.size();
     int rc = ensure_ref(std::max(total, 1LL));
     if (rc) return rc;
-    rc = ensure_items(std::max(nt, 1));
+    rc = ensure_tables(nt + 1, N_REF_FIELDS * nt + 1);
     if (rc) return rc;
     const size_t N = (size_t)d.N;
     PinMap pm;
-    const size_t o_fields = pm.take((size_t)ref_cap * REF_WORDS * 4);
-    const size_t o_items = pm.take(sizeof(StageItem) * (size_t)std::max(nt, 1));
-    const size_t o_err = pm.take(4 * (size_t)std::max(nt, 1));
-    const size_t o_fix = pm.take(24 * N), o_force = pm.take(24 * N), o_matp = pm.take(4 * N);
+    const size_t o_fields = host_direct ? 0 : pm.take((size_t)ref_cap * REF_WORDS * 4);
+    const size_t o_copies = pm.take(sizeof(HostCopy) * ((size_t)N_REF_FIELDS * nt + 1));
+    const size_t o_items = pm.take(sizeof(StageItem) * (size_t)(nt + 1));
+    const size_t o_err = pm.take(4 * (size_t)(nt + 1));
+    const size_t o_fix = host_direct ? 0 : pm.take(24 * N);
+    const size_t o_force = host_direct ? 0 : pm.take(24 * N);
+    const size_t o_matp = host_direct ? 0 : pm.take(4 * N);
     const size_t o_bst = pm.take(4 * (size_t)d.B), o_blen = pm.take(4 * (size_t)d.B);
     rc = ensure_pin(pm.bytes);
     if (rc) return rc;
@@ -1618,6 +1642,96 @@ int World::download_many(const int32_t *idx, dem_scene *const *outs, int count) 
     const int32_t *h_matp = reinterpret_cast<const int32_t *>(pb + o_matp);
     const int32_t *h_bst = reinterpret_cast<const int32_t *>(pb + o_bst);
     const float *h_blen = reinterpret_cast<const float *>(pb + o_blen);
+    float *dp0 = static_cast<float *>(ref_block);
+
+    // the conversion and its check words
+    if (nt > 0) {
+        CK(cudaMemcpyAsync(d_items, pb + o_items, sizeof(StageItem) * nt, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemsetAsync(d_item_err, 0, 4 * (size_t)(nt + 1), stream));
+        launch_stage_out(d, ref, d_items, nt, total, d_item_err, stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(pb + o_err, d_item_err, 4 * (size_t)(nt + 1), cudaMemcpyDeviceToHost, stream));
+    }
+    std::vector<std::pair<long long, long long>> rn, rb;
+    for (int k = 0; k < count; ++k) {
+        const SceneHost &h = sh[idx[k]];
+        rn.emplace_back(h.particle_base, h.n);
+        rb.emplace_back(h.bond_base, h.n_bonds);
+    }
+    rn = merge_runs(rn);
+    rb = merge_runs(rb);
+    auto fetch_bonds = [&]() -> cudaError_t {
+        for (const auto &x : rb) {
+            cudaError_t e2 = cudaMemcpyAsync(pb + o_bst + 4 * x.first, d.b_status + x.first, 4 * x.second,
+                                             cudaMemcpyDeviceToHost, stream);
+            if (e2 == cudaSuccess)
+                e2 = cudaMemcpyAsync(pb + o_blen + 4 * x.first, d.b_length + x.first, 4 * x.second,
+                                     cudaMemcpyDeviceToHost, stream);
+            if (e2 != cudaSuccess) return e2;
+        }
+        return cudaSuccess;
+    };
+    // what the host fills of scene k (mirrors: also fixity, forces, material pointers)
+    auto host_part = [&](int k, bool mirrors) {
+        const int s = idx[k];
+        const SceneHost &h = sh[s];
+        dem_scene *out = outs[k];
+        const size_t n = (size_t)h.n, base = (size_t)h.particle_base;
+        if (mirrors) {
+            if (out->fixity && n) std::memcpy(out->fixity, h_fix + 6 * base, 24 * n);
+            if (out->forces && n) std::memcpy(out->forces, h_force + 6 * base, 24 * n);
+            if (out->material_pointers && n) std::memcpy(out->material_pointers, h_matp + base, 4 * n);
+        }
+        if (out->materials && out->n_materials == h.n_mat)
+            std::memcpy(out->materials, h.materials.data(), h.materials.size() * 4);
+        if (out->bonds && out->n_bonds == h.n_bonds)
+            for (int q = 0; q < h.n_bonds; ++q) {
+                out->bonds[3 * q] = h_bst[h.bond_base + q];
+                out->bonds[3 * q + 1] = h.bond_angle[q];
+                out->bonds[3 * q + 2] = f2bits(h_blen[h.bond_base + q]);
+            }
+        control(s, out->coll_cont);
+        out->grid = h.grid;
+    };
+    auto first_error = [&]() -> int {
+        for (int i = 0; i < nt; ++i)
+            if (h_err[i]) {
+                const int r2 = unstage_error(h_err[i]);
+                err += " (scene " + std::to_string(tab[i].scene) + ")";
+                return r2;
+            }
+        return DEM_OK;
+    };
+
+    if (host_direct) {
+        HostCopy *hc = reinterpret_cast<HostCopy *>(pb + o_copies);
+        int nc = 0;
+        long long pieces = 0;
+        for (int i = 0; i < nt; ++i) {
+            dem_scene *out = outs[tab_k[i]];
+            for (int f = 0; f < N_REF_FIELDS; ++f) {
+                if (!OUT_FIELD[f]) continue;
+                const RefField &F = REF_FIELDS[f];
+                pieces = add_copy(hc, nc, dp0 + F.base * ref_cap + F.per * tab[i].off,
+                                  const_cast<void *>(scene_field(out, f)), 4LL * F.per * tab[i].n, pieces);
+            }
+            const size_t base = (size_t)tab[i].base;
+            pieces = add_copy(hc, nc, d.fix_ref + 6 * base, out->fixity, 24LL * tab[i].n, pieces);
+            pieces = add_copy(hc, nc, d.force_ref + 6 * base, out->forces, 24LL * tab[i].n, pieces);
+            pieces = add_copy(hc, nc, d.matp_ref + base, out->material_pointers, 4LL * tab[i].n, pieces);
+        }
+        if (nc > 0) {
+            CK(cudaMemcpyAsync(d_copies, hc, sizeof(HostCopy) * nc, cudaMemcpyHostToDevice, stream));
+            launch_copies(d_copies, nc, pieces, d_item_err + nt, stream);
+            CK(cudaGetLastError());
+        }
+        CK(fetch_bonds());
+        CK(cudaStreamSynchronize(stream));
+        rc = first_error();
+        if (rc) return rc;
+        par_for(count, [&](int k) { host_part(k, false); });
+        return DEM_OK;
+    }
 
     struct Chunk {
         int f, i0, i1;
@@ -1635,24 +1749,6 @@ int World::download_many(const int32_t *idx, dem_scene *const *outs, int count) 
     sizes.push_back(count);
     rc = ensure_events((int)chunks.size());
     if (rc) return rc;
-
-    // the conversion and its check words, then every chunk's copy and event
-    if (nt > 0) {
-        CK(cudaMemcpyAsync(d_items, pb + o_items, sizeof(StageItem) * nt, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemsetAsync(d_item_err, 0, 4 * (size_t)nt, stream));
-        launch_stage_out(d, ref, d_items, nt, total, d_item_err, stream);
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(pb + o_err, d_item_err, 4 * (size_t)nt, cudaMemcpyDeviceToHost, stream));
-    }
-    float *dp0 = static_cast<float *>(ref_block);
-    std::vector<std::pair<long long, long long>> rn, rb;
-    for (int k = 0; k < count; ++k) {
-        const SceneHost &h = sh[idx[k]];
-        rn.emplace_back(h.particle_base, h.n);
-        rb.emplace_back(h.bond_base, h.n_bonds);
-    }
-    rn = merge_runs(rn);
-    rb = merge_runs(rb);
     for (int c = 0; c < (int)chunks.size(); ++c) {
         const Chunk &ch = chunks[c];
         if (ch.f >= 0) {
@@ -1669,44 +1765,22 @@ int World::download_many(const int32_t *idx, dem_scene *const *outs, int count) 
                 CK(cudaMemcpyAsync(pb + o_matp + 4 * x.first, d.matp_ref + x.first, 4 * x.second,
                                    cudaMemcpyDeviceToHost, stream));
             }
-            for (const auto &x : rb) {
-                CK(cudaMemcpyAsync(pb + o_bst + 4 * x.first, d.b_status + x.first, 4 * x.second,
-                                   cudaMemcpyDeviceToHost, stream));
-                CK(cudaMemcpyAsync(pb + o_blen + 4 * x.first, d.b_length + x.first, 4 * x.second,
-                                   cudaMemcpyDeviceToHost, stream));
-            }
+            CK(fetch_bonds());
         }
         CK(cudaEventRecord(xfer_ev[c], stream));
     }
     HostPipe pipe(sizes, true);
     pipe.start([&](int c, long long u) {
         const Chunk &ch = chunks[c];
-        if (ch.f >= 0) {
-            const int i = ch.i0 + (int)u;
-            dem_scene *out = outs[tab_k[i]];
-            void *dst = const_cast<void *>(scene_field(out, ch.f));
-            if (!dst) return;
-            const RefField &F = REF_FIELDS[ch.f];
-            std::memcpy(dst, hp + F.base * ref_cap + F.per * tab[i].off, sizeof(float) * F.per * (size_t)tab[i].n);
+        if (ch.f < 0) {
+            host_part((int)u, true);
             return;
         }
-        const int k = (int)u, s = idx[k];
-        const SceneHost &h = sh[s];
-        dem_scene *out = outs[k];
-        const size_t n = (size_t)h.n, base = (size_t)h.particle_base;
-        if (out->fixity && n) std::memcpy(out->fixity, h_fix + 6 * base, 24 * n);
-        if (out->forces && n) std::memcpy(out->forces, h_force + 6 * base, 24 * n);
-        if (out->material_pointers && n) std::memcpy(out->material_pointers, h_matp + base, 4 * n);
-        if (out->materials && out->n_materials == h.n_mat)
-            std::memcpy(out->materials, h.materials.data(), h.materials.size() * 4);
-        if (out->bonds && out->n_bonds == h.n_bonds)
-            for (int q = 0; q < h.n_bonds; ++q) {
-                out->bonds[3 * q] = h_bst[h.bond_base + q];
-                out->bonds[3 * q + 1] = h.bond_angle[q];
-                out->bonds[3 * q + 2] = f2bits(h_blen[h.bond_base + q]);
-            }
-        control(s, out->coll_cont);
-        out->grid = h.grid;
+        const int i = ch.i0 + (int)u;
+        void *dst = const_cast<void *>(scene_field(outs[tab_k[i]], ch.f));
+        if (!dst) return;
+        const RefField &F = REF_FIELDS[ch.f];
+        std::memcpy(dst, hp + F.base * ref_cap + F.per * tab[i].off, sizeof(float) * F.per * (size_t)tab[i].n);
     });
     for (int c = 0; c < (int)chunks.size(); ++c) {
         const cudaError_t ce = cudaEventSynchronize(xfer_ev[c]);
@@ -1715,15 +1789,11 @@ int World::download_many(const int32_t *idx, dem_scene *const *outs, int count) 
             pipe.join();
             return fail(DEM_E_CUDA, cudaGetErrorString(ce));
         }
-        if (c == 0)
-            for (int i = 0; i < nt; ++i)
-                if (h_err[i]) {
-                    pipe.cancel();
-                    pipe.join();
-                    rc = unstage_error(h_err[i]);
-                    err += " (scene " + std::to_string(tab[i].scene) + ")";
-                    return rc;
-                }
+        if (c == 0 && (rc = first_error()) != DEM_OK) {
+            pipe.cancel();
+            pipe.join();
+            return rc;
+        }
         pipe.release(c);
     }
     pipe.join();

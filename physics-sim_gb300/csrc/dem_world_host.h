@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -132,7 +133,8 @@ class World {
     void fill_par(SceneHost &h);
     int push_par(int s);
     int push_det();
-    int stage_scene(int s, const dem_scene *scene, const SceneHost *probe);
+    int stage_many(const int32_t *idx, const dem_scene *const *scs, int count, const SceneHost *probes,
+                   const std::function<int()> &layouts);
     int force_rebuild();
     void enqueue_plain_step(bool first, bool last);
     void enqueue_rebuild(cudaStream_t st, const int32_t *gate);
@@ -148,11 +150,15 @@ class World {
     void *pin = nullptr;               // page-locked staging of the bulk transfers
     size_t pin_bytes = 0;
     int ensure_pin(size_t bytes);
-    // the item table of a staging transfer and one check word per item
+    // the item table of a staging transfer, one check word per item (plus
+    // their OR), and the table of its direct copies
     StageItem *d_items = nullptr;
     int32_t *d_item_err = nullptr;
     int items_cap = 0;
-    int ensure_items(int count);
+    HostCopy *d_copies = nullptr;
+    int copies_cap = 0;
+    int ensure_tables(int items, int copies);
+    bool host_direct = false;  // the device reads and writes the callers' arrays (dem_ext::host_copies)
     std::vector<cudaEvent_t> xfer_ev;  // one per chunk of a pipelined download
     int ensure_events(int count);
     RefArrays ref_at(long long off) const;

@@ -62,7 +62,7 @@ class Ext(C.Structure):
                 ("block_size", C.c_int32), ("search_cell_factor", C.c_float),
                 ("event_capacity", C.c_int32), ("list_skin", C.c_float),
                 ("plain_launches", C.c_int32), ("split_narrow", C.c_int32), ("unfused_lom", C.c_int32),
-                ("reserved", C.c_int32 * 3)]
+                ("host_copies", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class Scene(C.Structure):
@@ -249,7 +249,7 @@ def make_params(d):
 
 def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnostics=True,
              reorder_interval=0, block_size=0, search_cell_factor=0.0, event_capacity=0,
-             list_skin=0.0, plain_launches=False, split_narrow=0, unfused_lom=0, keep=None):
+             list_skin=0.0, plain_launches=False, split_narrow=0, unfused_lom=0, host_copies=0, keep=None):
     e = Ext()
     lib().dem_ext_defaults(C.byref(e))
     e.use_f64 = 1 if use_f64 else 0
@@ -263,6 +263,7 @@ def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnos
     e.plain_launches = 1 if plain_launches else 0
     e.split_narrow = 1 if split_narrow else 0
     e.unfused_lom = 1 if unfused_lom else 0
+    e.host_copies = 1 if host_copies else 0
     for attr, arr in (("bond_normal_strength", bond_sn), ("bond_shear_strength", bond_ss)):
         if arr is not None:
             a = np.ascontiguousarray(arr, dtype=np.float32)
@@ -275,6 +276,10 @@ def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnos
 F32_KEYS = ("pos", "radii", "vel", "acc", "rot", "rot_vel", "rot_acc", "forces", "del_pos",
             "del_rot", "materials", "data")
 I32_KEYS = ("fixity", "bonds", "contacts", "material_pointers")
+# words per particle of the per-particle arrays (state.rs:69-93)
+_PER_PARTICLE = (("pos", 2), ("vel", 2), ("acc", 2), ("rot", 1), ("rot_vel", 1), ("rot_acc", 1),
+                 ("forces", 6), ("fixity", 6), ("del_pos", 2), ("del_rot", 1), ("contacts", 84),
+                 ("material_pointers", 1), ("data", 7))
 
 
 def make_scene(sc):
@@ -287,8 +292,14 @@ def make_scene(sc):
         a = sc[k]
         if a.dtype != np.int32 or not a.flags.c_contiguous:
             raise TypeError("%s must be contiguous int32" % k)
-    s = Scene()
     n = int(sc["radii"].shape[0])
+    for k, per in _PER_PARTICLE:
+        a = sc.get(k)
+        if a is None and k == "data":
+            continue
+        if a.size != per * n:
+            raise ValueError("%s holds %d values, expected %d x %d particles" % (k, a.size, per, n))
+    s = Scene()
     s.n_particles = n
     s.n_bonds = int(sc["bonds"].shape[0] // 3)
     s.n_materials = int(sc["materials"].shape[0] // 6)
