@@ -192,16 +192,17 @@ __device__ __forceinline__ bool last_warp(uint32_t *ticket) {
 // 2D_LOM.wgsl:85-152 of one particle from its records (p, v, a, flags m,
 // rebuild position b); `ext`: positions were set externally, so the
 // displacement is the stored dext.  Position, displacement and bucket range
-// go to pr_out/dp_out/rr_out, the velocities and data[4..6] to vw/d4.
+// go to pr_out/dp_out/rr_out, the velocities to vw, and data[4..6] to d4
+// when keep_d4 (a later LOM pass of the same call would overwrite it).
 __device__ __forceinline__ void lom_core(const DevWorld &w, const ScenePar &P, int i, uint32_t m, float4 p,
-                                         float4 v, float4 a, float2 b, bool ext, float4 dext, float4 *pr_out,
-                                         float4 *dp_out, int2 *rr_out) {
+                                         float4 v, float4 a, float2 b, bool ext, float4 dext, bool keep_d4,
+                                         float4 *pr_out, float4 *dp_out, int2 *rr_out) {
     const float dT = P.p.dT;
     float ivx = v.x, ivy = v.y, iw = v.z;
     if (m & M_KICK_X) ivx = ivx + (a.x * dT) * 0.5f;               // :88
     if (m & M_KICK_Y) ivy = ivy + (a.y * dT) * 0.5f;               // :89
     if (m & M_KICK_R) iw = iw + (a.z * dT) * 0.5f;                 // :90
-    w.d4[i] = make_float4(ivx, ivy, iw, 0.0f);                     // :92-94
+    if (keep_d4) w.d4[i] = make_float4(ivx, ivy, iw, 0.0f);        // :92-94
     float4 d;
     if (!ext) {                                                    // :96-99
         d = make_float4(ivx * dT, ivy * dT, iw * dT, 0.0f);
@@ -274,7 +275,8 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     const ScenePar &P = w.par[s];
     if (p.z == 0.0f) return;                                       // :83
     const bool ext = w.cc3[s] != 0;
-    lom_core(w, P, i, m, p, v, a, b, ext, ext ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f), w.pr, w.dp, w.rr);
+    lom_core(w, P, i, m, p, v, a, b, ext, ext ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f), true, w.pr, w.dp,
+             w.rr);
 }
 
 // With w.ticket the kernel's last warp sets the rebuild conditional; without
@@ -773,8 +775,13 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // range go to the other buffers (pr_n, dp_n, rr_n), because neighbours still
 // read this step's values.  Particles that do not step on (zero radius, or a
 // served scene at its horizon) copy theirs across.
+// Accelerations and data[0..2] (this pass) and data[4..6] (the LOM pass) are
+// seen only by the caller after a call returns, and every step overwrites
+// them; a fused step whose scene steps on within the call therefore leaves
+// them to the scene's last step of the call (lom_final: the next step is the
+// call's last).  Results are unchanged; the intermediate writes are saved.
 template <int PART, bool FUSE>
-__device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr) {
+__device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr, bool lom_final) {
     // The particle's own records: the ones needed first are loaded now, the
     // rest (read only after the scene, detection and slot checks resolve)
     // are prefetched now, so the DRAM round trips overlap instead of
@@ -1098,7 +1105,9 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     }
     const float ax = fxs / mass, ay = fys / mass;
     const float al = moment / rot_inertia;
-    w.ac[i] = make_float4(ax, ay, al, 0.0f);
+    const long long rem = FUSE ? w.remaining[s] : 0;
+    const bool steps_on = FUSE && rem > 1;  // this scene's next step is in this call
+    if (!steps_on) w.ac[i] = make_float4(ax, ay, al, 0.0f);
     float4 v = w.vw[i];
     const float dT = P.p.dT;
     if (m & M_KICK_X) v.x = v.x + (0.5f * ax) * dT;
@@ -1106,9 +1115,9 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     if (m & M_KICK_R) v.z = v.z + (0.5f * al) * dT;
     if (!FUSE) {
         w.vw[i] = v;
-    } else if (w.remaining[s] > 1) {
+    } else if (steps_on) {
         lom_core(w, P, i, m, pa, v, make_float4(ax, ay, al, 0.0f), w.pbuild[i], false,
-                 make_float4(0.0f, 0.0f, 0.0f, 0.0f), w.pr_n, w.dp_n, w.rr_n);
+                 make_float4(0.0f, 0.0f, 0.0f, 0.0f), lom_final || rem == 2, w.pr_n, w.dp_n, w.rr_n);
     } else {
         w.vw[i] = v;
         w.pr_n[i] = pa;
@@ -1116,10 +1125,12 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         w.rr_n[i] = w.rr[i];
     }
     // data[0..2]; a particle without contacts writes +0 every step, which the
-    // slot word's DF_ZERO bit lets it skip
-    const bool zero = (__float_as_uint(acc.d0) | __float_as_uint(acc.d1) | __float_as_uint(acc.d2)) == 0u;
-    if (!(zero && (mask & DF_ZERO))) w.dF[i] = make_float4(acc.d0, acc.d1, acc.d2, 0.0f);
-    mask = zero ? (mask | DF_ZERO) : (mask & ~DF_ZERO);
+    // slot word's DF_ZERO bit (set while the stored value is all +0) lets it skip
+    if (!steps_on) {
+        const bool zero = (__float_as_uint(acc.d0) | __float_as_uint(acc.d1) | __float_as_uint(acc.d2)) == 0u;
+        if (!(zero && (mask & DF_ZERO))) w.dF[i] = make_float4(acc.d0, acc.d1, acc.d2, 0.0f);
+        mask = zero ? (mask | DF_ZERO) : (mask & ~DF_ZERO);
+    }
     if (mask != before) w.smask[i] = mask;
 }
 
@@ -1166,11 +1177,12 @@ __device__ __forceinline__ void interact_tail(const DevWorld &w, bool fused, int
 }
 
 template <bool FUSE>
-__global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w, int in_graph, cudaGraphConditionalHandle cond) {
+__global__ void __launch_bounds__(IB, 8) k_interact(DevWorld w, int in_graph, cudaGraphConditionalHandle cond,
+                                                    int lom_final) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle<0, FUSE>(w, i, nr);
+    if (i < w.N) interact_particle<0, FUSE>(w, i, nr, lom_final != 0);
     interact_tail(w, FUSE, in_graph, cond);
 }
 
@@ -1178,15 +1190,16 @@ __global__ void __launch_bounds__(IB, 12) k_narrow(DevWorld w) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle<1, false>(w, i, nr);
+    if (i < w.N) interact_particle<1, false>(w, i, nr, false);
 }
 
 template <bool FUSE>
-__global__ void __launch_bounds__(IB, 8) k_forces(DevWorld w, int in_graph, cudaGraphConditionalHandle cond) {
+__global__ void __launch_bounds__(IB, 8) k_forces(DevWorld w, int in_graph, cudaGraphConditionalHandle cond,
+                                                  int lom_final) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle<2, FUSE>(w, i, nr);
+    if (i < w.N) interact_particle<2, FUSE>(w, i, nr, lom_final != 0);
     interact_tail(w, FUSE, in_graph, cond);
 }
 
@@ -1310,8 +1323,8 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
     if (threadIdx.x == 0) out[15] = keep;
 }
 
-int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool in_graph,
-                    cudaGraphConditionalHandle cond) {
+int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool lom_final,
+                    bool in_graph, cudaGraphConditionalHandle cond) {
     (void)block;
     int k = 0;
     if (bigs && w.n_big_slots > 0) {
@@ -1319,15 +1332,15 @@ int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bo
         k++;
     }
     const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
-    const int ig = in_graph ? 1 : 0;
+    const int ig = in_graph ? 1 : 0, lf = lom_final ? 1 : 0;
     if (w.split) {
         k_narrow<<<g, IB, 0, st>>>(w);
-        if (fuse) k_forces<true><<<g, IB, 0, st>>>(w, ig, cond);
-        else k_forces<false><<<g, IB, 0, st>>>(w, ig, cond);
+        if (fuse) k_forces<true><<<g, IB, 0, st>>>(w, ig, cond, lf);
+        else k_forces<false><<<g, IB, 0, st>>>(w, ig, cond, lf);
         k += 2;
     } else {
-        if (fuse) k_interact<true><<<g, IB, 0, st>>>(w, ig, cond);
-        else k_interact<false><<<g, IB, 0, st>>>(w, ig, cond);
+        if (fuse) k_interact<true><<<g, IB, 0, st>>>(w, ig, cond, lf);
+        else k_interact<false><<<g, IB, 0, st>>>(w, ig, cond, lf);
         k++;
     }
     if (!w.ticket) {

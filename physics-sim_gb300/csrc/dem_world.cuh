@@ -203,9 +203,10 @@ void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStr
 void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
 // the Simulation pass of one step; with `fuse` also the next step's LOM pass
 // (into the other pr/dp/rr buffers), whose rebuild condition is set on `cond`
-// when in a graph
-int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool in_graph,
-                    cudaGraphConditionalHandle cond);
+// when in a graph.  A fused step is never a call's last step; lom_final: the
+// next one is (its LOM pass keeps data[4..6]).
+int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool lom_final,
+                    bool in_graph, cudaGraphConditionalHandle cond);
 void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
                            const int32_t *d_props, int block, cudaStream_t st);
 int scan_tmp_size(int n);

@@ -1389,7 +1389,7 @@ void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate) {
 // return at once unless a particle moved beyond its skin.  Within a call the
 // first step runs its own LOM pass; every step but the last runs the next
 // step's LOM pass inside its Simulation kernel.
-void World::enqueue_plain_step(bool first, bool last) {
+void World::enqueue_plain_step(bool first, bool last, bool next_last) {
     auto rec = [&](int kind, bool begin) {
         if (!timing) return;
         cudaEvent_t e;
@@ -1409,7 +1409,7 @@ void World::enqueue_plain_step(bool first, bool last) {
     rec(T_BROAD, false);
     rec(T_INTERACT, true);
     const bool fuse = fuse_lom && !last;
-    k += launch_interact(d, block, stream, has_bigs, fuse, false, cudaGraphConditionalHandle{});
+    k += launch_interact(d, block, stream, has_bigs, fuse, next_last, false, cudaGraphConditionalHandle{});
     rec(T_INTERACT, false);
     if (fuse) flip();
     launches += k + rebuild_kernels;
@@ -1512,12 +1512,12 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
         if (fuse_lom && k + 1 < R) {
             cudaGraphConditionalHandle hn{};
             CKR(cudaGraphConditionalHandleCreate(&hn, g, 0, cudaGraphCondAssignDefault));
-            kernels += launch_interact(d, block, stream, has_bigs, true, true, hn);
+            kernels += launch_interact(d, block, stream, has_bigs, true, k + 2 == R, true, hn);
             CKR(cudaGetLastError());
             flip();
             h = hn;
         } else {
-            kernels += launch_interact(d, block, stream, has_bigs, false, true, cudaGraphConditionalHandle{});
+            kernels += launch_interact(d, block, stream, has_bigs, false, false, true, cudaGraphConditionalHandle{});
             CKR(cudaGetLastError());
         }
     }
@@ -1567,7 +1567,7 @@ int World::step(int n_steps) {
         }
     }
     const int k0 = k;
-    for (; k < n_steps; ++k) enqueue_plain_step(k == k0, k + 1 == n_steps);
+    for (; k < n_steps; ++k) enqueue_plain_step(k == k0, k + 1 == n_steps, k + 2 == n_steps);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(DEM_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     return DEM_OK;
