@@ -622,6 +622,21 @@ class Batch:
         for (_, out), st in zip(pairs, structs):
             out["coll_cont"] = np.array(st.coll_cont[:], dtype=np.int32)
 
+    def kernel_timing(self, on):
+        """CUDA-event timing of every kernel kind (plain launches while on)."""
+        L = lib()
+        L.dem_batch_kernel_timing.argtypes = [C.c_void_p, C.c_int32]
+        self._check(L.dem_batch_kernel_timing(self.h, 1 if on else 0))
+
+    def kernel_time(self, kernel):
+        """(total device ms, launches) of a kernel since kernel timing was enabled."""
+        L = lib()
+        L.dem_batch_kernel_time.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+        ms = C.c_double(0.0)
+        n = C.c_int64(0)
+        self._check(L.dem_batch_kernel_time(self.h, kernel.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
     def break_events(self, cap=1 << 18):
         buf = np.zeros(cap, dtype=BREAK_DTYPE)
         n = C.c_int32(0)
