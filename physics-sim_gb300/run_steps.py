@@ -24,8 +24,12 @@ def main():
     ap.add_argument("--plain", action="store_true", help="no CUDA graphs (for ncu)")
     ap.add_argument("--split", action="store_true", help="Simulation pass as k_narrow + k_forces")
     ap.add_argument("--unfused", action="store_true", help="every step its own LOM kernel")
+    ap.add_argument("--cell-factor", type=float, default=0.0, help="search_cell_factor (0: default)")
+    ap.add_argument("--skin", type=float, default=0.0, help="list_skin (0: default)")
+    ap.add_argument("--block", type=int, default=0, help="block_size (0: default)")
     a = ap.parse_args()
-    knobs = {"split_narrow": int(a.split), "unfused_lom": int(a.unfused)}
+    knobs = {"split_narrow": int(a.split), "unfused_lom": int(a.unfused), "search_cell_factor": a.cell_factor,
+             "list_skin": a.skin, "block_size": a.block}
     if a.workload == "c3_batch":
         items = dem_scenes.c3_batch(n_scenes=a.particles or 512)
         with dem.Batch(items, reorder_interval=a.graph_steps, plain_launches=a.plain, **knobs) as b:
