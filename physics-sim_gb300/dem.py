@@ -193,6 +193,8 @@ def lib(path=None):
     L.dem_batch_synchronize.argtypes = [C.c_void_p]
     L.dem_batch_download.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Scene)]
     L.dem_batch_upload.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Scene)]
+    L.dem_batch_upload_many.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+    L.dem_batch_download_many.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
     L.dem_batch_set_params.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Params)]
     L.dem_batch_set_properties.argtypes = [C.c_void_p, C.c_int32, _IP, _IP]
     L.dem_batch_break_events.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
@@ -282,8 +284,34 @@ _PER_PARTICLE = (("pos", 2), ("vel", 2), ("acc", 2), ("rot", 1), ("rot_vel", 1),
                  ("material_pointers", 1), ("data", 7))
 
 
-def make_scene(sc):
-    """Scene struct pointing into the numpy arrays of dict `sc` (kept alive by the caller)."""
+# The data pointer of an ndarray is the first field after the object header
+# (PyArrayObject_fields.data, which numpy's PyArray_DATA reads); on CPython
+# reading it there costs a fifth of __array_interface__, which matters when
+# hundreds of scenes are marshalled per call.  Checked once against numpy's
+# own answer; anything else falls back to the interface.
+_DATA_OFFSET = 2 * C.sizeof(C.c_void_p)
+
+
+def _fast_data_probe():
+    import platform
+    if platform.python_implementation() != "CPython":
+        return False
+    a = np.zeros(3, dtype=np.float32)
+    return C.c_void_p.from_address(id(a) + _DATA_OFFSET).value == a.ctypes.data
+
+
+_FAST_DATA = _fast_data_probe()
+
+
+def _addr(a):
+    if _FAST_DATA:
+        return C.c_void_p.from_address(id(a) + _DATA_OFFSET).value
+    return a.__array_interface__["data"][0]
+
+
+def make_scene(sc, s=None):
+    """Scene struct (or the given one, filled) pointing into the numpy arrays of
+    dict `sc` (kept alive by the caller)."""
     for k in F32_KEYS:
         a = sc[k]
         if a.dtype != np.float32 or not a.flags.c_contiguous:
@@ -299,14 +327,15 @@ def make_scene(sc):
             continue
         if a.size != per * n:
             raise ValueError("%s holds %d values, expected %d x %d particles" % (k, a.size, per, n))
-    s = Scene()
+    if s is None:
+        s = Scene()
     s.n_particles = n
     s.n_bonds = int(sc["bonds"].shape[0] // 3)
     s.n_materials = int(sc["materials"].shape[0] // 6)
     for k in F32_KEYS:
-        setattr(s, k, sc[k].__array_interface__["data"][0])
+        setattr(s, k, _addr(sc[k]))
     for k in I32_KEYS:
-        setattr(s, k, sc[k].__array_interface__["data"][0])
+        setattr(s, k, _addr(sc[k]))
     s.coll_cont[:] = [int(v) for v in sc["coll_cont"]]
     cs, cap, w, h = sc["grid"]
     s.grid.cell_size = float(cs)
@@ -604,23 +633,32 @@ class Batch:
         st = make_scene(sc)
         self._check(lib().dem_batch_upload(self.h, int(scene), C.byref(st)))
 
+    @staticmethod
+    def _scene_table(pairs):
+        """The pairs' scene structs in one array, their indices and pointers."""
+        n = len(pairs)
+        structs = (Scene * n)()
+        for k, (_, sc) in enumerate(pairs):
+            make_scene(sc, structs[k])
+        idx = np.array([int(k) for k, _ in pairs], dtype=np.int32)
+        ptrs = np.arange(n, dtype=np.uint64) * C.sizeof(Scene) + C.addressof(structs)
+        return structs, idx, ptrs
+
     def upload_many(self, pairs):
         """[(scene index, scene dict), ...] in one call (dem_batch_upload_many)."""
-        n = len(pairs)
-        structs = [make_scene(sc) for _, sc in pairs]
-        idx = (C.c_int32 * n)(*[int(k) for k, _ in pairs])
-        ptrs = (C.c_void_p * n)(*[C.addressof(st) for st in structs])
-        self._check(lib().dem_batch_upload_many(self.h, n, idx, ptrs))
+        structs, idx, ptrs = self._scene_table(pairs)
+        self._check(lib().dem_batch_upload_many(self.h, len(pairs), C.c_void_p(idx.ctypes.data),
+                                                C.c_void_p(ptrs.ctypes.data)))
 
     def download_many(self, pairs):
         """[(scene index, scene dict to fill), ...] in one call (dem_batch_download_many)."""
-        n = len(pairs)
-        structs = [make_scene(out) for _, out in pairs]
-        idx = (C.c_int32 * n)(*[int(k) for k, _ in pairs])
-        ptrs = (C.c_void_p * n)(*[C.addressof(st) for st in structs])
-        self._check(lib().dem_batch_download_many(self.h, n, idx, ptrs))
-        for (_, out), st in zip(pairs, structs):
-            out["coll_cont"] = np.array(st.coll_cont[:], dtype=np.int32)
+        structs, idx, ptrs = self._scene_table(pairs)
+        self._check(lib().dem_batch_download_many(self.h, len(pairs), C.c_void_p(idx.ctypes.data),
+                                                  C.c_void_p(ptrs.ctypes.data)))
+        raw = np.frombuffer(structs, dtype=np.uint8).reshape(len(pairs), C.sizeof(Scene))
+        cc = raw[:, Scene.coll_cont.offset:Scene.coll_cont.offset + 16].copy().view(np.int32)
+        for k, (_, out) in enumerate(pairs):
+            out["coll_cont"] = cc[k]
 
     def kernel_timing(self, on):
         """CUDA-event timing of every kernel kind (plain launches while on)."""
