@@ -104,18 +104,19 @@ struct Acc3 {
 // kns = {1/(1/kn_a + 1/kn_b), 1/(1/ks_a + 1/ks_b)} of the two materials
 // (2D_Simulation.wgsl:345-346), evaluated once per material pair on the host
 // with the same float operations
+// L = len2f(pa - pb), which the caller computes once per slot (every float
+// distance of the slot is this same value)
 __device__ __forceinline__ F3 linear_model(const ScenePar &P, float2 kns, float4 pa,
-                                           float4 da, float4 pb, float4 db, float length, float &tf,
+                                           float4 da, float4 pb, float4 db, float length, float L, float &tf,
                                            Acc3 &acc) {
     F3 out = {0.0f, 0.0f, 0.0f};
-    float d2 = distance2(P.use_f64, pa, pb, length);
+    float d2 = P.use_f64 ? distance2(1, pa, pb, length) : L - length;
     float nd = d2 < 0.0f ? d2 : 0.0f;
     if (nd == 0.0f) return out;
     float kn = kns.x;
     float ks = kns.y;
     float Fn = (-nd) * kn;
     float vx = pa.x - pb.x, vy = pa.y - pb.y;
-    float L = len2f(vx, vy);
     float nx = vx / L, ny = vy / L;
     float tx = -ny, ty = nx;
     float dra = da.z * pa.z;
@@ -952,9 +953,12 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         }
         const float2 kns = __ldg(&w.pair[P.pair_base + (int)meta_mat(m) * P.n_mat + (int)meta_mat(mb)]);
         F3 f = {0.0f, 0.0f, 0.0f};
+        // L = |pa - pb| in float, taken once per slot where the branch needs
+        // it: every float distance of the slot is this value (b - a differs
+        // from a - b only in sign, so the squares agree)
         if (bonded < 0 || bonds_model == 0) {
             float tf = tf0;
-            f = linear_model(P, kns, pa, da, pb, db, pa.z + pb.z, tf, acc);
+            f = linear_model(P, kns, pa, da, pb, db, pa.z + pb.z, len2f(pa.x - pb.x, pa.y - pb.y), tf, acc);
             w.s_tf[j * N + i] = tf;
         } else {
             const int bg = P.bond_base + bonded;
@@ -964,10 +968,10 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 const float Rr = P.lambda * (pa.z < pb.z ? pa.z : pb.z);
                 const float A = (2.0f * Rr) * 1.0f;
                 const float I = ((2.0f / 3.0f * Rr) * Rr) * Rr;
-                const float nd = distance2(P.use_f64, pa, pb, blen);
+                const float L = len2f(pa.x - pb.x, pa.y - pb.y);
+                const float nd = P.use_f64 ? distance2(1, pa, pb, blen) : L - blen;
                 float Fn = ((-kn) * nd) * A;
                 const float vx = pa.x - pb.x, vy = pa.y - pb.y;
-                const float L = len2f(vx, vy);
                 const float nx = vx / L, ny = vy / L;
                 const float tx = -ny, ty = nx;
                 const float dra = da.z * pa.z, drb = db.z * pb.z;
@@ -1004,17 +1008,17 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 acc.d1 = acc.d1 + btf;
                 acc.d2 = acc.d2 + M;
                 float tf = tf0;
-                const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, tf, acc);
+                const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, L, tf, acc);
                 w.s_tf[j * N + i] = tf;
                 f.x = Fx + lm.x;
                 f.y = Fy + lm.y;
                 f.z = M + lm.z;
             } else if (bonds_model == 1) {                         // :419-432
-                const float disp = distance1(P.use_f64, pa, pb);
+                const float L = len2f(pa.x - pb.x, pa.y - pb.y);
+                const float disp = P.use_f64 ? distance1(1, pa, pb) : L - (pa.z + pb.z);
                 float fx = 0.0f, fy = 0.0f;
                 const float sf = P.p.bond_normal_stiffness * disp;
                 const float vx = pb.x - pa.x, vy = pb.y - pa.y;
-                const float L = len2f(vx, vy);
                 fx = fx + sf * (vx / L);
                 fy = fy + sf * (vy / L);
                 if (P.p.bonds_tear == 1 && sf >= sn) {
@@ -1026,18 +1030,18 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     fy = 0.0f;
                 }
                 float tf = tf0;
-                const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, tf, acc);
+                const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, L, tf, acc);
                 w.s_tf[j * N + i] = tf;
                 f.x = lm.x + fx;
                 f.y = lm.y + fy;
                 f.z = lm.z + 0.0f;
             } else if (bonds_model == 2) {                         // :375-417
-                const float nd = distance1(P.use_f64, pa, pb);
+                const float L = len2f(pa.x - pb.x, pa.y - pb.y);
+                const float nd = P.use_f64 ? distance1(1, pa, pb) : L - (pa.z + pb.z);
                 const float kn = P.kb2;
                 const float ks = P.ksb2;
                 float Fn = (-nd) * kn;
                 const float vx = pa.x - pb.x, vy = pa.y - pb.y;
-                const float L = len2f(vx, vy);
                 const float nx = vx / L, ny = vy / L;
                 const float tx = -ny, ty = nx;
                 const float dra = da.z * pa.z, drb = db.z * pb.z;
