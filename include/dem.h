@@ -353,6 +353,13 @@ int dem_server_poll(dem_server *sv, int64_t *done_ids, int32_t cap, int32_t *n);
 int dem_server_fetch(dem_server *sv, int64_t id, dem_scene *out, double times[3]);
 int dem_server_events(dem_server *sv, int64_t id, dem_break_event *buf, int32_t cap, int32_t *n);
 int dem_server_release(dem_server *sv, int64_t id);
+/* Withdraws a request in any state: a queued one leaves the queue, a running
+ * one stops and its device ranges are freed, a finished one is released.
+ * Its id is unknown afterwards.  A request with more particles than the
+ * particle arena is refused at submit (DEM_E_CAPACITY); one that cannot be
+ * admitted even into empty arenas (cells, bonds, materials, large-particle
+ * records) is failed: poll lists it and fetch returns the admission error. */
+int dem_server_cancel(dem_server *sv, int64_t id);
 int dem_server_get_stats(dem_server *sv, dem_server_stats *out);
 void *dem_server_stream(dem_server *sv);
 

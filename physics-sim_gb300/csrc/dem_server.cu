@@ -11,6 +11,7 @@
 // countdown), so its result is the result of running it alone.
 #include <chrono>
 #include <cstring>
+#include <algorithm>
 #include <deque>
 #include <map>
 #include <memory>
@@ -75,7 +76,9 @@ struct Request {
     int64_t horizon = 0;
     int64_t steps_done = 0;
     int slot = -1;
-    int state = 0;  // 0 queued, 1 running, 2 done
+    int state = 0;  // 0 queued, 1 running, 2 done, 3 failed (can never be admitted)
+    int fail_code = 0;
+    std::string fail_msg;
     double t_submit = 0, t_admit = 0, t_done = 0;
     std::vector<dem_break_event> events;
 };
@@ -133,6 +136,17 @@ int retire_finished(dem_server *sv) {
     return DEM_OK;
 }
 
+// a queued request that cannot be admitted even into empty arenas is failed
+// (reported by poll, its error returned by fetch) so that the queue moves on
+void fail_request(dem_server *sv, Request &r, int code, const std::string &msg) {
+    r.state = 3;
+    r.fail_code = code;
+    r.fail_msg = msg;
+    r.t_done = now_s();
+    r.in = SceneCopy();
+    sv->done_unpolled.push_back(r.id);
+}
+
 int admit_queued(dem_server *sv) {
     // first come, first served; a request that does not fit waits at the head
     while (!sv->queue.empty()) {
@@ -145,7 +159,13 @@ int admit_queued(dem_server *sv) {
         e.bond_normal_strength = r.sn.empty() ? nullptr : r.sn.data();
         e.bond_shear_strength = r.ss.empty() ? nullptr : r.ss.data();
         int slot = sv->world.admit(&r.in.view, r.params, e, r.horizon);
-        if (slot == DEM_E_CAPACITY) break;
+        if (slot == DEM_E_CAPACITY && sv->active_particles > 0) break;  // waits for ranges to free
+        if (slot == DEM_E_CAPACITY || slot == DEM_E_INVALID || slot == DEM_E_UNSUPPORTED) {
+            // the request itself cannot run here: fail it, keep serving the rest
+            fail_request(sv, r, slot, sv->world.err);
+            sv->queue.pop_front();
+            continue;
+        }
         if (slot < 0) return src_(sv, slot);
         r.slot = slot;
         r.state = 1;
@@ -255,6 +275,9 @@ int dem_server_submit(dem_server *sv, const dem_scene *scene, const dem_params *
                       int64_t horizon_steps, int64_t *request_id) {
     SERVER_GUARD(sv);
     if (!scene || !params || horizon_steps <= 0) return sset(sv, DEM_E_INVALID, "bad request");
+    if (scene->n_particles < 0 || (long long)scene->n_particles > sv->world.a_part.capacity())
+        return sset(sv, DEM_E_CAPACITY, "request has more particles than the server's arena (" +
+                                            std::to_string(sv->world.a_part.capacity()) + ")");
     auto r = std::make_unique<Request>();
     r->id = sv->next_id++;
     r->in.from(*scene, true);
@@ -313,6 +336,7 @@ int dem_server_fetch(dem_server *sv, int64_t id, dem_scene *out, double times[3]
     auto it = sv->reqs.find(id);
     if (it == sv->reqs.end()) return sset(sv, DEM_E_INVALID, "unknown request id");
     Request &r = *it->second;
+    if (r.state == 3) return sset(sv, r.fail_code, "request failed at admission: " + r.fail_msg);
     if (r.state != 2) return sset(sv, DEM_E_STATE, "request not completed");
     if (times) {
         times[0] = r.t_submit;
@@ -355,7 +379,27 @@ int dem_server_release(dem_server *sv, int64_t id) {
     SERVER_GUARD(sv);
     auto it = sv->reqs.find(id);
     if (it == sv->reqs.end()) return sset(sv, DEM_E_INVALID, "unknown request id");
-    if (it->second->state != 2) return sset(sv, DEM_E_STATE, "request not completed");
+    if (it->second->state < 2) return sset(sv, DEM_E_STATE, "request not completed");
+    sv->reqs.erase(it);
+    return DEM_OK;
+}
+
+int dem_server_cancel(dem_server *sv, int64_t id) {
+    SERVER_GUARD(sv);
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end()) return sset(sv, DEM_E_INVALID, "unknown request id");
+    Request &r = *it->second;
+    if (r.state == 0) {
+        sv->queue.erase(std::find(sv->queue.begin(), sv->queue.end(), id));
+    } else if (r.state == 1) {
+        // between advances nothing of the scene is in flight: free its ranges
+        int rc = sv->world.retire(r.slot);
+        if (rc) return src_(sv, rc);
+        sv->slot_req[r.slot] = 0;
+        sv->active_particles -= r.in.view.n_particles;
+    }
+    sv->done_unpolled.erase(std::remove(sv->done_unpolled.begin(), sv->done_unpolled.end(), id),
+                            sv->done_unpolled.end());
     sv->reqs.erase(it);
     return DEM_OK;
 }

@@ -131,7 +131,8 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_server_poll", "dem_server_fetch", "dem_server_events", "dem_server_release",
            "dem_server_get_stats", "dem_server_stream", "dem_batch_autotune", "dem_tune_last_error",
            "dem_generate_bonds", "dem_bondgen_last_error", "dem_event", "dem_get_datum",
-           "dem_batch_event", "dem_batch_get_datum", "dem_batch_upload_many", "dem_batch_download_many"]
+           "dem_batch_event", "dem_batch_get_datum", "dem_batch_upload_many", "dem_batch_download_many",
+           "dem_server_cancel"]
 
 _lib = None
 
@@ -228,6 +229,7 @@ def lib(path=None):
     L.dem_server_fetch.argtypes = [C.c_void_p, C.c_int64, C.POINTER(Scene), C.POINTER(C.c_double)]
     L.dem_server_events.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
     L.dem_server_release.argtypes = [C.c_void_p, C.c_int64]
+    L.dem_server_cancel.argtypes = [C.c_void_p, C.c_int64]
     L.dem_server_get_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
     L.dem_server_stream.argtypes = [C.c_void_p]
     L.dem_server_stream.restype = C.c_void_p
@@ -770,6 +772,15 @@ class Server:
             self._check(lib().dem_server_release(self.h, int(rid)))
             self._templates.pop(rid, None)
         return out, (times[0], times[1], times[2]), ev
+
+    def cancel(self, rid):
+        """Withdraw a queued, running or finished request (dem_server_cancel)."""
+        self._check(lib().dem_server_cancel(self.h, int(rid)))
+        self._templates.pop(rid, None)
+
+    def release(self, rid):
+        self._check(lib().dem_server_release(self.h, int(rid)))
+        self._templates.pop(rid, None)
 
     def events(self, rid):
         n = C.c_int32(0)

@@ -6,8 +6,10 @@ at run time.  Outputs:
 
   *.bin        byte copies of the reference's small experiment saved states
                (saved_states/TEXPS.bin, Chain_TEXP.bin, PBEXPS.bin,
-               Chain_EXP.bin, Strings.bin) -- FlatBuffers `State` tables
-               (new_schema.fbs:86-104) carrying the experiment scripts
+               Chain_EXP.bin, Strings.bin, MicroStrings.bin) -- FlatBuffers
+               `State` tables (new_schema.fbs:86-104) carrying the
+               experiment scripts; MicroStrings holds 2048 particles, 4193
+               broken bonds and a NaN velocity
   traces.npz   every exported CSV trace of those experiments (data/TEXP_k.csv,
                data/Chain_T_k.csv, data/pb_experiment_k_1.csv, data/Chain_k.csv)
                as float64 arrays [rows, 12] in the column order of
@@ -24,7 +26,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REFERENCE = os.environ.get("REFERENCE", "/root/reference")
-STATES = ["TEXPS.bin", "Chain_TEXP.bin", "PBEXPS.bin", "Chain_EXP.bin", "Strings.bin"]
+STATES = ["TEXPS.bin", "Chain_TEXP.bin", "PBEXPS.bin", "Chain_EXP.bin", "Strings.bin", "MicroStrings.bin"]
 TRACE_GLOBS = ["TEXP_*.csv", "Chain_T_*.csv", "pb_experiment_*_1.csv", "Chain_[0-9]*.csv"]
 
 

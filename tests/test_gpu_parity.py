@@ -157,6 +157,38 @@ def test_strings_scene_bit_exact(golden_dir):
     assert len(gev) == len(oev)
 
 
+def test_nan_velocity_and_broken_bonds_scene_bit_exact(golden_dir):
+    """The reference's MicroStrings state: 2048 particles in strings, 4193
+    bonds already broken (code -9) and one NaN velocity; NaN compares equal
+    to NaN, every other bit must match."""
+    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "MicroStrings.bin"))
+    assert np.isnan(scene["vel"]).any()
+    g, o, gev, oev = run_both(scene, uni, 200, chunk=50, use_f64=info["use_f64"])
+    assert_same_state(g, o)
+    assert len(gev) == len(oev)
+
+
+def test_out_of_grid_and_nan_particles_bit_exact():
+    """Particles beyond the reference bucket grid find no partners (the
+    reference's clamped bucket loops are empty for them; circular bounds of
+    radius 1e6 keep them out there, since the rectangle walls always act,
+    2D_LOM.wgsl:101-145), and a NaN velocity turns its particle's position
+    NaN; GPU and oracle agree."""
+    sc, p, ext = dem_scenes.dense_bed(900, seed=5)
+    p = dict(p)
+    p["round_bounds"] = 1
+    p["bound_radius"] = 1.0e6
+    sc = copy_scene(sc)
+    pos = sc["pos"].reshape(-1, 2)
+    far = np.argsort(pos[:, 0])[-40:]          # the 40 right-most particles, still touching
+    pos[far, 0] += np.float32(2 * p["hor_bound"])   # one another, moved beyond the grid
+    sc["vel"].reshape(-1, 2)[450, 0] = np.float32("nan")
+    g, o, _, _ = run_both(sc, p, 120, chunk=40, reorder_interval=7)
+    assert np.isnan(g["pos"]).any()
+    assert not contact_pairs(o) & {(int(a), int(b)) for a in far for b in far}
+    assert_same_state(g, o)
+
+
 def test_broad_phase_keys_and_order():
     sc, p, ext = dem_scenes.c0_settle(n=3000, seed=2, box=(80, 120), spacing=2.3)
     with dem.Context(sc, p) as ctx:

@@ -87,3 +87,63 @@ def test_capacity_refuses_nothing_and_queues():
         ga, _, _ = out[a]
         gb, _, _ = out[b]
         assert_same_state(ga, gb)
+
+
+def test_request_beyond_the_arenas_is_refused_and_the_queue_moves_on():
+    """A request larger than the particle arena is refused at submit; one whose
+    bonds cannot fit even into empty arenas is failed at admission (poll lists
+    it, fetch raises the admission error) and the requests behind it run."""
+    small, p, ext = dem_scenes.dense_bed(900, seed=31)
+    chains = dem_scenes.c1_chains(chains=20, length=64, seed=32, pull_velocity=0.0)
+    with dem.Server(memory_budget_bytes=1 << 30, max_active_particles=2048, max_scenes=4,
+                    bonds_per_particle=0.0) as sv:
+        cap = sv.stats()["capacity_particles"]
+        big, pb, eb = dem_scenes.dense_bed(cap + 1000, seed=33)
+        with pytest.raises(dem.DemError) as e:
+            sv.submit(big, pb, 10, **eb)
+        assert e.value.code == -7
+        (csc, cp, cext) = chains
+        bad = sv.submit(csc, cp, 10, **cext)      # 20 x 63 bonds; the bond arena holds 1024
+        good = sv.submit(small, p, 40, **ext)
+        seen = set()
+        for _ in range(6):
+            sv.advance(35)
+            seen.update(sv.poll())
+        assert seen == {bad, good}
+        with pytest.raises(dem.DemError) as e:
+            sv.fetch(bad)
+        assert e.value.code == -7
+        sv.release(bad)
+        got, _, _ = sv.fetch(good)
+    ref, _ = _alone(small, p, ext, 40)
+    assert_same_state(got, ref)
+
+
+def test_cancel_queued_and_running_requests():
+    """Cancelling a running request frees its ranges and a queued one never
+    runs; the requests left give the results of running alone."""
+    a_sc, a_p, a_ext = dem_scenes.dense_bed(1500, seed=41)
+    b_sc, b_p, b_ext = dem_scenes.c3_mix_scene(1400, 0.3, 42)
+    c_sc, c_p, c_ext = dem_scenes.c3_mix_scene(1200, 0.2, 43)
+    with dem.Server(memory_budget_bytes=1 << 30, max_active_particles=1600, max_scenes=4) as sv:
+        a = sv.submit(a_sc, a_p, 400, **a_ext)
+        b = sv.submit(b_sc, b_p, 50, **b_ext)   # waits: a holds the particle budget
+        sv.advance(35)
+        st = sv.stats()
+        assert st["running"] == 1 and st["queued"] == 1
+        sv.cancel(b)
+        assert sv.stats()["queued"] == 0
+        sv.cancel(a)
+        st = sv.stats()
+        assert st["running"] == 0 and st["active_particles"] == 0
+        c = sv.submit(c_sc, c_p, 70, **c_ext)
+        done = {}
+        for _ in range(8):
+            sv.advance(35)
+            for rid in sv.poll():
+                done[rid] = sv.fetch(rid)
+        assert set(done) == {c}
+        with pytest.raises(dem.DemError):
+            sv.events(a)                         # the cancelled id is unknown
+    ref, _ = _alone(c_sc, c_p, c_ext, 70)
+    assert_same_state(done[c][0], ref)

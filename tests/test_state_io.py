@@ -14,11 +14,13 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def _same_scene(a, b):
+    """Every array bit for bit (a saved NaN must come back as the same NaN)."""
     for k in a:
         if k == "grid":
             assert a[k] == b[k]
         else:
-            assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
+            x, y = np.asarray(a[k]), np.asarray(b[k])
+            assert x.dtype == y.dtype and x.shape == y.shape and x.tobytes() == y.tobytes(), k
 
 
 @pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.bin"))), ids=os.path.basename)
