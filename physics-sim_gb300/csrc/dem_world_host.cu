@@ -540,45 +540,171 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
     h.n = n;
     h.n_bonds = sc->n_bonds;
     h.n_mat = sc->n_materials;
+    // One pass over the particles: the first invalid one, the largest
+    // radius, the bounding box of the finite positions of nonzero radii, and
+    // the large-particle threshold: 4x the median of the nonzero radii when
+    // few particles (at most max(64, n/256)) lie above it; the search cells
+    // are then sized by the largest of the others.  Large scenes split the
+    // pass over host threads (results identical: the lowest invalid index
+    // decides the message, the reductions do not depend on order, and the
+    // median is selected exactly).
+    const int T = n >= (1 << 18) ? std::max(1, std::min(layout_threads, n >> 16)) : 1;
+    struct Part {
+        int bad = INT_MAX, bad_kind = 0;
+        float rmax = 0.0f, xmin = 0, xmax = 0, ymin = 0, ymax = 0;
+        bool any = false;
+        std::vector<uint32_t> hist;  // nonzero radii by their 16 high bits
+    };
+    std::vector<Part> parts(T);
+    auto scan = [&](int t) {
+        Part &q = parts[t];
+        const int i0 = (int)((long long)n * t / T), i1 = (int)((long long)n * (t + 1) / T);
+        if (T > 1) q.hist.assign(1 << 16, 0u);
+        for (int i = i0; i < i1; ++i) {
+            const float r = sc->radii[i];
+            if (!(r >= 0.0f) || !std::isfinite(r)) {
+                q.bad = i;
+                q.bad_kind = 1;
+                return;
+            }
+            q.rmax = std::max(q.rmax, r);
+            const int32_t mp = sc->material_pointers[i];
+            if (mp < 0 || mp >= sc->n_materials) {
+                q.bad = i;
+                q.bad_kind = 2;
+                return;
+            }
+            const float x = sc->pos[2 * i], y = sc->pos[2 * i + 1];
+            if (std::isfinite(x) && std::isfinite(y) && r > 0.0f) {
+                if (!q.any) {
+                    q.xmin = q.xmax = x;
+                    q.ymin = q.ymax = y;
+                    q.any = true;
+                }
+                q.xmin = std::min(q.xmin, x);
+                q.xmax = std::max(q.xmax, x);
+                q.ymin = std::min(q.ymin, y);
+                q.ymax = std::max(q.ymax, y);
+            }
+            if (T > 1 && r > 0.0f) {
+                uint32_t bits;
+                std::memcpy(&bits, &r, 4);
+                q.hist[bits >> 16]++;
+            }
+        }
+    };
+    if (T == 1) {
+        scan(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < T; ++t) pool.emplace_back(scan, t);
+        for (auto &th : pool) th.join();
+    }
     float rmax = 0.0f;
     float xmin = 0, xmax = 0, ymin = 0, ymax = 0;
     bool any = false;
-    for (int i = 0; i < n; ++i) {
-        float r = sc->radii[i];
-        if (!(r >= 0.0f) || !std::isfinite(r)) return fail(DEM_E_INVALID, "radius must be finite and >= 0");
-        rmax = std::max(rmax, r);
-        int32_t mp = sc->material_pointers[i];
-        if (mp < 0 || mp >= sc->n_materials) return fail(DEM_E_INVALID, "material pointer out of range");
-        float x = sc->pos[2 * i], y = sc->pos[2 * i + 1];
-        if (std::isfinite(x) && std::isfinite(y) && r > 0.0f) {
-            if (!any) { xmin = xmax = x; ymin = ymax = y; any = true; }
-            xmin = std::min(xmin, x); xmax = std::max(xmax, x);
-            ymin = std::min(ymin, y); ymax = std::max(ymax, y);
+    {
+        int bad = INT_MAX, kind = 0;
+        for (const Part &q : parts)
+            if (q.bad < bad) {
+                bad = q.bad;
+                kind = q.bad_kind;
+            }
+        if (kind == 1) return fail(DEM_E_INVALID, "radius must be finite and >= 0");
+        if (kind == 2) return fail(DEM_E_INVALID, "material pointer out of range");
+        for (const Part &q : parts) {
+            rmax = std::max(rmax, q.rmax);
+            if (!q.any) continue;
+            if (!any) {
+                xmin = q.xmin; xmax = q.xmax; ymin = q.ymin; ymax = q.ymax;
+                any = true;
+            }
+            xmin = std::min(xmin, q.xmin); xmax = std::max(xmax, q.xmax);
+            ymin = std::min(ymin, q.ymin); ymax = std::max(ymax, q.ymax);
         }
     }
-    // contact records are checked on the device as they are staged (stage_scene)
-    // Large particles: radius above 4x the median of the nonzero radii, when
-    // there are few of them (at most max(64, n/256)); the search cells are
-    // then sized by the largest of the others.
+    // contact records are checked on the device as they are staged (stage_many)
     h.r_big = std::numeric_limits<float>::infinity();
     h.n_big = 0;
     {
-        std::vector<float> rs;
-        rs.reserve(n);
-        for (int i = 0; i < n; ++i)
-            if (sc->radii[i] > 0.0f) rs.push_back(sc->radii[i]);
-        if (!rs.empty()) {
-            std::nth_element(rs.begin(), rs.begin() + rs.size() / 2, rs.end());
-            const float thr = 4.0f * rs[rs.size() / 2];
-            int cnt = 0;
+        // the median of the nonzero radii: the element of rank m/2 in
+        // ascending order (what nth_element at rs.size()/2 returns)
+        float med = 0.0f;
+        long long m = 0;
+        if (T == 1) {
+            std::vector<float> rs;
+            rs.reserve(n);
+            for (int i = 0; i < n; ++i)
+                if (sc->radii[i] > 0.0f) rs.push_back(sc->radii[i]);
+            m = (long long)rs.size();
+            if (m > 0) {
+                std::nth_element(rs.begin(), rs.begin() + m / 2, rs.end());
+                med = rs[m / 2];
+            }
+        } else {
+            // positive floats order as their bit patterns: find the 16-bit
+            // bucket holding rank m/2, then select inside that bucket
+            std::vector<uint64_t> hist(1 << 16, 0);
+            for (const Part &q : parts)
+                for (int b = 0; b < (1 << 16); ++b) hist[b] += q.hist[b];
+            for (int b = 0; b < (1 << 16); ++b) m += (long long)hist[b];
+            if (m > 0) {
+                long long k = m / 2, below = 0;
+                int bucket = 0;
+                while (below + (long long)hist[bucket] <= k) below += (long long)hist[bucket++];
+                std::vector<std::vector<float>> ins(T);
+                std::vector<std::thread> pool;
+                for (int t = 0; t < T; ++t)
+                    pool.emplace_back([&, t]() {
+                        const int i0 = (int)((long long)n * t / T), i1 = (int)((long long)n * (t + 1) / T);
+                        for (int i = i0; i < i1; ++i) {
+                            const float r = sc->radii[i];
+                            uint32_t bits;
+                            std::memcpy(&bits, &r, 4);
+                            if (r > 0.0f && (int)(bits >> 16) == bucket) ins[t].push_back(r);
+                        }
+                    });
+                for (auto &th : pool) th.join();
+                std::vector<float> in;
+                in.reserve(hist[bucket]);
+                for (const auto &v : ins) in.insert(in.end(), v.begin(), v.end());
+                std::nth_element(in.begin(), in.begin() + (k - below), in.end());
+                med = in[k - below];
+            }
+        }
+        if (m > 0) {
+            const float thr = 4.0f * med;
+            std::vector<long long> cnts(T, 0);
+            std::vector<float> smalls(T, 0.0f);
+            auto count = [&](int t) {
+                const int i0 = (int)((long long)n * t / T), i1 = (int)((long long)n * (t + 1) / T);
+                long long c = 0;
+                float rs = 0.0f;
+                for (int i = i0; i < i1; ++i) {
+                    const float r = sc->radii[i];
+                    if (!(r > 0.0f)) continue;
+                    if (r > thr) ++c;
+                    else rs = std::max(rs, r);
+                }
+                cnts[t] = c;
+                smalls[t] = rs;
+            };
+            if (T == 1) {
+                count(0);
+            } else {
+                std::vector<std::thread> pool;
+                for (int t = 0; t < T; ++t) pool.emplace_back(count, t);
+                for (auto &th : pool) th.join();
+            }
+            long long cnt = 0;
             float rsmall = 0.0f;
-            for (float r : rs) {
-                if (r > thr) ++cnt;
-                else rsmall = std::max(rsmall, r);
+            for (int t = 0; t < T; ++t) {
+                cnt += cnts[t];
+                rsmall = std::max(rsmall, smalls[t]);
             }
             if (cnt > 0 && cnt <= std::max(64, n / 256)) {
                 h.r_big = thr;
-                h.n_big = cnt;
+                h.n_big = (int)cnt;
                 rmax = rsmall;
             }
         }
@@ -966,6 +1092,7 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     split_narrow = ext.split_narrow != 0;
     fuse_lom = ext.unfused_lom == 0;
     host_direct = ext.host_copies == 0 && device_reads_pageable();
+    layout_threads = host_threads();
     diagnostics = ext.diagnostics != 0;
     sh.assign(S, SceneHost{});
     long long N = 0, C = 0, B = 0, M = 0, MP = 0, TB = 0;
@@ -1057,6 +1184,7 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     split_narrow = ext.split_narrow != 0;
     fuse_lom = ext.unfused_lom == 0;
     host_direct = ext.host_copies == 0 && device_reads_pageable();
+    layout_threads = host_threads();
     diagnostics = ext.diagnostics != 0;
     const int S = scenes + 1;  // the last slot owns the unused particles
     free_slot = scenes;
@@ -1247,6 +1375,7 @@ int World::upload_many(const int32_t *idx, const dem_scene *const *scs, int coun
         for (int t = 0; t < T; ++t)
             pool.emplace_back([&, t]() {
                 scratch[t].skin_factor = skin_factor;
+                scratch[t].layout_threads = std::max(1, host_threads() / count);
                 for (int k = t; k < count; k += T) {
                     rcs[k] = scratch[t].compute_layout(probes[k], scs[k]);
                     if (rcs[k]) errs[k] = scratch[t].err;

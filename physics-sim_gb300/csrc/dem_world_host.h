@@ -133,6 +133,7 @@ class World {
     void fill_par(SceneHost &h);
     int push_par(int s);
     int push_det();
+    int layout_threads = 1;  // host threads compute_layout may use on a large scene
     int stage_many(const int32_t *idx, const dem_scene *const *scs, int count, const SceneHost *probes,
                    const std::function<int()> &layouts);
     int force_rebuild();

@@ -189,6 +189,29 @@ def test_out_of_grid_and_nan_particles_bit_exact():
     assert_same_state(g, o)
 
 
+def test_large_scene_layout_on_host_threads_bit_exact():
+    """Above 2^18 particles the layout is derived on host threads (the median
+    radius from a histogram of the radii's float bits, then a selection in
+    one bucket): the large particles are those of the serial rule (4x the
+    median of the nonzero radii, at most max(64, n/256) of them), and the
+    run equals the oracle."""
+    sc, p, ext = dem_scenes.c2_impact(cols=512, rows=600, seed=3, projectile_radius=12.0,
+                                      projectile_speed=80.0, projectiles=3)
+    n = len(sc["radii"])
+    assert n >= 1 << 18
+    r = sc["radii"]
+    nz = r[r > 0]
+    med = np.partition(nz, nz.size // 2)[nz.size // 2]
+    big = set(np.nonzero(r > 4 * med)[0].tolist())
+    assert 0 < len(big) <= max(64, n // 256)
+    with dem.Context(sc, p, **ext) as ctx:
+        keys, order, cell_start = ctx.broad_phase()
+    last = set(np.nonzero(keys == keys.max())[0].tolist())
+    assert last == big | set(np.nonzero(r == 0)[0].tolist())
+    g, o, _, _ = run_both(sc, p, 12, **ext)
+    assert_same_state(g, o)
+
+
 def test_broad_phase_keys_and_order():
     sc, p, ext = dem_scenes.c0_settle(n=3000, seed=2, box=(80, 120), spacing=2.3)
     with dem.Context(sc, p) as ctx:
