@@ -566,6 +566,31 @@ def autotune(items, *, device=-1, sample_particles=0, trial_steps=0, **world_kw)
     return chosen, info
 
 
+class SceneTable:
+    """The dem_scene structs of [(scene index, scene dict), ...] in one array,
+    as a C caller keeps them: pointers into the dicts' arrays, with the
+    coll_cont and grid values of the moment it is built (build it again after
+    replacing an array or changing those values).  Bulk calls accept it in
+    place of the list, which spares re-marshalling hundreds of scenes."""
+
+    def __init__(self, pairs):
+        self.pairs = list(pairs)
+        self.n = len(self.pairs)
+        self.structs = (Scene * self.n)()
+        for k, (_, sc) in enumerate(self.pairs):
+            make_scene(sc, self.structs[k])
+        self.idx = np.array([int(k) for k, _ in self.pairs], dtype=np.int32)
+        self.ptrs = np.arange(self.n, dtype=np.uint64) * C.sizeof(Scene) + C.addressof(self.structs)
+
+    def read_control(self):
+        """coll_cont of every struct (written by a download) into its dict."""
+        raw = np.frombuffer(self.structs, dtype=np.uint8).reshape(self.n, C.sizeof(Scene))
+        off = Scene.coll_cont.offset
+        cc = raw[:, off:off + 16].copy().view(np.int32)
+        for k, (_, out) in enumerate(self.pairs):
+            out["coll_cont"] = cc[k]
+
+
 class Batch:
     """Many independent scenes resident on one GPU, stepped together
     (dem_batch_*).  `items` is a list of (scene, params, ext) triples as the
@@ -635,32 +660,20 @@ class Batch:
         st = make_scene(sc)
         self._check(lib().dem_batch_upload(self.h, int(scene), C.byref(st)))
 
-    @staticmethod
-    def _scene_table(pairs):
-        """The pairs' scene structs in one array, their indices and pointers."""
-        n = len(pairs)
-        structs = (Scene * n)()
-        for k, (_, sc) in enumerate(pairs):
-            make_scene(sc, structs[k])
-        idx = np.array([int(k) for k, _ in pairs], dtype=np.int32)
-        ptrs = np.arange(n, dtype=np.uint64) * C.sizeof(Scene) + C.addressof(structs)
-        return structs, idx, ptrs
-
     def upload_many(self, pairs):
-        """[(scene index, scene dict), ...] in one call (dem_batch_upload_many)."""
-        structs, idx, ptrs = self._scene_table(pairs)
-        self._check(lib().dem_batch_upload_many(self.h, len(pairs), C.c_void_p(idx.ctypes.data),
-                                                C.c_void_p(ptrs.ctypes.data)))
+        """[(scene index, scene dict), ...] -- or a SceneTable of them -- in one
+        call (dem_batch_upload_many)."""
+        t = pairs if isinstance(pairs, SceneTable) else SceneTable(pairs)
+        self._check(lib().dem_batch_upload_many(self.h, t.n, C.c_void_p(t.idx.ctypes.data),
+                                                C.c_void_p(t.ptrs.ctypes.data)))
 
     def download_many(self, pairs):
-        """[(scene index, scene dict to fill), ...] in one call (dem_batch_download_many)."""
-        structs, idx, ptrs = self._scene_table(pairs)
-        self._check(lib().dem_batch_download_many(self.h, len(pairs), C.c_void_p(idx.ctypes.data),
-                                                  C.c_void_p(ptrs.ctypes.data)))
-        raw = np.frombuffer(structs, dtype=np.uint8).reshape(len(pairs), C.sizeof(Scene))
-        cc = raw[:, Scene.coll_cont.offset:Scene.coll_cont.offset + 16].copy().view(np.int32)
-        for k, (_, out) in enumerate(pairs):
-            out["coll_cont"] = cc[k]
+        """[(scene index, scene dict to fill), ...] -- or a SceneTable of them --
+        in one call (dem_batch_download_many)."""
+        t = pairs if isinstance(pairs, SceneTable) else SceneTable(pairs)
+        self._check(lib().dem_batch_download_many(self.h, t.n, C.c_void_p(t.idx.ctypes.data),
+                                                  C.c_void_p(t.ptrs.ctypes.data)))
+        t.read_control()
 
     def kernel_timing(self, on):
         """CUDA-event timing of every kernel kind (plain launches while on)."""

@@ -92,7 +92,11 @@ def test_bulk_upload_and_download_equal_per_scene_calls():
         for x in bulk:
             for key in ("pos", "vel", "contacts", "data"):
                 x[key][:] = 0
-        b.download_many(list(enumerate(bulk)))
+        table = dem.SceneTable(list(enumerate(bulk)))  # built once, used twice
+        b.download_many(table)
+        for x in bulk:
+            x["vel"][:] = 0
+        b.download_many(table)
         for k in range(len(items)):
             assert_same_state(bulk[k], per[k], "download_many scene %d: " % k)
             assert np.array_equal(bulk[k]["fixity"], per[k]["fixity"])
