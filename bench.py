@@ -117,6 +117,21 @@ def build_batch_workload(n_scenes, seed):
     return items, desc
 
 
+def job_rate(units, dev_ms, ws, device):
+    """Whole-job throughput of the replicas: the units every rank processed
+    (summed over ranks) over the slowest rank's device time (max over ranks).
+    Returns (units per second, max ms, total units)."""
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+        m = torch.tensor([float(dev_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        dist.all_reduce(m, op=dist.ReduceOp.MAX)
+        units, dev_ms = float(u.item()), float(m.item())
+    return units / (dev_ms / 1e3), dev_ms, units
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -363,11 +378,7 @@ def run_ours(args):
     launches = ctx.stats()["kernel_launches"] - launches0
     sampler.stop()
     dev_ms = sum(a.elapsed_time(b) for a, b in evs)
-    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = n * F * args.steps * ws / (max_ms / 1e3)
+    value, max_ms, _ = job_rate(n * F * args.steps, dev_ms, ws, dev)
     clocks = sampler.summary()
 
     # roofline pass: events around every k_interact launch, same stream, plain launches
@@ -411,7 +422,8 @@ def run_ours(args):
     barrier()
     e2e_s = time.perf_counter() - t0
     del out, _dem
-    e2e = {"value": n * F * e2e_n * ws / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+    e2e = {"value": job_rate(n * F * e2e_n, e2e_s * 1e3, ws, dev)[0], "unit": "particle-steps/s",
+           "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h,
            "note": "dem_upload (restore) of the whole scene + dem_step(frame) + dem_download (update_state)"}
 
@@ -548,11 +560,7 @@ def run_ours_batch(args):
     launches = st["kernel_launches"] - launches0
     sampler.stop()
     dev_ms = sum(a.elapsed_time(b) for a, b in evs)
-    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = ntot * F * args.steps * ws / (max_ms / 1e3)
+    value, max_ms, _ = job_rate(ntot * F * args.steps, dev_ms, ws, dev)
     clocks = sampler.summary()
 
     # the same scenes through the plain single-scene path, one after another
@@ -618,7 +626,8 @@ def run_ours_batch(args):
     barrier()
     e2e_s = time.perf_counter() - t0
     del outs, up_tab, down_tab
-    e2e = {"value": ntot * F * e2e_n * ws / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+    e2e = {"value": job_rate(ntot * F * e2e_n, e2e_s * 1e3, ws, dev)[0], "unit": "particle-steps/s",
+           "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": h2d,
            "note": "dem_batch_upload_many of all scenes + dem_batch_step(frame) + dem_batch_download_many of all "
                    "scenes, from and into the callers' host arrays (scene struct tables built once)"}
