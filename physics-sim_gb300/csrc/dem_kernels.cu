@@ -841,11 +841,16 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         } else if (lc != NL_OVERFLOW) {
             const int4 lb = lc > 7 ? __ldg(&w.nl[2 * (size_t)i + 1]) : make_int4(0, 0, 0, 0);
             // distance tests first, all gathers independent; then the bucket
-            // test and ordering of the partners that touch
+            // test and ordering of the partners that touch.  The unrolled
+            // tests stop at the longest list among the warp's lanes here
+            // (a warp-uniform exit: sparse warps skip the empty tail).
             uint32_t pass = 0u;
+            const int lmax = __reduce_max_sync(__activemask(), lc);
 #pragma unroll
-            for (int k = 1; k <= NL; ++k)
+            for (int k = 1; k <= NL; ++k) {
+                if (k > lmax) break;
                 if (k <= lc && touching(pa, __ldg(&w.pr[i + nl_entry(la, lb, k)]))) pass |= 1u << k;
+            }
             if (pass || (h0 & NL_NEAR_BIG)) unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
             for (; pass; pass &= pass - 1)
                 accept_partner(w, i + nl_entry(la, lb, __ffs(pass) - 1), ax0, ax1, ay0, ay1, nr);
