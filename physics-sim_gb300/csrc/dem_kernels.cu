@@ -283,9 +283,16 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
 // With w.ticket the kernel's last warp sets the rebuild conditional; without
 // it (large worlds, where thousands of fenced ticket atomics cost more than a
 // launch) k_decide does it.
+// a 128-particle chunk holding at least one particle of a scene (served
+// worlds keep the map; elsewhere every chunk is live).  Warps never straddle
+// chunks, so the test is warp-uniform.
+__device__ __forceinline__ bool chunk_live(const DevWorld &w, int i) {
+    return w.live == nullptr || __ldg(&w.live[i >> 7]) != 0;
+}
+
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_lom(DevWorld w, int in_graph, cudaGraphConditionalHandle cond) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) lom_particle(w, i);
+    if (i < w.N && chunk_live(w, i)) lom_particle(w, i);
     if (w.ticket && last_warp(&w.tickets[0])) {
         if ((threadIdx.x & 31) == 0) {
             int need = *(volatile int32_t *)w.rebuild;
@@ -1194,7 +1201,7 @@ __global__ void __launch_bounds__(IB, 12) k_interact(DevWorld w, int in_graph, c
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle<0, FUSE>(w, i, nr, lom_final != 0);
+    if (i < w.N && chunk_live(w, i)) interact_particle<0, FUSE>(w, i, nr, lom_final != 0);
     interact_tail(w, FUSE, in_graph, cond);
 }
 
@@ -1202,7 +1209,7 @@ __global__ void __launch_bounds__(IB, 12) k_narrow(DevWorld w) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle<1, false>(w, i, nr, false);
+    if (i < w.N && chunk_live(w, i)) interact_particle<1, false>(w, i, nr, false);
 }
 
 template <bool FUSE>
@@ -1211,7 +1218,7 @@ __global__ void __launch_bounds__(IB, 9) k_forces(DevWorld w, int in_graph, cuda
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N) interact_particle<2, FUSE>(w, i, nr, lom_final != 0);
+    if (i < w.N && chunk_live(w, i)) interact_particle<2, FUSE>(w, i, nr, lom_final != 0);
     interact_tail(w, FUSE, in_graph, cond);
 }
 

@@ -161,6 +161,8 @@ struct DevWorld {
     int32_t *big_scene;         // [slots] scene of each big-partner record, -1 unused
     int32_t n_big_slots;
     int32_t *det;               // [S] narrow phase runs in the current step
+    const uint8_t *live;        // [ceil(N/128)] 0: every particle of the 128-particle chunk is free
+                                // (served worlds: the step kernels skip it); null: all chunks live
     int32_t *act;               // [S] 1 = the scene steps; 0 = frozen (finished or free slot)
     long long *remaining;       // [S] steps left before the scene freezes (served scenes)
 };

@@ -417,6 +417,24 @@ void World::release() {
     owned.clear();
     d = DevWorld{};
     spare = DevWorld{};
+    live_d = nullptr;
+}
+
+// served worlds: the 128-particle chunks that hold a particle of a scene in
+// use (the step kernels skip the others)
+int World::update_live() {
+    if (!live_d) return DEM_OK;
+    const size_t chunks = ((size_t)d.N + 127) / 128;
+    std::vector<uint8_t> live(chunks, 0);
+    for (size_t s = 0; s < sh.size(); ++s) {
+        const SceneHost &h = sh[s];
+        if ((int)s == free_slot || h.n <= 0) continue;
+        for (size_t c = (size_t)h.particle_base / 128; c <= ((size_t)h.particle_base + h.n - 1) / 128; ++c)
+            live[c] = 1;
+    }
+    CK(cudaMemcpyAsync(live_d, live.data(), chunks, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    return DEM_OK;
 }
 
 template <class T>
@@ -1200,6 +1218,15 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
                    ev_cap);
     if (rc) return rc;
     launch_mark_free(d, 0, (int)particles, free_slot, stream);
+    {
+        // the live map: every chunk free until a scene is admitted
+        bool ok = true;
+        const size_t chunks = ((size_t)particles + 127) / 128;
+        live_d = dalloc<uint8_t>(owned, chunks, ok);
+        if (!ok) return fail(DEM_E_OOM, "live map allocation failed");
+        CK(cudaMemsetAsync(live_d, 0, chunks, stream));
+        d.live = live_d;
+    }
     a_big.reset(bigs);
     a_part.reset(particles);
     a_cell.reset(cells);
@@ -1289,6 +1316,7 @@ int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e
     }
     if (rc == DEM_OK) rc = push_active(s, true, horizon);
     if (rc == DEM_OK) rc = push_det();
+    if (rc == DEM_OK) rc = update_live();
     if (rc == DEM_OK) rc = force_rebuild();
     if (rc != DEM_OK) {
         retire(s);
@@ -1318,6 +1346,8 @@ int World::retire(int s) {
     h.params.collision_interval = 1;
     h.n_cells = 1;
     free_slots.push_back(s);
+    rc = update_live();
+    if (rc) return rc;
     return force_rebuild();
 }
 

@@ -134,6 +134,8 @@ class World {
     int push_par(int s);
     int push_det();
     int layout_threads = 1;  // host threads compute_layout may use on a large scene
+    uint8_t *live_d = nullptr;  // served worlds: the live map of 128-particle chunks (DevWorld::live)
+    int update_live();
     int stage_many(const int32_t *idx, const dem_scene *const *scs, int count, const SceneHost *probes,
                    const std::function<int()> &layouts);
     int force_rebuild();
