@@ -887,26 +887,6 @@ int World::push_active(int s, bool on, long long steps) {
 }
 
 // ---- staging: reference layout -> internal layout --------------------------
-// the staging arrays of a scene whose particles start at `off` in the block
-RefArrays World::ref_at(long long off) const {
-    RefArrays r = ref;
-    r.pos += 2 * off;
-    r.radii += off;
-    r.vel += 2 * off;
-    r.acc += 2 * off;
-    r.rot += off;
-    r.rot_vel += off;
-    r.rot_acc += off;
-    r.forces += 6 * off;
-    r.del_pos += 2 * off;
-    r.del_rot += off;
-    r.data += 7 * off;
-    r.fixity += 6 * off;
-    r.contacts += 84 * off;
-    r.material_pointers += off;
-    return r;
-}
-
 int World::stage_error(int32_t e) {
     if (e & 1) return fail(DEM_E_INVALID, "material pointer out of range");
     if (e & 2) return fail(DEM_E_INVALID, "contact bonded index beyond n_bonds");

@@ -164,7 +164,6 @@ class World {
     bool host_direct = false;  // the device reads and writes the callers' arrays (dem_ext::host_copies)
     std::vector<cudaEvent_t> xfer_ev;  // one per chunk of a pipelined download
     int ensure_events(int count);
-    RefArrays ref_at(long long off) const;
     int stage_error(int32_t e);
     int layout_fits(int s, const SceneHost &probe);
     void apply_layout(int s, const SceneHost &probe);
