@@ -834,6 +834,9 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     if (detect) {                                                  // :126-228
         nr.cnt = 0;
         int ax0, ax1, ay0, ay1;
+        bool direct = false;       // accepted partners that own a slot only mark it found
+        int n_acc = 0;             // partners accepted in direct mode
+        uint32_t found_slots = 0u;
         const int4 la = __ldg(&w.nl[2 * (size_t)i]);
         const int h0 = la.x & 0xFFFF;
         const int lc = h0 & 0xFF;
@@ -859,8 +862,40 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 if (k <= lc && touching(pa, __ldg(&w.pr[i + nl_entry(la, lb, k)]))) pass |= 1u << k;
             }
             if (pass || (h0 & NL_NEAR_BIG)) unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
-            for (; pass; pass &= pass - 1)
-                accept_partner(w, i + nl_entry(la, lb, __ffs(pass) - 1), ax0, ax1, ay0, ay1, nr);
+            // With at most 14 partners touching and no large particle near,
+            // the accepted list is never cut at 14, so a partner that already
+            // owns a slot needs no key: it only marks the slot found.  The
+            // others are keyed and ordered for creation as usual.
+            direct = !(h0 & NL_NEAR_BIG) && __popc(pass) <= K;
+            if (direct) {
+                for (; pass; pass &= pass - 1) {
+                    const int b = i + nl_entry(la, lb, __ffs(pass) - 1);
+                    int bx0, bx1, by0, by1;
+                    unpack_range(__ldg(&w.rr[b]), bx0, bx1, by0, by1);
+                    if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) continue;
+                    ++n_acc;
+                    uint32_t hit = 0u;
+                    for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
+                        const int j = __ffs(left) - 1;
+                        if (w.s_b[j * N + i] == b) hit |= 1u << j;
+                    }
+                    if (hit) {
+                        found_slots |= hit;
+                        continue;
+                    }
+                    const int fy = by0 > ay0 ? by0 : ay0;
+                    const int fx = bx0 > ax0 ? bx0 : ax0;
+                    unsigned rank = (unsigned)((fy - ay0) * (ax1 - ax0 + 1) + (fx - ax0));
+                    if (rank > 15u) {
+                        atomicOr(w.err, 2);
+                        rank = 15u;
+                    }
+                    top14_insert((rank << 28) | (uint32_t)__ldg(&w.orig[b]), b, nr);
+                }
+            } else {
+                for (; pass; pass &= pass - 1)
+                    accept_partner(w, i + nl_entry(la, lb, __ffs(pass) - 1), ax0, ax1, ay0, ay1, nr);
+            }
             if (h0 & NL_NEAR_BIG) {
                 int bb, bn;
                 big_range(w, P, bb, bn);
@@ -885,18 +920,20 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         }
         const int cnt = nr.cnt;
         const int t = threadIdx.x;
-        if (cnt == K) atomicAdd(&w.stats[0], 1ull);
+        if ((direct ? n_acc : cnt) == K) atomicAdd(&w.stats[0], 1ull);
         // delete contacts that were not found (:185-204); `matched` marks the
         // accepted partners that already own a slot
         uint32_t matched = 0u;
         for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
             const int j = __ffs(left) - 1;
-            const int sb = w.s_b[j * N + i];
-            bool found = false;
-            for (int q = 0; q < cnt; ++q) {
-                const bool hit = nr_ci[q * IB + t] == sb;
-                found |= hit;
-                matched |= hit ? (1u << q) : 0u;
+            bool found = (found_slots >> j) & 1u;
+            if (!direct) {
+                const int sb = w.s_b[j * N + i];
+                for (int q = 0; q < cnt; ++q) {
+                    const bool hit = nr_ci[q * IB + t] == sb;
+                    found |= hit;
+                    matched |= hit ? (1u << q) : 0u;
+                }
             }
             if (found) continue;
             const bool bonded_nn = (mask >> (BSHIFT + j)) & 1u;   // bonded >= 0
