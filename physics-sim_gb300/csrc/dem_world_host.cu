@@ -1014,7 +1014,12 @@ int World::stage_many(const int32_t *idx, const dem_scene *const *scs, int count
         if (ce == cudaSuccess)
             ce = cudaMemcpyAsync(h_err, d_item_err, 4 * (size_t)nt, cudaMemcpyDeviceToHost, stream);
     }
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+    {
+        // waited for even after a failed call: until then the copies may be
+        // reading the callers' arrays
+        const cudaError_t se = cudaStreamSynchronize(stream);
+        if (ce == cudaSuccess) ce = se;
+    }
     if (ce != cudaSuccess) return fail(DEM_E_CUDA, cudaGetErrorString(ce));
     for (int i = 0; i < nt; ++i)
         if (h_err[i]) {
@@ -1864,8 +1869,10 @@ int World::download_many(const int32_t *idx, dem_scene *const *outs, int count) 
             launch_copies(d_copies, nc, pieces, d_item_err + nt, stream);
             CK(cudaGetLastError());
         }
-        CK(fetch_bonds());
-        CK(cudaStreamSynchronize(stream));
+        cudaError_t ce = fetch_bonds();
+        const cudaError_t se = cudaStreamSynchronize(stream);  // the copies write the callers' arrays until then
+        if (ce == cudaSuccess) ce = se;
+        if (ce != cudaSuccess) return fail(DEM_E_CUDA, cudaGetErrorString(ce));
         rc = first_error();
         if (rc) return rc;
         par_for(count, [&](int k) { host_part(k, false); });
