@@ -484,6 +484,65 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_cell_order(DevWorld w, const
     }
 }
 
+// Grouping by contact count: within each window of WIN consecutive
+// cell-order positions, the particles of a scene's search cells are put in
+// order of their number of occupied slots (ties by position), so that the
+// warps of the Simulation kernels hold particles with similar contact (and
+// candidate) counts and diverge less; particles stay in their window, so
+// neighbours stay close in memory.  Positions of other scenes, and of the
+// large and zero-radius particles' cells, do not move.  No result depends on
+// the order: every order-dependent choice keys on original indices.
+// wperm[r] = the position the particle at cell-order position r takes.
+constexpr int WIN = 128;
+__global__ void __launch_bounds__(WIN) k_window_order(DevWorld w, const int32_t *gate) {
+    if (gated_off(gate)) return;
+    __shared__ uint32_t key[WIN];
+    __shared__ uint32_t seg_id[WIN];
+    __shared__ int wsum[WIN / 32];
+    const int total = w.cell_start[w.C];
+    const int r0 = blockIdx.x * WIN;
+    if (r0 >= total) return;  // uniform for the block
+    const int lane = threadIdx.x;
+    const int r = r0 + lane;
+    const bool valid = r < total;
+    uint32_t sid = 0xFFFFFFFFu, cnt = 0u;
+    if (valid) {
+        const int old = w.sorted[r];
+        const uint32_t s = meta_scene(w.meta[old]);
+        const ScenePar &P = w.par[s];
+        const bool search = r < w.cell_start[P.big_cell];
+        sid = (s << 1) | (search ? 0u : 1u);
+        cnt = search ? (uint32_t)__popc(w.smask[old] & ((1u << K) - 1u)) : 0u;
+    }
+    seg_id[lane] = sid;
+    __syncthreads();
+    // segment number within the window: segments start where the scene or
+    // the region (search cells / large and dead cells) changes
+    const bool start = lane == 0 || seg_id[lane] != seg_id[lane - 1];
+    const unsigned bal = __ballot_sync(0xffffffffu, start);
+    if ((lane & 31) == 0) wsum[lane >> 5] = __popc(bal);
+    __syncthreads();
+    uint32_t seg = (uint32_t)__popc(bal & ((2u << (lane & 31)) - 1u));
+    for (int q = 0; q < (lane >> 5); ++q) seg += (uint32_t)wsum[q];
+    // unique keys: segment, slot count (search cells only), position
+    key[lane] = valid ? (seg << 11) | (cnt << 7) | (uint32_t)lane : 0xFFFFFFFFu;
+    __syncthreads();
+    for (int size = 2; size <= WIN; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const int partner = lane ^ stride;
+            if (partner > lane) {
+                const uint32_t a = key[lane], b = key[partner];
+                if ((a > b) == ((lane & size) == 0)) {
+                    key[lane] = b;
+                    key[partner] = a;
+                }
+            }
+            __syncthreads();
+        }
+    const uint32_t ks = key[lane];
+    if (ks != 0xFFFFFFFFu) w.wperm[r0 + (int)(ks & (WIN - 1))] = r0 + lane;
+}
+
 void launch_exclusive_scan(const int32_t *in, int32_t *out, int n, int32_t *tmp, cudaStream_t st) {
     const int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (ntiles > 0) k_scan_tiles<<<ntiles, SCAN_THREADS, 0, st>>>(in, out, n, tmp, nullptr);
@@ -499,15 +558,17 @@ int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int3
     k_scan_add<<<ntiles, SCAN_THREADS, 0, st>>>(w.cell_start, w.C, w.scan_tmp, gate);
     k_scatter<<<(w.N + block - 1) / block, block, 0, st>>>(w, gate);
     k_cell_order<<<(w.C + 255) / 256, 256, 0, st>>>(w, gate);
+    k_window_order<<<(w.N + WIN - 1) / WIN, WIN, 0, st>>>(w, gate);
     return 0;
 }
 
 // --------------------------------------------------------------- reorder
-// Permute every per-particle array into cell order (new i <- old sorted[i])
-// and remap partner indices; the cell lists become the identity.
-// The particle at cell-order position k (sorted[k]) moves to its scene's
-// range at the same offset: new = particle_base + (k - first position of the
-// scene's cells).  Particles of frozen scenes stay where they are.
+// Permute every per-particle array into cell order, grouped by contact count
+// within windows (new i <- old src[i]), and remap partner indices; the cell
+// list then names the new indices.  The particle at cell-order position k
+// (sorted[k]) moves to its scene's range at the offset of its grouped
+// position: new = particle_base + (wperm[k] - first position of the scene's
+// cells).  Particles of frozen scenes stay where they are.
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_inverse(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -515,9 +576,10 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_inverse(DevWorld w, const in
     if (t < w.cell_start[w.C]) {
         const int old = w.sorted[t];
         const ScenePar &P = w.par[meta_scene(w.meta[old])];
-        const int nw = P.particle_base + (t - w.cell_start[P.cell_base]);
+        const int nw = P.particle_base + (w.wperm[t] - w.cell_start[P.cell_base]);
         w.inv[old] = nw;
         w.src[nw] = old;
+        w.sorted[t] = nw;  // the cell list names the new indices
     }
     if (!w.act[meta_scene(w.meta[t])]) {
         w.inv[t] = t;
@@ -551,11 +613,9 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_gather(DevWorld w, DevWorld 
         o.s_btf[j * N + i] = w.s_btf[j * N + src];
         o.s_thb[j * N + i] = w.s_thb[j * N + src];
     }
-    // the cell-order list now names the new indices
     const int ss = (int)meta_scene(w.meta[src]);
     if (w.act[ss]) {
         const ScenePar &P = w.par[ss];
-        w.sorted[i - P.particle_base + w.cell_start[P.cell_base]] = i;
         w.o2i[P.particle_base + w.orig[src]] = i;
     }
 }
@@ -1302,7 +1362,6 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
     if (threadIdx.x == 0) scount = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int c0 = w.cell_start[P.cell_base];
     auto consider = [&](int b) {
         if (b == i) return;
         if (!touching(pa, __ldg(&w.pr[b]))) return;
@@ -1325,7 +1384,7 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
     for (int cy = cy0 + warp; cy <= cy1; cy += BIG_THREADS / 32) {
         const int row = P.cell_base + cy * P.g_w;
         const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
-        for (int q = beg + lane; q < end; q += 32) consider(P.particle_base + (q - c0));
+        for (int q = beg + lane; q < end; q += 32) consider(w.sorted[q]);
     }
     for (int b = bb + threadIdx.x; b < bb + bn; b += BIG_THREADS) consider(b);
     __syncthreads();

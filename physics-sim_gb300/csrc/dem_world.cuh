@@ -138,6 +138,7 @@ struct DevWorld {
     // broad phase
     uint32_t *keys;
     int32_t *cell_count, *cell_start, *sorted, *inv, *src, *scan_tmp;
+    int32_t *wperm;             // rebuild: cell-order position -> position after grouping by contact count
     // bond breaks of the current step (applied after the Simulation pass)
     Pending *pend;
     uint32_t *pend_count;

@@ -494,6 +494,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
     w.sorted = dalloc<int32_t>(owned, N, ok);
     w.inv = dalloc<int32_t>(owned, N, ok);
     w.src = dalloc<int32_t>(owned, N, ok);
+    w.wperm = dalloc<int32_t>(owned, N, ok);
     w.scan_tmp = dalloc<int32_t>(owned, scan_tmp_size(C), ok);
     w.pend_cap = (uint32_t)std::max<long long>(2LL * B + 64, 64);
     w.pend = dalloc<Pending>(owned, w.pend_cap, ok);
@@ -1524,7 +1525,7 @@ void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate) {
     launch_broad_phase(d, block, st, gate);
     launch_reorder(d, spare, block, st, gate);
     launch_list_build(d, block, st, gate);
-    rebuild_kernels = 1 + 5 + 3 + 2;
+    rebuild_kernels = 1 + 6 + 3 + 2;
 }
 
 // One step with plain launches; the rebuild kernels run every step and
