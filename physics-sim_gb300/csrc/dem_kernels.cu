@@ -333,7 +333,7 @@ __device__ __forceinline__ bool gated_off(const int32_t *gate) {
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_keys(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.N) return;
+    if (i >= w.N || !chunk_live(w, i)) return;
     uint32_t m = w.meta[i];
     if (!w.act[meta_scene(m)]) return;  // frozen scenes keep their order and take no cells
     const ScenePar &P = w.par[meta_scene(m)];
@@ -455,7 +455,7 @@ int scan_tmp_size(int n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_scatter(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.N) return;
+    if (i >= w.N || !chunk_live(w, i)) return;
     if (!w.act[meta_scene(w.meta[i])]) return;
     uint32_t key = w.keys[i];
     int slot = w.cell_start[key] + atomicSub(&w.cell_count[key], 1) - 1;
@@ -581,7 +581,7 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_inverse(DevWorld w, const in
         w.src[nw] = old;
         w.sorted[t] = nw;  // the cell list names the new indices
     }
-    if (!w.act[meta_scene(w.meta[t])]) {
+    if (chunk_live(w, t) && !w.act[meta_scene(w.meta[t])]) {  // free chunks are not gathered
         w.inv[t] = t;
         w.src[t] = t;
     }
@@ -590,7 +590,7 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_inverse(DevWorld w, const in
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_gather(DevWorld w, DevWorld o, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.N) return;
+    if (i >= w.N || !chunk_live(w, i)) return;  // a free chunk stays as it is
     int src = w.src[i];
     o.pr[i] = w.pr[src];
     o.vw[i] = w.vw[src];
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_gather(DevWorld w, DevWorld 
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_copy_back(DevWorld w, DevWorld o, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.N) return;
+    if (i >= w.N || !chunk_live(w, i)) return;
     w.pr[i] = o.pr[i];
     w.vw[i] = o.vw[i];
     w.ac[i] = o.ac[i];
@@ -668,7 +668,7 @@ void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStr
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_list_build(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.N) return;
+    if (i >= w.N || !chunk_live(w, i)) return;
     const uint32_t m = w.meta[i];
     const ScenePar &P = w.par[meta_scene(m)];
     const float4 pa = w.pr[i];
