@@ -760,7 +760,8 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
     }
     double cap_cells = std::max(4.0 * n, 65536.0);
     double span_x = (ex1 - ex0) + 2.0 * reach, span_y = (ey1 - ey0) + 2.0 * reach;
-    if (!(span_x > 0) || !(span_y > 0) || !std::isfinite(span_x) || !std::isfinite(span_y)) {
+    // no particle with a nonzero radius (an empty scene): nothing to search
+    if (!any || !(span_x > 0) || !(span_y > 0) || !std::isfinite(span_x) || !std::isfinite(span_y)) {
         span_x = span_y = 2.0 * reach;
         ex0 = ey0 = -reach; ex1 = ey1 = reach;
     }

@@ -148,6 +148,38 @@ def test_transfer_routes_agree(host_copies):
             assert_same_state(b.download(k), a.download(k), "after upload, scene %d: " % k)
 
 
+def _empty_like(sc):
+    """A scene of the same settings and materials with no particles."""
+    e = {k: (v[:0].copy() if hasattr(v, "shape") and k not in ("materials", "bonds", "coll_cont") else v)
+         for k, v in sc.items()}
+    e["materials"] = sc["materials"].copy()
+    e["bonds"] = np.array([-1], dtype=np.int32)
+    e["coll_cont"] = sc["coll_cont"].copy()
+    return e
+
+
+def test_empty_scene_in_a_batch():
+    """A scene without particles sits in a batch without disturbing the
+    others, downloads as empty, and takes part in bulk transfers."""
+    a, p, ext = dem_scenes.dense_bed(700, seed=21)
+    b_sc, bp, bext = dem_scenes.c3_mix_scene(900, 0.3, 22)
+    items = [(a, p, ext), (_empty_like(a), p, ext), (b_sc, bp, bext)]
+    with dem.Batch(items) as bt:
+        bt.step(70)
+        got = [bt.download(k) for k in range(3)]
+        assert got[1]["radii"].size == 0
+        bt.upload_many(list(enumerate(got)))
+        bt.step(35)
+        again = [bt.download(k) for k in range(3)]
+    for k in (0, 2):
+        sc, pp, ee = items[k]
+        with dem.Context(sc, pp, **ee) as ctx:
+            ctx.step(70)
+            ctx.upload(ctx.download())
+            ctx.step(35)
+            assert_same_state(again[k], ctx.download(), "scene %d: " % k)
+
+
 def test_bulk_upload_rejects_a_bad_scene_and_writes_nothing():
     items = _items()[:3]
     with dem.Batch(items) as b:

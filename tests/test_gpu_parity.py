@@ -212,6 +212,19 @@ def test_large_scene_layout_on_host_threads_bit_exact():
     assert_same_state(g, o)
 
 
+@pytest.mark.parametrize("split", [0, 1])
+def test_list_overflow_cell_search_bit_exact(split):
+    """A skin of 2 r_max puts more than 15 candidates on most particles of a
+    packed bed: they search the rebuild's cell table every step instead of a
+    candidate list (both Simulation-kernel forms), with the oracle's results."""
+    sc, p, ext = dem_scenes.dense_bed(n=1500, seed=9)
+    g, o, _, _ = run_both(sc, p, 120, chunk=40, list_skin=2.0, split_narrow=split, reorder_interval=7)
+    with dem.Context(sc, p, list_skin=2.0, split_narrow=split) as ctx:
+        ctx.step(10)
+        assert ctx.stats()["list_overflows"] > 0
+    assert_same_state(g, o)
+
+
 def test_broad_phase_keys_and_order():
     sc, p, ext = dem_scenes.c0_settle(n=3000, seed=2, box=(80, 120), spacing=2.3)
     with dem.Context(sc, p) as ctx:
