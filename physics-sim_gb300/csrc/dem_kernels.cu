@@ -493,8 +493,11 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_cell_order(DevWorld w, const
 // large and zero-radius particles' cells, do not move.  No result depends on
 // the order: every order-dependent choice keys on original indices.
 // wperm[r] = the position the particle at cell-order position r takes.
-constexpr int WIN = 128;
+// Windows of 128 suit batches of many scenes, which rebuild more often;
+// a single large scene gains from windows of 1024.
+template <int WIN>
 __global__ void __launch_bounds__(WIN) k_window_order(DevWorld w, const int32_t *gate) {
+    constexpr int LB = WIN == 1024 ? 10 : 7;  // log2(WIN)
     if (gated_off(gate)) return;
     __shared__ uint32_t key[WIN];
     __shared__ uint32_t seg_id[WIN];
@@ -525,7 +528,7 @@ __global__ void __launch_bounds__(WIN) k_window_order(DevWorld w, const int32_t 
     uint32_t seg = (uint32_t)__popc(bal & ((2u << (lane & 31)) - 1u));
     for (int q = 0; q < (lane >> 5); ++q) seg += (uint32_t)wsum[q];
     // unique keys: segment, slot count (search cells only), position
-    key[lane] = valid ? (seg << 11) | (cnt << 7) | (uint32_t)lane : 0xFFFFFFFFu;
+    key[lane] = valid ? (seg << (LB + 4)) | (cnt << LB) | (uint32_t)lane : 0xFFFFFFFFu;
     __syncthreads();
     for (int size = 2; size <= WIN; size <<= 1)
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -558,7 +561,8 @@ int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int3
     k_scan_add<<<ntiles, SCAN_THREADS, 0, st>>>(w.cell_start, w.C, w.scan_tmp, gate);
     k_scatter<<<(w.N + block - 1) / block, block, 0, st>>>(w, gate);
     k_cell_order<<<(w.C + 255) / 256, 256, 0, st>>>(w, gate);
-    k_window_order<<<(w.N + WIN - 1) / WIN, WIN, 0, st>>>(w, gate);
+    if (w.S == 1) k_window_order<1024><<<(w.N + 1023) / 1024, 1024, 0, st>>>(w, gate);
+    else k_window_order<128><<<(w.N + 127) / 128, 128, 0, st>>>(w, gate);
     return 0;
 }
 
