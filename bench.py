@@ -228,8 +228,9 @@ def profiled_traffic(workload):
 
 
 def interact_bytes(s_u, s_b, n, fused):
-    """Algorithmic bytes of one Simulation-kernel launch (the survey's byte
-    model): 12 per unbonded and 36 per bonded directed slot, plus per
+    """Algorithmic bytes of one Simulation-kernel launch (the per-step byte
+    model of the workload definition): 12 per unbonded and 36 per bonded
+    directed slot, plus per
     particle the force pass's 56 (pos, r, del_pos, del_rot, material,
     external force read; acc, rot_acc, vel, rot_vel written) or, when the
     kernel also carries the next step's LOM pass, the whole 120-byte state
