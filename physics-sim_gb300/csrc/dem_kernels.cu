@@ -852,7 +852,10 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // them; a fused step whose scene steps on within the call therefore leaves
 // them to the scene's last step of the call (lom_final: the next step is the
 // call's last).  Results are unchanged; the intermediate writes are saved.
-template <int PART, bool FUSE>
+// BM: the bond model when every scene of the world uses the same one (0 or
+// 3), fixed at compile time so that the other models' code and registers
+// drop out; -1 reads each scene's setting.
+template <int PART, bool FUSE, int BM>
 __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr, bool lom_final) {
     // The particle's own records: the ones needed first are loaded now, the
     // rest (read only after the scene, detection and slot checks resolve)
@@ -890,7 +893,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         return;
     }
     const uint32_t before = mask;
-    const int bonds_model = P.p.bonds;
+    const int bonds_model = BM >= 0 ? BM : P.p.bonds;
 
     // Loads that only some particles need (the bucket range, the second half
     // of the candidate list, del_pos) wait until the particle needs them.
@@ -1293,33 +1296,34 @@ __device__ __forceinline__ void interact_tail(const DevWorld &w, bool fused, int
         cudaGraphSetConditional(cond, *(volatile int32_t *)w.rebuild != 0 ? 1u : 0u);
 }
 
-template <bool FUSE>
 // Minimum blocks per SM: measured on GB300 (c3 mix, c2 scene).  Occupancy
 // outweighs the few spilled words down to 40 registers for k_interact (12
 // blocks: 7 % faster than 8) and 56 for k_forces (9 blocks).
+template <bool FUSE, int BM>
 __global__ void __launch_bounds__(IB, 12) k_interact(DevWorld w, int in_graph, cudaGraphConditionalHandle cond,
                                                     int lom_final) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N && chunk_live(w, i)) interact_particle<0, FUSE>(w, i, nr, lom_final != 0);
+    if (i < w.N && chunk_live(w, i)) interact_particle<0, FUSE, BM>(w, i, nr, lom_final != 0);
     interact_tail(w, FUSE, in_graph, cond);
 }
 
+template <int BM>
 __global__ void __launch_bounds__(IB, 12) k_narrow(DevWorld w) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N && chunk_live(w, i)) interact_particle<1, false>(w, i, nr, false);
+    if (i < w.N && chunk_live(w, i)) interact_particle<1, false, BM>(w, i, nr, false);
 }
 
-template <bool FUSE>
+template <bool FUSE, int BM>
 __global__ void __launch_bounds__(IB, 9) k_forces(DevWorld w, int in_graph, cudaGraphConditionalHandle cond,
                                                   int lom_final) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N && chunk_live(w, i)) interact_particle<2, FUSE>(w, i, nr, lom_final != 0);
+    if (i < w.N && chunk_live(w, i)) interact_particle<2, FUSE, BM>(w, i, nr, lom_final != 0);
     interact_tail(w, FUSE, in_graph, cond);
 }
 
@@ -1442,8 +1446,22 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
     if (threadIdx.x == 0) out[15] = keep;
 }
 
+template <int BM>
+static int launch_sim(const DevWorld &w, int g, cudaStream_t st, bool fuse, int ig, int lf,
+                      cudaGraphConditionalHandle cond) {
+    if (w.split) {
+        k_narrow<BM><<<g, IB, 0, st>>>(w);
+        if (fuse) k_forces<true, BM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+        else k_forces<false, BM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+        return 2;
+    }
+    if (fuse) k_interact<true, BM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+    else k_interact<false, BM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+    return 1;
+}
+
 int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool lom_final,
-                    bool in_graph, cudaGraphConditionalHandle cond) {
+                    bool in_graph, cudaGraphConditionalHandle cond, int bond_model) {
     (void)block;
     int k = 0;
     if (bigs && w.n_big_slots > 0) {
@@ -1452,16 +1470,9 @@ int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bo
     }
     const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
     const int ig = in_graph ? 1 : 0, lf = lom_final ? 1 : 0;
-    if (w.split) {
-        k_narrow<<<g, IB, 0, st>>>(w);
-        if (fuse) k_forces<true><<<g, IB, 0, st>>>(w, ig, cond, lf);
-        else k_forces<false><<<g, IB, 0, st>>>(w, ig, cond, lf);
-        k += 2;
-    } else {
-        if (fuse) k_interact<true><<<g, IB, 0, st>>>(w, ig, cond, lf);
-        else k_interact<false><<<g, IB, 0, st>>>(w, ig, cond, lf);
-        k++;
-    }
+    if (bond_model == 3) k += launch_sim<3>(w, g, st, fuse, ig, lf, cond);
+    else if (bond_model == 0) k += launch_sim<0>(w, g, st, fuse, ig, lf, cond);
+    else k += launch_sim<-1>(w, g, st, fuse, ig, lf, cond);
     if (!w.ticket) {
         k_end_step<<<1, END_THREADS, 0, st>>>(w);
         k++;

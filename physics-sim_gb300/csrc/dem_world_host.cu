@@ -1162,7 +1162,22 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     CK(cudaStreamSynchronize(stream));
     rc = push_det();
     if (rc) return rc;
+    update_bond_model();
     return force_rebuild();
+}
+
+// the Simulation kernels specialised for a bond model when every scene uses
+// it (0: none, 3: parallel bonds); a change recaptures the graphs
+void World::update_bond_model() {
+    int m = sh.empty() ? -1 : sh[0].params.bonds;
+    for (const auto &h : sh)
+        if (h.params.bonds != m) m = -1;
+    if (m != 0 && m != 3) m = -1;
+    if (served) m = -1;
+    if (m != kernel_bm) {
+        kernel_bm = m;
+        drop_graph();
+    }
 }
 
 long long World::bytes_per_particle() const {
@@ -1193,6 +1208,7 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     diagnostics = ext.diagnostics != 0;
     const int S = scenes + 1;  // the last slot owns the unused particles
     free_slot = scenes;
+    served = true;
     sh.assign(S, SceneHost{});
     for (auto &h : sh) {
         h.active = false;
@@ -1442,6 +1458,7 @@ int World::set_params(int s, const dem_params &p) {
     if (rc) return rc;
     rc = push_det();
     if (rc) return rc;
+    update_bond_model();
     return geometry ? force_rebuild() : DEM_OK;
 }
 
@@ -1555,7 +1572,7 @@ void World::enqueue_plain_step(bool first, bool last, bool next_last) {
     rec(T_BROAD, false);
     rec(T_INTERACT, true);
     const bool fuse = fuse_lom && !last;
-    k += launch_interact(d, block, stream, has_bigs, fuse, next_last, false, cudaGraphConditionalHandle{});
+    k += launch_interact(d, block, stream, has_bigs, fuse, next_last, false, cudaGraphConditionalHandle{}, kernel_bm);
     rec(T_INTERACT, false);
     if (fuse) flip();
     launches += k + rebuild_kernels;
@@ -1658,12 +1675,13 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
         if (fuse_lom && k + 1 < R) {
             cudaGraphConditionalHandle hn{};
             CKR(cudaGraphConditionalHandleCreate(&hn, g, 0, cudaGraphCondAssignDefault));
-            kernels += launch_interact(d, block, stream, has_bigs, true, k + 2 == R, true, hn);
+            kernels += launch_interact(d, block, stream, has_bigs, true, k + 2 == R, true, hn, kernel_bm);
             CKR(cudaGetLastError());
             flip();
             h = hn;
         } else {
-            kernels += launch_interact(d, block, stream, has_bigs, false, false, true, cudaGraphConditionalHandle{});
+            kernels += launch_interact(d, block, stream, has_bigs, false, false, true, cudaGraphConditionalHandle{},
+                                       kernel_bm);
             CKR(cudaGetLastError());
         }
     }
