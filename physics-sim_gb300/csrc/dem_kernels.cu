@@ -106,11 +106,14 @@ struct Acc3 {
 // with the same float operations
 // L = len2f(pa - pb), which the caller computes once per slot (every float
 // distance of the slot is this same value)
+// F64: the scene may use the F64 distance (read from its settings); false
+// compiles the FP32 form only
+template <bool F64>
 __device__ __forceinline__ F3 linear_model(const ScenePar &P, float2 kns, float4 pa,
                                            float4 da, float4 pb, float4 db, float length, float L, float &tf,
                                            Acc3 &acc) {
     F3 out = {0.0f, 0.0f, 0.0f};
-    float d2 = P.use_f64 ? distance2(1, pa, pb, length) : L - length;
+    float d2 = (F64 && P.use_f64) ? distance2(1, pa, pb, length) : L - length;
     float nd = d2 < 0.0f ? d2 : 0.0f;
     if (nd == 0.0f) return out;
     float kn = kns.x;
@@ -852,10 +855,11 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // them; a fused step whose scene steps on within the call therefore leaves
 // them to the scene's last step of the call (lom_final: the next step is the
 // call's last).  Results are unchanged; the intermediate writes are saved.
-// BM: the bond model when every scene of the world uses the same one (0 or
-// 3), fixed at compile time so that the other models' code and registers
-// drop out; -1 reads each scene's setting.
-template <int PART, bool FUSE, int BM>
+// FORM: what the world's scenes need, fixed at compile time so that the
+// rest (and the registers it holds) drops out: 0 or 3, every scene uses that
+// bond model and none the F64 distances; -2, any bond model, no F64
+// distances; -1, anything.  Only -1 carries the double-precision paths.
+template <int PART, bool FUSE, int FORM>
 __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr, bool lom_final) {
     // The particle's own records: the ones needed first are loaded now, the
     // rest (read only after the scene, detection and slot checks resolve)
@@ -893,7 +897,8 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         return;
     }
     const uint32_t before = mask;
-    const int bonds_model = BM >= 0 ? BM : P.p.bonds;
+    const int bonds_model = FORM == 0 ? 0 : FORM == 3 ? 3 : P.p.bonds;
+    constexpr bool MAY_F64 = FORM == -1;
 
     // Loads that only some particles need (the bucket range, the second half
     // of the candidate list, del_pos) wait until the particle needs them.
@@ -1074,7 +1079,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         // from a - b only in sign, so the squares agree)
         if (bonded < 0 || bonds_model == 0) {
             float tf = tf0;
-            f = linear_model(P, kns, pa, da, pb, db, pa.z + pb.z, len2f(pa.x - pb.x, pa.y - pb.y), tf, acc);
+            f = linear_model<MAY_F64>(P, kns, pa, da, pb, db, pa.z + pb.z, len2f(pa.x - pb.x, pa.y - pb.y), tf, acc);
             w.s_tf[j * N + i] = tf;
         } else {
             const int bg = P.bond_base + bonded;
@@ -1085,7 +1090,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 const float A = (2.0f * Rr) * 1.0f;
                 const float I = ((2.0f / 3.0f * Rr) * Rr) * Rr;
                 const float L = len2f(pa.x - pb.x, pa.y - pb.y);
-                const float nd = P.use_f64 ? distance2(1, pa, pb, blen) : L - blen;
+                const float nd = (MAY_F64 && P.use_f64) ? distance2(1, pa, pb, blen) : L - blen;
                 float Fn = ((-kn) * nd) * A;
                 const float vx = pa.x - pb.x, vy = pa.y - pb.y;
                 const float nx = vx / L, ny = vy / L;
@@ -1124,14 +1129,14 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 acc.d1 = acc.d1 + btf;
                 acc.d2 = acc.d2 + M;
                 float tf = tf0;
-                const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, L, tf, acc);
+                const F3 lm = linear_model<MAY_F64>(P, kns, pa, da, pb, db, blen, L, tf, acc);
                 w.s_tf[j * N + i] = tf;
                 f.x = Fx + lm.x;
                 f.y = Fy + lm.y;
                 f.z = M + lm.z;
             } else if (bonds_model == 1) {                         // :419-432
                 const float L = len2f(pa.x - pb.x, pa.y - pb.y);
-                const float disp = P.use_f64 ? distance1(1, pa, pb) : L - (pa.z + pb.z);
+                const float disp = (MAY_F64 && P.use_f64) ? distance1(1, pa, pb) : L - (pa.z + pb.z);
                 float fx = 0.0f, fy = 0.0f;
                 const float sf = P.p.bond_normal_stiffness * disp;
                 const float vx = pb.x - pa.x, vy = pb.y - pa.y;
@@ -1146,14 +1151,14 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     fy = 0.0f;
                 }
                 float tf = tf0;
-                const F3 lm = linear_model(P, kns, pa, da, pb, db, blen, L, tf, acc);
+                const F3 lm = linear_model<MAY_F64>(P, kns, pa, da, pb, db, blen, L, tf, acc);
                 w.s_tf[j * N + i] = tf;
                 f.x = lm.x + fx;
                 f.y = lm.y + fy;
                 f.z = lm.z + 0.0f;
             } else if (bonds_model == 2) {                         // :375-417
                 const float L = len2f(pa.x - pb.x, pa.y - pb.y);
-                const float nd = P.use_f64 ? distance1(1, pa, pb) : L - (pa.z + pb.z);
+                const float nd = (MAY_F64 && P.use_f64) ? distance1(1, pa, pb) : L - (pa.z + pb.z);
                 const float kn = P.kb2;
                 const float ks = P.ksb2;
                 float Fn = (-nd) * kn;
@@ -1299,31 +1304,31 @@ __device__ __forceinline__ void interact_tail(const DevWorld &w, bool fused, int
 // Minimum blocks per SM: measured on GB300 (c3 mix, c2 scene).  Occupancy
 // outweighs the few spilled words down to 40 registers for k_interact (12
 // blocks: 7 % faster than 8) and 56 for k_forces (9 blocks).
-template <bool FUSE, int BM>
+template <bool FUSE, int FORM>
 __global__ void __launch_bounds__(IB, 12) k_interact(DevWorld w, int in_graph, cudaGraphConditionalHandle cond,
                                                     int lom_final) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N && chunk_live(w, i)) interact_particle<0, FUSE, BM>(w, i, nr, lom_final != 0);
+    if (i < w.N && chunk_live(w, i)) interact_particle<0, FUSE, FORM>(w, i, nr, lom_final != 0);
     interact_tail(w, FUSE, in_graph, cond);
 }
 
-template <int BM>
+template <int FORM>
 __global__ void __launch_bounds__(IB, 12) k_narrow(DevWorld w) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N && chunk_live(w, i)) interact_particle<1, false, BM>(w, i, nr, false);
+    if (i < w.N && chunk_live(w, i)) interact_particle<1, false, FORM>(w, i, nr, false);
 }
 
-template <bool FUSE, int BM>
+template <bool FUSE, int FORM>
 __global__ void __launch_bounds__(IB, 9) k_forces(DevWorld w, int in_graph, cudaGraphConditionalHandle cond,
                                                   int lom_final) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N && chunk_live(w, i)) interact_particle<2, FUSE, BM>(w, i, nr, lom_final != 0);
+    if (i < w.N && chunk_live(w, i)) interact_particle<2, FUSE, FORM>(w, i, nr, lom_final != 0);
     interact_tail(w, FUSE, in_graph, cond);
 }
 
@@ -1446,22 +1451,22 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
     if (threadIdx.x == 0) out[15] = keep;
 }
 
-template <int BM>
+template <int FORM>
 static int launch_sim(const DevWorld &w, int g, cudaStream_t st, bool fuse, int ig, int lf,
                       cudaGraphConditionalHandle cond) {
     if (w.split) {
-        k_narrow<BM><<<g, IB, 0, st>>>(w);
-        if (fuse) k_forces<true, BM><<<g, IB, 0, st>>>(w, ig, cond, lf);
-        else k_forces<false, BM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+        k_narrow<FORM><<<g, IB, 0, st>>>(w);
+        if (fuse) k_forces<true, FORM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+        else k_forces<false, FORM><<<g, IB, 0, st>>>(w, ig, cond, lf);
         return 2;
     }
-    if (fuse) k_interact<true, BM><<<g, IB, 0, st>>>(w, ig, cond, lf);
-    else k_interact<false, BM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+    if (fuse) k_interact<true, FORM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+    else k_interact<false, FORM><<<g, IB, 0, st>>>(w, ig, cond, lf);
     return 1;
 }
 
 int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool lom_final,
-                    bool in_graph, cudaGraphConditionalHandle cond, int bond_model) {
+                    bool in_graph, cudaGraphConditionalHandle cond, int form) {
     (void)block;
     int k = 0;
     if (bigs && w.n_big_slots > 0) {
@@ -1470,9 +1475,12 @@ int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bo
     }
     const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
     const int ig = in_graph ? 1 : 0, lf = lom_final ? 1 : 0;
-    if (bond_model == 3) k += launch_sim<3>(w, g, st, fuse, ig, lf, cond);
-    else if (bond_model == 0) k += launch_sim<0>(w, g, st, fuse, ig, lf, cond);
-    else k += launch_sim<-1>(w, g, st, fuse, ig, lf, cond);
+    switch (form) {
+        case 3: k += launch_sim<3>(w, g, st, fuse, ig, lf, cond); break;
+        case 0: k += launch_sim<0>(w, g, st, fuse, ig, lf, cond); break;
+        case -2: k += launch_sim<-2>(w, g, st, fuse, ig, lf, cond); break;
+        default: k += launch_sim<-1>(w, g, st, fuse, ig, lf, cond); break;
+    }
     if (!w.ticket) {
         k_end_step<<<1, END_THREADS, 0, st>>>(w);
         k++;

@@ -208,10 +208,11 @@ void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int3
 // (into the other pr/dp/rr buffers), whose rebuild condition is set on `cond`
 // when in a graph.  A fused step is never a call's last step; lom_final: the
 // next one is (its LOM pass keeps data[4..6]).
-// bond_model: 0 or 3 when every scene uses that model (kernels specialised
-// for it), else -1 (each scene's setting read at run time)
+// form selects the Simulation kernels compiled for what the scenes need:
+// 0 or 3 (every scene uses that bond model, none the F64 distances), -2 (any
+// bond model, no F64 distances), -1 (anything)
 int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool lom_final,
-                    bool in_graph, cudaGraphConditionalHandle cond, int bond_model);
+                    bool in_graph, cudaGraphConditionalHandle cond, int form);
 void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
                            const int32_t *d_props, int block, cudaStream_t st);
 int scan_tmp_size(int n);

@@ -1162,20 +1162,28 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     CK(cudaStreamSynchronize(stream));
     rc = push_det();
     if (rc) return rc;
-    update_bond_model();
+    update_kernel_form();
     return force_rebuild();
 }
 
-// the Simulation kernels specialised for a bond model when every scene uses
-// it (0: none, 3: parallel bonds); a change recaptures the graphs
-void World::update_bond_model() {
-    int m = sh.empty() ? -1 : sh[0].params.bonds;
-    for (const auto &h : sh)
-        if (h.params.bonds != m) m = -1;
-    if (m != 0 && m != 3) m = -1;
-    if (served) m = -1;
-    if (m != kernel_bm) {
-        kernel_bm = m;
+// the Simulation kernels compiled for what the scenes need (launch_interact):
+// the double-precision paths only while some scene uses the F64 distances
+// (they cost the FP32 scenes registers), and one bond model built in when
+// every scene uses it (served worlds, whose scenes come and go, do not
+// specialise on the model); a change recaptures the graphs
+void World::update_kernel_form() {
+    unsigned models = 0u;
+    bool f64 = false;
+    for (size_t s = 0; s < sh.size(); ++s) {
+        if ((int)s == free_slot) continue;
+        const SceneHost &h = sh[s];
+        models |= (h.params.bonds >= 0 && h.params.bonds <= 3) ? 1u << h.params.bonds : 0xFu;
+        f64 |= h.use_f64 != 0;
+    }
+    int form = f64 ? -1 : -2;
+    if (!f64 && free_slot < 0) form = models == 1u ? 0 : models == 8u ? 3 : -2;
+    if (form != kernel_form) {
+        kernel_form = form;
         drop_graph();
     }
 }
@@ -1208,7 +1216,6 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     diagnostics = ext.diagnostics != 0;
     const int S = scenes + 1;  // the last slot owns the unused particles
     free_slot = scenes;
-    served = true;
     sh.assign(S, SceneHost{});
     for (auto &h : sh) {
         h.active = false;
@@ -1320,6 +1327,7 @@ int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e
     if (rc == DEM_OK) rc = push_active(s, true, horizon);
     if (rc == DEM_OK) rc = push_det();
     if (rc == DEM_OK) rc = update_live();
+    if (rc == DEM_OK) update_kernel_form();
     if (rc == DEM_OK) rc = force_rebuild();
     if (rc != DEM_OK) {
         retire(s);
@@ -1351,6 +1359,7 @@ int World::retire(int s) {
     free_slots.push_back(s);
     rc = update_live();
     if (rc) return rc;
+    update_kernel_form();
     return force_rebuild();
 }
 
@@ -1458,7 +1467,7 @@ int World::set_params(int s, const dem_params &p) {
     if (rc) return rc;
     rc = push_det();
     if (rc) return rc;
-    update_bond_model();
+    update_kernel_form();
     return geometry ? force_rebuild() : DEM_OK;
 }
 
@@ -1572,7 +1581,7 @@ void World::enqueue_plain_step(bool first, bool last, bool next_last) {
     rec(T_BROAD, false);
     rec(T_INTERACT, true);
     const bool fuse = fuse_lom && !last;
-    k += launch_interact(d, block, stream, has_bigs, fuse, next_last, false, cudaGraphConditionalHandle{}, kernel_bm);
+    k += launch_interact(d, block, stream, has_bigs, fuse, next_last, false, cudaGraphConditionalHandle{}, kernel_form);
     rec(T_INTERACT, false);
     if (fuse) flip();
     launches += k + rebuild_kernels;
@@ -1675,13 +1684,13 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
         if (fuse_lom && k + 1 < R) {
             cudaGraphConditionalHandle hn{};
             CKR(cudaGraphConditionalHandleCreate(&hn, g, 0, cudaGraphCondAssignDefault));
-            kernels += launch_interact(d, block, stream, has_bigs, true, k + 2 == R, true, hn, kernel_bm);
+            kernels += launch_interact(d, block, stream, has_bigs, true, k + 2 == R, true, hn, kernel_form);
             CKR(cudaGetLastError());
             flip();
             h = hn;
         } else {
             kernels += launch_interact(d, block, stream, has_bigs, false, false, true, cudaGraphConditionalHandle{},
-                                       kernel_bm);
+                                       kernel_form);
             CKR(cudaGetLastError());
         }
     }

@@ -134,9 +134,8 @@ class World {
     int push_par(int s);
     int push_det();
     int layout_threads = 1;  // host threads compute_layout may use on a large scene
-    int kernel_bm = -1;      // bond model the Simulation kernels are specialised for (-1: any)
-    bool served = false;     // a served world (arenas, scenes come and go)
-    void update_bond_model();
+    int kernel_form = -1;     // Simulation kernels' form (launch_interact): -1 carries everything
+    void update_kernel_form();
     uint8_t *live_d = nullptr;  // served worlds: the live map of 128-particle chunks (DevWorld::live)
     int update_live();
     int stage_many(const int32_t *idx, const dem_scene *const *scs, int count, const SceneHost *probes,
