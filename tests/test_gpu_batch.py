@@ -53,6 +53,28 @@ def test_batch_scene_equals_scene_alone():
         assert _ev_tuples(bev, k) == _ev_tuples(aev)
 
 
+def test_batch_with_an_f64_scene_equals_scenes_alone():
+    """One scene with F64 distances puts the whole batch on the Simulation
+    kernels that carry them (the others alone run kernels compiled without
+    them, for their one bond model); every result is still the scene's
+    result alone, bit for bit."""
+    items = _items()[:4]
+    sc, p, ext = dem_scenes.c1_chains(chains=3, length=20, seed=31, pull_velocity=20.0)
+    items.insert(2, (sc, p, dict(ext, use_f64=True)))
+    steps = 105
+    with dem.Batch(items, reorder_interval=35) as b:
+        b.step(steps)
+        got = [b.download(k) for k in range(len(items))]
+        bev = b.break_events()
+    for k, (sc, p, ext) in enumerate(items):
+        with dem.Context(sc, p, reorder_interval=35, **ext) as ctx:
+            ctx.step(steps)
+            alone = ctx.download()
+            aev = ctx.break_events()
+        assert_same_state(got[k], alone, "scene %d: " % k)
+        assert _ev_tuples(bev, k) == _ev_tuples(aev)
+
+
 def test_batch_matches_oracle():
     items = _items()[:3]
     steps = 90

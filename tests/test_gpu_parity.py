@@ -125,6 +125,31 @@ def test_bond_models_bit_exact(model):
     assert len(gev) == len(oev)
 
 
+def test_bond_model_changes_between_calls_bit_exact():
+    """The Simulation kernels are compiled per bond model; a context whose
+    model changes between calls (parallel -> none -> linear -> parallel)
+    changes kernels and recaptures its graphs, and still gives the oracle's
+    results under the same parameter sequence."""
+    sc, p, _ = dem_scenes.c1_chains(chains=3, length=24, seed=5, pull_velocity=8.0)
+    p = dict(p)
+    p["bond_normal_strength"] = 2e3
+    o = copy_scene(sc)
+    done = 0
+    oev = []
+    with dem.Context(sc, dict(p, bonds=3), bond_lambda=0.8, reorder_interval=35) as ctx:
+        for model, k in ((3, 70), (0, 70), (1, 105), (3, 70)):
+            q = dict(p, bonds=model)
+            ctx.set_params(q)
+            ctx.step(k)
+            ev, _ = oracle.step(o, q, k, step_base=done, bond_lambda=0.8)
+            oev.append(ev)
+            done += k
+        g = ctx.download()
+        gev = ctx.break_events()
+    assert_same_state(g, o)
+    assert len(gev) == len(np.concatenate(oev))
+
+
 @pytest.mark.parametrize("variant", ["planet", "round_walls", "interval3", "f64", "fixity_mix"])
 def test_setting_variants_bit_exact(variant):
     sc, p, ext = dem_scenes.c0_settle(n=500, seed=7, box=(50, 60), spacing=2.3)

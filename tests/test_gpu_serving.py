@@ -70,6 +70,42 @@ def test_each_result_equals_the_scene_alone():
     assert admits[3] >= admits[2]
 
 
+def test_f64_request_joins_and_leaves_a_running_world():
+    """An F64 request admitted among FP32 scenes moves the world onto the
+    Simulation kernels that carry the F64 paths, and its retirement moves it
+    back, while the others run on; every result equals the scene alone."""
+    chains = dem_scenes.c1_chains(chains=3, length=20, seed=22, pull_velocity=20.0)
+    reqs = [
+        (dem_scenes.c3_mix_scene(1200, 0.3, 21), 175),
+        ((chains[0], chains[1], dict(chains[2], use_f64=True)), 70),
+        (dem_scenes.dense_bed(700, seed=23), 105),
+    ]
+    with dem.Server(memory_budget_bytes=1 << 30, max_scenes=4, reorder_interval=35) as sv:
+        ids = {}
+        (sc, p, ext), h = reqs[0]
+        ids[sv.submit(sc, p, h, **ext)] = 0
+        sv.advance(35)
+        (sc, p, ext), h = reqs[1]
+        ids[sv.submit(sc, p, h, **ext)] = 1
+        sv.advance(35)
+        (sc, p, ext), h = reqs[2]
+        ids[sv.submit(sc, p, h, **ext)] = 2
+        done = {}
+        for _ in range(20):
+            sv.advance(35)
+            for rid in sv.poll():
+                done[rid] = sv.fetch(rid)
+            if len(done) == len(reqs):
+                break
+    assert len(done) == len(reqs)
+    for rid, (got, times, ev) in done.items():
+        k = ids[rid]
+        (sc, p, ext), h = reqs[k]
+        ref, rev = _alone(sc, p, ext, h)
+        assert_same_state(got, ref, "request %d: " % k)
+        assert _ev(ev) == _ev(rev)
+
+
 def test_capacity_refuses_nothing_and_queues():
     sc, p, ext = dem_scenes.dense_bed(3000, seed=21)
     with dem.Server(memory_budget_bytes=1 << 30, max_active_particles=3000, max_scenes=4) as sv:
