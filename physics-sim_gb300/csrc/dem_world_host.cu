@@ -1547,16 +1547,16 @@ int World::kernel_time(int kind, double *ms, long long *n) {
 // of the particle arrays into cell order, candidate lists.  `gate` is the
 // device word that says whether a rebuild is due (kernels return at once when
 // it is 0); inside a conditional graph node it is always 1.
-void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate) {
+// every_step: the kernels are launched at every step and do nothing unless a
+// rebuild is due (plain launches); otherwise they run only when it is due
+void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate, bool every_step) {
     launch_keys(d, block, st, gate);
     launch_broad_phase(d, block, st, gate);
     launch_reorder(d, spare, block, st, gate);
-    launch_list_build(d, block, st, gate);
+    launch_list_build(d, block, st, gate, every_step);
     rebuild_kernels = 1 + 6 + 3 + 2;
 }
 
-// One step with plain launches; the rebuild kernels run every step and
-// return at once unless a particle moved beyond its skin.
 // One step with plain launches; the rebuild kernels run every step and
 // return at once unless a particle moved beyond its skin.  Within a call the
 // first step runs its own LOM pass; every step but the last runs the next
@@ -1577,7 +1577,7 @@ void World::enqueue_plain_step(bool first, bool last, bool next_last) {
         rec(T_LOM, false);
     }
     rec(T_BROAD, true);
-    enqueue_rebuild(stream, d.rebuild);
+    enqueue_rebuild(stream, d.rebuild, true);
     rec(T_BROAD, false);
     rec(T_INTERACT, true);
     const bool fuse = fuse_lom && !last;
@@ -1674,7 +1674,7 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
         CKR(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np));
         cudaGraph_t body = np.conditional.phGraph_out[0];
         CKR(cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-        enqueue_rebuild(side, d.rebuild);
+        enqueue_rebuild(side, d.rebuild, false);
         const cudaError_t le = cudaGetLastError();
         cudaGraph_t body_out = nullptr;
         const cudaError_t ee = cudaStreamEndCapture(side, &body_out);

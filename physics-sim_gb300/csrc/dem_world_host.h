@@ -142,7 +142,7 @@ class World {
                    const std::function<int()> &layouts);
     int force_rebuild();
     void enqueue_plain_step(bool first, bool last, bool next_last);
-    void enqueue_rebuild(cudaStream_t st, const int32_t *gate);
+    void enqueue_rebuild(cudaStream_t st, const int32_t *gate, bool every_step);
     int capture_graph(int R, cudaGraphExec_t *out, int *kernels);
     void drop_graph();
     DevWorld spare{};

@@ -75,6 +75,26 @@ def test_batch_with_an_f64_scene_equals_scenes_alone():
         assert _ev_tuples(bev, k) == _ev_tuples(aev)
 
 
+@pytest.mark.parametrize("scenes", [1, 9])
+def test_plain_launches_equal_graphs(scenes):
+    """Plain launches (the rebuild kernels launched at every step on grids the
+    SMs hold at once, doing nothing unless a rebuild is due) give the graphs'
+    results bit for bit, rebuilds included; one scene groups by contact count
+    in windows of 1024, several in windows of 128."""
+    items = _items()[:scenes]
+    runs = []
+    for plain in (0, 1):
+        with dem.Batch(items, reorder_interval=35, plain_launches=plain) as b:
+            b.step(140)
+            runs.append(([b.download(k) for k in range(len(items))], b.stats()["reorders"],
+                         _ev_tuples(b.break_events())))
+    (g, g_re, g_ev), (p, p_re, p_ev) = runs
+    assert g_re == p_re and g_re > 0
+    for k in range(len(items)):
+        assert_same_state(p[k], g[k], "scene %d: " % k)
+    assert p_ev == g_ev
+
+
 def test_batch_matches_oracle():
     items = _items()[:3]
     steps = 90
