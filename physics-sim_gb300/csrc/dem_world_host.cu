@@ -1456,9 +1456,6 @@ int World::set_params(int s, const dem_params &p) {
     h.params = p;
     bool geometry = old.hor_bound != p.hor_bound || old.vert_bound != p.vert_bound ||
                     old.round_bounds != p.round_bounds || old.bound_radius != p.bound_radius;
-    if (geometry) {
-        // walls moved: the search grid keeps its allocation and clamps particles to it
-    }
     h.step0 = host_step;
     h.cc0_0 = cc[0];
     h.cc1_0 = cc[1];
@@ -1468,6 +1465,8 @@ int World::set_params(int s, const dem_params &p) {
     rc = push_det();
     if (rc) return rc;
     update_kernel_form();
+    // walls moved: the search grid keeps its allocation (it clamps particles
+    // to its extent) and the cell lists are rebuilt before the next step
     return geometry ? force_rebuild() : DEM_OK;
 }
 
