@@ -104,3 +104,43 @@ def test_invalid_scene_is_rejected_before_device_work(L):
     rc = L.dem_create(C.byref(st), C.byref(pp), C.byref(e), -1, C.byref(h))
     assert rc != 0 and not h.value
     assert L.dem_last_error(None)
+
+
+_C_STRUCTS = [("Params", "dem_params"), ("GridInfo", "dem_grid_info"), ("Ext", "dem_ext"),
+              ("Scene", "dem_scene"), ("BreakEvent", "dem_break_event"), ("Stats", "dem_stats"),
+              ("ServerConfig", "dem_server_config"), ("ServerStats", "dem_server_stats"),
+              ("TuneResult", "dem_tune_result")]
+
+
+def test_headers_compile_as_c_and_match_the_binding(tmp_path):
+    """dem.h and dem_debug.h compile as C11 with warnings as errors, and every
+    struct's size and field offsets, as a C compiler lays them out, equal the
+    binding's ctypes mirrors (the layouts a Rust or C host of the reference
+    binds against)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "dem.h"', '#include "dem_debug.h"',
+             "int main(void) {"]
+    for py, c in _C_STRUCTS:
+        lines.append('    printf("%s sizeof %%zu\\n", sizeof(%s));' % (py, c))
+        for f in getattr(dem, py)._fields_:
+            lines.append('    printf("%s %s %%zu\\n", offsetof(%s, %s));' % (py, f[0], c, f[0]))
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layouts.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layouts"
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-I", INCLUDE, str(src), "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            py, field, val = line.split()
+            got[(py, field)] = int(val)
+    for py, _ in _C_STRUCTS:
+        cls = getattr(dem, py)
+        assert got[(py, "sizeof")] == C.sizeof(cls), py
+        for f in cls._fields_:
+            assert got[(py, f[0])] == getattr(cls, f[0]).offset, (py, f[0])
