@@ -173,7 +173,8 @@ int dem_grid_capacity(const dem_params *p, const float *radii, int32_t n_radii, 
                       dem_grid_info *out);
 
 /* WGPUComputeProg::new + restore: copy a scene to the device.  device < 0
- * keeps the current CUDA device. */
+ * keeps the current CUDA device.  A context, batch or server holds at most
+ * 2^30 particles, 2^30 search cells and 2^30 bonds (DEM_E_INVALID beyond). */
 int dem_create(const dem_scene *scene, const dem_params *params, const dem_ext *ext, int device,
                dem_ctx **out);
 void dem_destroy(dem_ctx *ctx);
