@@ -174,7 +174,8 @@ int dem_grid_capacity(const dem_params *p, const float *radii, int32_t n_radii, 
 
 /* WGPUComputeProg::new + restore: copy a scene to the device.  device < 0
  * keeps the current CUDA device.  A context, batch or server holds at most
- * 2^30 particles, 2^30 search cells and 2^30 bonds (DEM_E_INVALID beyond). */
+ * 153,391,689 particles (14 slot rows of 32-bit indices), 2^30 search cells
+ * and 2^30 bonds (DEM_E_INVALID beyond; a server sizes its arenas within). */
 int dem_create(const dem_scene *scene, const dem_params *params, const dem_ext *ext, int device,
                dem_ctx **out);
 void dem_destroy(dem_ctx *ctx);

@@ -246,7 +246,7 @@ int dem_server_create(const dem_server_config *cfg, int device, dem_server **out
                        32.0 * c.bonds_per_particle;
     long long np = (long long)((double)c.memory_budget_bytes / per);
     if (c.max_active_particles > 0) np = std::min<long long>(np, (long long)(c.max_active_particles * 1.25) + 65536);
-    np = std::max<long long>(np, 1024);
+    np = std::max<long long>(std::min<long long>(np, demgb::MAX_WORLD_PARTICLES), 1024);
     long long nc = std::min<long long>((long long)(np * (double)c.cells_per_particle) + 4096, 1LL << 30);
     long long nb = std::min<long long>((long long)(np * (double)c.bonds_per_particle) + 1024, 1LL << 30);
     int rc = sv->world.build_capacity(np, nc, nb, c.max_scenes, 4 * c.max_scenes, c.ext);

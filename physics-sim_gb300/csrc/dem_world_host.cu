@@ -1137,11 +1137,8 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
         MP += (long long)h.n_mat * h.n_mat;
         TB += h.n_big;
     }
-    // at most 2^30 particles, cells and bonds: the kernels index them with
-    // 32-bit ints, and a grid-stride loop's index must not pass 2^31 on its
-    // last stride
-    if (N > (1LL << 30) || C > (1LL << 30) || B > (1LL << 30))
-        return fail(DEM_E_INVALID, "world too large (more than 2^30 particles, search cells or bonds)");
+    if (N > MAX_WORLD_PARTICLES || C > (1LL << 30) || B > (1LL << 30))
+        return fail(DEM_E_INVALID, "world too large (particles, search cells or bonds beyond the limits in dem.h)");
     uint32_t ev_cap = ext.event_capacity > 0 ? (uint32_t)ext.event_capacity : 1u << 16;
     int rc = alloc((int)N, (int)C, (int)B, S, (int)M, (int)MP, (int)TB, ev_cap);
     if (rc) return rc;
@@ -1202,8 +1199,8 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     if (particles <= 0 || cells <= 0 || scenes <= 0 || materials <= 0)
         return fail(DEM_E_INVALID, "capacities must be positive");
     if (scenes >= MAX_SCENES) return fail(DEM_E_INVALID, "too many scene slots");
-    if (particles > (1LL << 30) || cells > (1LL << 30) || bonds > (1LL << 30))
-        return fail(DEM_E_INVALID, "capacity too large (more than 2^30 particles, search cells or bonds)");
+    if (particles > MAX_WORLD_PARTICLES || cells > (1LL << 30) || bonds > (1LL << 30))
+        return fail(DEM_E_INVALID, "capacity too large (particles, search cells or bonds beyond the limits in dem.h)");
     if (ext.block_size) {
         if (ext.block_size < 32 || ext.block_size > 1024 || (ext.block_size & 31))
             return fail(DEM_E_INVALID, "block_size must be a multiple of 32 in [32, 1024]");

@@ -2,6 +2,7 @@
 // layout (grid geometry, offsets), conversion between the reference's host
 // layouts and the internal device layout, and step orchestration.
 #pragma once
+#include <climits>
 #include <cuda_runtime.h>
 
 #include <map>
@@ -13,6 +14,11 @@
 #include "dem_world.cuh"
 
 namespace demgb {
+
+// World limits: the kernels index particles, cells and bonds with 32-bit
+// ints, the slot rows as j * N + i (j < K), and a grid-stride loop's index
+// must not pass 2^31 on its last stride.
+constexpr long long MAX_WORLD_PARTICLES = (long long)INT_MAX / K;  // 153,391,689
 
 struct SceneHost {
     // reference-layout copies of what the step never writes (kept for download;
