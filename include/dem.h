@@ -99,7 +99,8 @@ typedef struct dem_ext {
                                          when a particle moves beyond half the skin; results do not
                                          depend on it */
     int32_t plain_launches;           /* 1: no CUDA graphs (for profilers that cannot see kernels inside
-                                         graphs with conditional nodes) */
+                                         graphs with conditional nodes, and for hosts that capture the
+                                         calls into graphs of their own); results do not depend on it */
     int32_t split_narrow;             /* 1: narrow phase and forces as two kernels (fewer registers
                                          each; faster in dense scenes); results do not depend on it */
     int32_t unfused_lom;              /* 1: every step runs its own LOM kernel instead of the next
