@@ -1,0 +1,38 @@
+"""The oracle is deterministic whatever the number of host threads: every
+array of the state and the break-event list are byte-identical between one
+thread and many (it is the checker of every parity test, so its own results
+must not depend on how it was run)."""
+import numpy as np
+import pytest
+
+import dem_scenes
+import oracle
+from gpu_backend import copy_scene
+
+
+def _run(sc, p, steps, threads, **kw):
+    o = copy_scene(sc)
+    ev, _ = oracle.step(o, p, steps, threads=threads, **kw)
+    return o, ev
+
+
+@pytest.mark.parametrize("workload", ["settle", "chains"])
+def test_thread_count_does_not_change_results(workload):
+    if workload == "settle":
+        sc, p, ext = dem_scenes.c0_settle(n=3000, seed=11, box=(60, 120), spacing=2.05)
+        kw = {}
+        steps = 120
+    else:
+        sc, p, ext = dem_scenes.c1_chains(chains=8, length=64, seed=12, pull_velocity=30.0)
+        kw = {"bond_lambda": ext["bond_lambda"], "bond_sn": ext["bond_sn"], "bond_ss": ext["bond_ss"]}
+        steps = 200
+    runs = [_run(sc, p, steps, t, **kw) for t in (1, 3, 0)]
+    (a, ea) = runs[0]
+    for b, eb in runs[1:]:
+        for k in a:
+            if k == "grid":
+                continue
+            assert np.asarray(a[k]).tobytes() == np.asarray(b[k]).tobytes(), k
+        assert np.asarray(ea).tobytes() == np.asarray(eb).tobytes()
+    if workload == "chains":
+        assert len(ea) > 0, "the pulled chains should break bonds"
