@@ -1,4 +1,5 @@
-"""The oracle is deterministic whatever the number of host threads: every
+"""The oracle is deterministic whatever the number of host threads and however
+the steps are split into calls: every
 array of the state and the break-event list are byte-identical between one
 thread and many (it is the checker of every parity test, so its own results
 must not depend on how it was run)."""
@@ -36,3 +37,28 @@ def test_thread_count_does_not_change_results(workload):
         assert np.asarray(ea).tobytes() == np.asarray(eb).tobytes()
     if workload == "chains":
         assert len(ea) > 0, "the pulled chains should break bonds"
+
+
+@pytest.mark.parametrize("interval", [1, 3])
+def test_chunked_calls_equal_one_call(interval):
+    """Stepping in chunks (as the parity tests do on both sides) equals one
+    call of all the steps: the control words carry the interval schedule
+    across calls, and the events keep their step numbers."""
+    sc, p, ext = dem_scenes.c1_chains(chains=6, length=48, seed=13, pull_velocity=30.0)
+    p = dict(p, collision_interval=interval)
+    kw = {"bond_lambda": ext["bond_lambda"], "bond_sn": ext["bond_sn"], "bond_ss": ext["bond_ss"]}
+    whole, ew = _run(sc, p, 210, 0, **kw)
+    part = copy_scene(sc)
+    evs = []
+    done = 0
+    for k in (1, 40, 69, 100):
+        ev, _ = oracle.step(part, p, k, step_base=done, **kw)
+        evs.append(ev)
+        done += k
+    for k in whole:
+        if k == "grid":
+            continue
+        assert np.asarray(whole[k]).tobytes() == np.asarray(part[k]).tobytes(), k
+    ep = np.concatenate(evs)
+    assert len(ew) > 0
+    assert np.asarray(ew).tobytes() == np.asarray(ep).tobytes()
