@@ -1,8 +1,6 @@
-"""The oracle is deterministic whatever the number of host threads and however
-the steps are split into calls: every
-array of the state and the break-event list are byte-identical between one
-thread and many (it is the checker of every parity test, so its own results
-must not depend on how it was run)."""
+"""The oracle's results do not depend on how it is run: one host thread or
+many, all steps in one call or split over several, give byte-identical
+states and break-event lists.  It is the checker of every parity test."""
 import numpy as np
 import pytest
 
