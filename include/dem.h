@@ -374,8 +374,15 @@ void *dem_server_stream(dem_server *sv);
  * (cell of a position = floor((x - x0) * inv_cell), floor((y - y0) * inv_cell)
  * clamped to gw x gh; key = cy * gw + cx; zero-radius particles get key
  * gw * gh).  Outputs (device): d_keys [n], d_order [n] (particle indices in
- * stable cell order), d_cell_start [gw * gh + 2].  Work is enqueued on
- * `stream` (a cudaStream_t, NULL = default stream) and not waited for.
+ * stable cell order: by key, then by index, built by a counting sort whose
+ * cost does not depend on how many particles share a cell), d_cell_start
+ * [gw * gh + 2].  d_keys also serves as the sort's second buffer and holds
+ * the keys only once the work has run.  Unlike the context's broad phase
+ * (dem_debug_broad_phase), which puts a scene's large particles in the last
+ * cell ahead of its zero-radius ones, every particle with a radius is keyed
+ * here by its position, and the last cell holds the zero-radius particles
+ * only.  Work is enqueued on `stream` (a cudaStream_t, NULL = default stream)
+ * and not waited for.  n is at most 2^30 (DEM_E_CAPACITY beyond).
  * Scratch is a fixed device array inside the library, held by every GPU that
  * loads it until exit: at most DEM_NOALLOC_MAX_CELLS cells (gw * gh + 1),
  * larger grids are rejected with DEM_E_CAPACITY.  All calls share that array

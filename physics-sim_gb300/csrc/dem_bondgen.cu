@@ -10,11 +10,14 @@
 // processed) all precede its own.  The same result is built here without the
 // sequential walk:
 //   1. a uniform grid of cells at least 2.1 r_max wide (every bonding pair
-//      lies in neighbouring cells), counting sort of the particles by cell;
+//      lies in neighbouring cells), the particles binned by cell;
 //   2. per i, the first max_bonds partners j > i in index order that pass
-//      the reference's test, from the 3x3 cells;
+//      the reference's test, from the 3x3 cells (the selection keeps the
+//      smallest qualifying indices whatever order a cell lists its members
+//      in, so the bins need no order);
 //   3. bond numbers = exclusive scan of the per-i counts (creation order);
-//   4. per particle, its bonds where it is the j side, sorted by number,
+//   4. per particle, its bonds where it is the j side in ascending number --
+//      a stable counting sort of the bond numbers by j (dem_sort.cuh) --
 //      then its own; the first 14 fill its contact slots.
 // The bond record's length and angle are evaluated on the host, one pass
 // over the bonds, with the host's powf and atan2f as the reference does
@@ -30,6 +33,7 @@
 #include <vector>
 
 #include "dem.h"
+#include "dem_sort.cuh"
 #include "dem_world.cuh"
 
 namespace {
@@ -71,22 +75,6 @@ __global__ void k_bg_scatter(const int32_t *__restrict__ keys, int n, const int3
     if (i >= n) return;
     const int c = keys[i];
     order[start[c] + atomicSub(&counts[c], 1) - 1] = i;
-}
-
-// members of every cell in ascending index (the scatter's order is arbitrary)
-__global__ void k_bg_cell_sort(const int32_t *__restrict__ start, int cells, int32_t *order) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cells) return;
-    const int beg = start[c], end = start[c + 1];
-    for (int a = beg + 1; a < end; ++a) {
-        const int v = order[a];
-        int b = a - 1;
-        while (b >= beg && order[b] > v) {
-            order[b + 1] = order[b];
-            --b;
-        }
-        order[b + 1] = v;
-    }
 }
 
 // the first max_bonds partners j > i (ascending j) that pass state.rs:301-304
@@ -145,31 +133,26 @@ __global__ void k_bg_write(int n, int max_bonds, const int32_t *__restrict__ sel
     }
 }
 
-__global__ void k_bg_incoming(const int32_t *__restrict__ bond_j, long long nbonds, const int32_t *__restrict__ in_start,
-                              int32_t *in_fill, int32_t *__restrict__ in_list) {
-    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbonds) return;
-    const int j = bond_j[b];
-    in_list[in_start[j] + atomicAdd(&in_fill[j], 1)] = (int32_t)b;
-}
+// the sort's input: bond numbers in order, keyed by their j side
+struct BgBonds {
+    const int32_t *bond_j;
+    int n;
+    __device__ __forceinline__ int length() const { return n; }
+    __device__ __forceinline__ bool get(int t, uint32_t &k, int32_t &v) const {
+        k = (uint32_t)bond_j[t];
+        v = t;
+        return true;
+    }
+};
 
 // contact slots: bonds where p is the j side (ascending number), then p's own
 __global__ void k_bg_slots(int n, int max_bonds, const int32_t *__restrict__ count, const int32_t *__restrict__ base,
                            const int32_t *__restrict__ sel, const int32_t *__restrict__ in_start,
-                           int32_t *__restrict__ in_list, const int32_t *__restrict__ bond_i,
+                           const int32_t *__restrict__ in_list, const int32_t *__restrict__ bond_i,
                            int32_t *__restrict__ contacts) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const int beg = in_start[p], end = in_start[p + 1];
-    for (int a = beg + 1; a < end; ++a) {
-        const int v = in_list[a];
-        int b = a - 1;
-        while (b >= beg && in_list[b] > v) {
-            in_list[b + 1] = in_list[b];
-            --b;
-        }
-        in_list[b + 1] = v;
-    }
     int32_t *c = contacts + (size_t)p * K * 6;
     int s = 0;
     for (int a = beg; a < end && s < K; ++a, ++s) {
@@ -271,7 +254,6 @@ int dem_generate_bonds(const float *pos, const float *radii, int32_t n, int32_t 
             k_bg_keys<<<G, T, 0, st>>>(d_pos, n, g, d_keys, d_cnt);
             demgb::launch_exclusive_scan(d_cnt, d_start, cells, d_tmp, st);
             k_bg_scatter<<<G, T, 0, st>>>(d_keys, n, d_start, d_cnt, d_order);
-            k_bg_cell_sort<<<(cells + T - 1) / T, T, 0, st>>>(d_start, cells, d_order);
             k_bg_select<<<G, T, 0, st>>>(d_pos, d_r, n, g, d_start, d_order, max_bonds, d_sel, d_count);
             demgb::launch_exclusive_scan(d_count, d_base, n, d_tmp, st);
         }
@@ -288,17 +270,38 @@ int dem_generate_bonds(const float *pos, const float *radii, int32_t n, int32_t 
         if (rc == DEM_OK) {
             int32_t *d_bonds = db.get<int32_t>(3 * (size_t)total), *d_bi = db.get<int32_t>(total);
             int32_t *d_bj = db.get<int32_t>(total), *d_in = db.get<int32_t>(n), *d_in_start = db.get<int32_t>(n + 1);
-            int32_t *d_fill = db.get<int32_t>(n), *d_list = db.get<int32_t>(total);
+            int32_t *d_list = db.get<int32_t>(total), *d_v2 = db.get<int32_t>(total);
+            uint32_t *d_k1 = db.get<uint32_t>(total), *d_k2 = db.get<uint32_t>(total);
+            int32_t *d_sc = db.get<int32_t>((size_t)demgb::SORT_GRID_MAX * demgb::SORT_BINS);
             int32_t *d_contacts = db.get<int32_t>((size_t)n * K * 6);
-            if (!d_bonds || !d_bi || !d_bj || !d_in || !d_in_start || !d_fill || !d_list || !d_contacts) {
+            if (!d_bonds || !d_bi || !d_bj || !d_in || !d_in_start || !d_list || !d_v2 || !d_k1 || !d_k2 ||
+                !d_sc || !d_contacts) {
                 rc = bfail(DEM_E_OOM, "device allocation failed");
             } else {
                 cudaMemsetAsync(d_in, 0, sizeof(int32_t) * n, st);
-                cudaMemsetAsync(d_fill, 0, sizeof(int32_t) * n, st);
                 k_bg_write<<<G, T, 0, st>>>(n, max_bonds, d_sel, d_count, d_base, d_bonds, d_bi, d_bj, d_in);
                 demgb::launch_exclusive_scan(d_in, d_in_start, n, d_tmp, st);
-                if (total > 0)
-                    k_bg_incoming<<<(total + T - 1) / T, T, 0, st>>>(d_bj, total, d_in_start, d_fill, d_list);
+                if (total > 0) {
+                    // incoming bonds of every particle in ascending bond number:
+                    // passes ping-pong (d_k1, d_v2) / (d_k2, d_list) and end in d_list
+                    int dev = 0, sms = 0;
+                    cudaGetDevice(&dev);
+                    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+                        sms = 1;
+                    const int grid = demgb::sort_grid(total, 2 * sms);
+                    const int passes = demgb::sort_passes(n);
+                    demgb::SortArrays prev{nullptr, nullptr, (int)total, nullptr};
+                    for (int p = 0; p < passes; ++p) {
+                        const bool last = p == passes - 1;
+                        const bool odd = ((passes - 1 - p) & 1) != 0;
+                        uint32_t *ok = last ? nullptr : (odd ? d_k1 : d_k2);
+                        int32_t *ov = odd ? d_v2 : d_list;
+                        if (p == 0) demgb::launch_sort_pass(BgBonds{d_bj, (int)total}, 0, grid, d_sc, ok, ov, st, nullptr);
+                        else demgb::launch_sort_pass(prev, 8 * p, grid, d_sc, ok, ov, st, nullptr);
+                        prev.key = ok;
+                        prev.val = ov;
+                    }
+                }
                 k_bg_slots<<<G, T, 0, st>>>(n, max_bonds, d_count, d_base, d_sel, d_in_start, d_list, d_bi,
                                             d_contacts);
                 std::vector<int32_t> bi(total), bj(total);

@@ -16,6 +16,7 @@
 #include <tuple>
 #include <vector>
 
+#include "dem_sort.cuh"
 #include "dem_world.cuh"
 
 namespace demgb {
@@ -363,6 +364,24 @@ static int resident_blocks(const void *fn, int block) {
     return sms * per;
 }
 
+// SMs of the current device (cached per device)
+static int device_sms() {
+    static std::mutex mu;
+    static std::vector<std::pair<int, int>> cache;  // device, SMs
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto &c : cache)
+        if (c.first == dev) return c.second;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    cache.emplace_back(dev, sms);
+    return sms;
+}
+
 template <typename Kernel>
 static int capped_grid(Kernel *kernel, long long items, int per_block, int block) {
     const long long need = (items + per_block - 1) / per_block;
@@ -441,10 +460,12 @@ __device__ __forceinline__ int block_excl_scan(int v, int *total) {
     return r;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(const int32_t *__restrict__ in,
+// clear: when set, every count read is set back to 0 (the world's cell
+// counts start the next rebuild's histogram from zero)
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(int32_t *__restrict__ in,
                                                              int32_t *__restrict__ out, int n,
                                                              int32_t *__restrict__ tile_sums,
-                                                             const int32_t *gate) {
+                                                             const int32_t *gate, int clear) {
     if (gated_off(gate)) return;
     __shared__ int total;
     const int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
@@ -457,6 +478,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(const int32_t *__re
             int idx = base + k;
             v[k] = idx < n ? in[idx] : 0;
             sum += v[k];
+        }
+        if (clear) {
+#pragma unroll
+            for (int k = 0; k < SCAN_PER_THREAD; ++k)
+                if (base + k < n) in[base + k] = 0;
         }
         int off = block_excl_scan(sum, &total);
 #pragma unroll
@@ -505,44 +531,30 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_add(int32_t *out, int n,
 
 int scan_tmp_size(int n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
 
-// scatter: slot = start + (count-1) taken by an atomic decrement, which also
-// returns every count to zero for the next histogram
-__device__ __forceinline__ void scatter_one(const DevWorld &w, int i) {
-    if (!chunk_live(w, i)) return;
-    if (!w.act[meta_scene(w.meta[i])]) return;
-    uint32_t key = w.keys[i];
-    int slot = w.cell_start[key] + atomicSub(&w.cell_count[key], 1) - 1;
-    w.sorted[slot] = i;
-}
-
-__global__ void __launch_bounds__(PK_MAX_THREADS) k_scatter(DevWorld w, const int32_t *gate) {
-    if (gated_off(gate)) return;
-    FOR_EACH_ITEM(i, w.N) scatter_one(w, i);
-}
-
-// in-cell ordering: each cell's members sorted by scene-local particle index,
-// so the cell lists equal a stable sort of the particles by cell key
-__device__ __forceinline__ void cell_order_one(const DevWorld &w, int c) {
-    int beg = w.cell_start[c], end = w.cell_start[c + 1];
-    if (end - beg < 2) return;
-    for (int a = beg + 1; a < end; ++a) {
-        int v = w.sorted[a];
-        int ov = w.orig[v];
-        int b = a - 1;
-        while (b >= beg) {
-            int u = w.sorted[b];
-            if (w.orig[u] <= ov) break;
-            w.sorted[b + 1] = u;
-            --b;
-        }
-        w.sorted[b + 1] = v;
+// Stable counting sort of the particles by search-cell key (dem_sort.cuh).
+// The sequence is the scenes' particles in scene-local index order -- position
+// t = particle_base + scene-local index, the particle being o2i[t] -- so the
+// members of every cell come out in scene-local index order, the order in
+// which the reference's insertion loop (2D_LOM.wgsl:165-200) would fill its
+// buckets if its threads ran in index order.  Positions of frozen scenes and
+// of free chunks take no part, as in the histogram (keys_one).
+struct SortWorldFirst {
+    const uint8_t *live;
+    const uint32_t *meta;
+    const int32_t *act;
+    const int32_t *o2i;
+    const uint32_t *keys;
+    int n;
+    __device__ __forceinline__ int length() const { return n; }
+    __device__ __forceinline__ bool get(int t, uint32_t &k, int32_t &v) const {
+        if (live != nullptr && __ldg(&live[t >> 7]) == 0) return false;
+        if (!act[meta_scene(meta[t])]) return false;  // the scene owning position t
+        const int i = o2i[t];
+        k = keys[i];
+        v = i;
+        return true;
     }
-}
-
-__global__ void __launch_bounds__(PK_MAX_THREADS) k_cell_order(DevWorld w, const int32_t *gate) {
-    if (gated_off(gate)) return;
-    FOR_EACH_ITEM(c, w.C) cell_order_one(w, c);
-}
+};
 
 // Grouping by contact count: within each window of WIN consecutive
 // cell-order positions, the particles of a scene's search cells are put in
@@ -617,27 +629,48 @@ __global__ void __launch_bounds__(WIN) k_window_order(DevWorld w, const int32_t 
 void launch_exclusive_scan(const int32_t *in, int32_t *out, int n, int32_t *tmp, cudaStream_t st) {
     const int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (ntiles > 0) k_scan_tiles<<<capped_grid(k_scan_tiles, ntiles, 1, SCAN_THREADS), SCAN_THREADS, 0, st>>>(
-        in, out, n, tmp, nullptr);
+        const_cast<int32_t *>(in), out, n, tmp, nullptr, 0);
     k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(tmp, ntiles, out, n, nullptr);
     if (ntiles > 0) k_scan_add<<<capped_grid(k_scan_add, ntiles, 1, SCAN_THREADS), SCAN_THREADS, 0, st>>>(
         out, n, tmp, nullptr);
 }
 
+// Cell start table (scan of the histogram, which it clears for the next
+// rebuild), then the cell-ordered particle list by the stable counting sort:
+// passes of 8 bits over the keys [0, C), ping-ponging through inv/wperm
+// (keys) and src/sorted (particles), which the reorder rewrites afterwards;
+// the last pass writes the particles to `sorted`.  Returns the kernels launched.
 int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate) {
+    (void)block;
     if (w.N == 0) return 0;
     int ntiles = (w.C + SCAN_TILE - 1) / SCAN_TILE;
     k_scan_tiles<<<capped_grid(k_scan_tiles, ntiles, 1, SCAN_THREADS), SCAN_THREADS, 0, st>>>(
-        w.cell_count, w.cell_start, w.C, w.scan_tmp, gate);
+        w.cell_count, w.cell_start, w.C, w.scan_tmp, gate, 1);
     k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(w.scan_tmp, ntiles, w.cell_start, w.C, gate);
     k_scan_add<<<capped_grid(k_scan_add, ntiles, 1, SCAN_THREADS), SCAN_THREADS, 0, st>>>(w.cell_start, w.C,
                                                                                           w.scan_tmp, gate);
-    k_scatter<<<capped_grid(k_scatter, w.N, block, block), block, 0, st>>>(w, gate);
-    k_cell_order<<<capped_grid(k_cell_order, w.C, 256, 256), 256, 0, st>>>(w, gate);
+    int k = 3;
+    const int passes = sort_passes(w.C);
+    const int g = sort_grid(w.N, 2 * device_sms());
+    uint32_t *keyA = reinterpret_cast<uint32_t *>(w.inv), *keyB = reinterpret_cast<uint32_t *>(w.wperm);
+    SortWorldFirst first{w.live, w.meta, w.act, w.o2i, w.keys, w.N};
+    SortArrays prev{nullptr, nullptr, 0, w.cell_start + w.C};
+    for (int p = 0; p < passes; ++p) {
+        const bool last = p == passes - 1;
+        const bool setA = ((passes - 1 - p) & 1) != 0;  // odd distance from the last pass: inv/src
+        uint32_t *ok = last ? nullptr : (setA ? keyA : keyB);
+        int32_t *ov = last ? w.sorted : (setA ? w.src : w.sorted);
+        if (p == 0) launch_sort_pass(first, 0, g, w.sort_counts, ok, ov, st, gate);
+        else launch_sort_pass(prev, 8 * p, g, w.sort_counts, ok, ov, st, gate);
+        prev.key = ok;
+        prev.val = ov;
+        k += 3;
+    }
     if (w.S == 1)
         k_window_order<1024><<<capped_grid(k_window_order<1024>, w.N, 1024, 1024), 1024, 0, st>>>(w, gate);
     else
         k_window_order<128><<<capped_grid(k_window_order<128>, w.N, 128, 128), 128, 0, st>>>(w, gate);
-    return 0;
+    return k + 1;
 }
 
 // --------------------------------------------------------------- reorder

@@ -2,12 +2,17 @@
 //
 // dem_broad_phase_noalloc() computes, for n particles given as device float4
 // {x, y, radius, -}, their search-cell keys, the particle indices in stable
-// cell order and the cell start table -- the same three outputs as the
-// context's broad phase (dem_debug_broad_phase) -- without calling
+// cell order and the cell start table -- the three outputs of the context's
+// broad phase (dem_debug_broad_phase), with one difference: the context keeps
+// a scene's large particles out of the search cells (they head its last
+// cell), while here every particle with a radius is keyed by its position and
+// the last cell holds the zero-radius particles only -- without calling
 // cudaMalloc, cudaFree or any allocating routine.  Its only scratch (one
-// counter per cell and one sum per scan tile) lives in the file-scope device
-// array below, of fixed size, which every GPU that loads the library keeps
-// until the process exits.
+// counter per cell and one sum per scan tile, then the sort's per-block digit
+// counts in the same words) lives in the file-scope device array below, of
+// fixed size, which every GPU that loads the library keeps until the process
+// exits.  The order comes from the stable counting sort of dem_sort.cuh, with
+// the caller's d_keys buffer as its second buffer (the keys are written last).
 //
 // Who needs this: code that runs where allocation is not allowed or not
 // possible -- inside a caller's memory pool that owns the whole device heap,
@@ -21,6 +26,7 @@
 #include <string>
 
 #include "dem.h"
+#include "dem_sort.cuh"
 
 namespace {
 
@@ -28,8 +34,11 @@ constexpr int NA_THREADS = 256;
 constexpr int NA_PER_THREAD = 8;
 constexpr int NA_TILE = NA_THREADS * NA_PER_THREAD;
 constexpr int NA_TILES_MAX = (DEM_NOALLOC_MAX_CELLS + NA_TILE - 1) / NA_TILE;
+static_assert((long long)demgb::SORT_GRID_MAX * demgb::SORT_BINS <= DEM_NOALLOC_MAX_CELLS,
+              "the sort passes' digit counts fit in the cell counters");
 
-// counters [0, DEM_NOALLOC_MAX_CELLS), then tile sums [.., + NA_TILES_MAX + 1)
+// counters [0, DEM_NOALLOC_MAX_CELLS) (cell histogram, then the sort's digit
+// counts), then tile sums [.., + NA_TILES_MAX + 1)
 static __device__ __align__(256) int32_t g_noalloc_scratch[DEM_NOALLOC_MAX_CELLS + NA_TILES_MAX + 1];
 
 constexpr int MAX_DEVICES = 64;
@@ -64,24 +73,62 @@ __global__ void k_na_zero(int32_t *counts, int c) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c; i += gridDim.x * blockDim.x) counts[i] = 0;
 }
 
-__global__ void k_na_keys(const float4 *__restrict__ pr, int n, float x0, float y0, float inv, int gw,
-                          int gh, int32_t *__restrict__ keys, int32_t *counts) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 p = pr[i];
-    int key;
-    if (p.z == 0.0f) {
-        key = gw * gh;
-    } else {
+// search-cell key of a particle record
+struct NaGrid {
+    float x0, y0, inv;
+    int gw, gh;
+    __device__ __forceinline__ uint32_t key(float4 p) const {
+        if (p.z == 0.0f) return (uint32_t)(gw * gh);
         int a = __float2int_rd((p.x - x0) * inv);
         int b = __float2int_rd((p.y - y0) * inv);
         a = a < 0 ? 0 : (a > gw - 1 ? gw - 1 : a);
         b = b < 0 ? 0 : (b > gh - 1 ? gh - 1 : b);
-        key = b * gw + a;
+        return (uint32_t)(b * gw + a);
     }
-    keys[i] = key;
-    atomicAdd(&counts[key], 1);
+};
+
+constexpr int NA_GRID_CAP = 4096;  // blocks of the per-particle kernels (grid-stride loops)
+
+inline int na_grid(long long n) {
+    long long g = (n + 255) / 256;
+    return (int)(g < 1 ? 1 : (g > NA_GRID_CAP ? NA_GRID_CAP : g));
 }
+
+__global__ void k_na_count(const float4 *__restrict__ pr, int n, NaGrid g, int32_t *counts) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&counts[g.key(pr[i])], 1);
+}
+
+__global__ void k_na_write_keys(const float4 *__restrict__ pr, int n, NaGrid g, int32_t *__restrict__ keys) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        keys[i] = (int32_t)g.key(pr[i]);
+}
+
+// the sort's inputs: the particles in index order (first pass), then the
+// previous pass's particle list, keys recomputed from the positions
+struct NaFirst {
+    const float4 *pr;
+    int n;
+    NaGrid g;
+    __device__ __forceinline__ int length() const { return n; }
+    __device__ __forceinline__ bool get(int t, uint32_t &k, int32_t &v) const {
+        k = g.key(pr[t]);
+        v = t;
+        return true;
+    }
+};
+struct NaNext {
+    const float4 *pr;
+    const int32_t *val;
+    int n;
+    NaGrid g;
+    __device__ __forceinline__ int length() const { return n; }
+    __device__ __forceinline__ bool get(int t, uint32_t &k, int32_t &v) const {
+        v = val[t];
+        k = g.key(pr[v]);
+        return true;
+    }
+};
 
 __device__ __forceinline__ int na_warp_incl(int v) {
     int lane = threadIdx.x & 31;
@@ -154,30 +201,6 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_scan_add(int32_t *out, int n,
         if (base + k < n) out[base + k] += add;
 }
 
-__global__ void k_na_scatter(const int32_t *__restrict__ keys, int n, const int32_t *__restrict__ start,
-                             int32_t *counts, int32_t *__restrict__ order) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int key = keys[i];
-    order[start[key] + atomicSub(&counts[key], 1) - 1] = i;
-}
-
-// members of each cell in ascending particle index (a stable sort by key)
-__global__ void k_na_cell_order(const int32_t *__restrict__ start, int c, int32_t *order) {
-    int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= c) return;
-    int beg = start[cell], end = start[cell + 1];
-    for (int a = beg + 1; a < end; ++a) {
-        int v = order[a];
-        int b = a - 1;
-        while (b >= beg && order[b] > v) {
-            order[b + 1] = order[b];
-            --b;
-        }
-        order[b + 1] = v;
-    }
-}
-
 }  // namespace
 
 extern "C" {
@@ -188,6 +211,7 @@ int dem_broad_phase_noalloc(const float *d_pos_radius, int32_t n, float x0, floa
                             int32_t gw, int32_t gh, int32_t *d_keys, int32_t *d_order,
                             int32_t *d_cell_start, void *stream) {
     if (n < 0 || gw <= 0 || gh <= 0) return na_fail(DEM_E_INVALID, "n must be >= 0 and the grid non-empty");
+    if (n > (1 << 30)) return na_fail(DEM_E_CAPACITY, "n is above 2^30 particles");
     if ((long long)gw * gh + 1 > DEM_NOALLOC_MAX_CELLS)
         return na_fail(DEM_E_CAPACITY, "grid has more cells than DEM_NOALLOC_MAX_CELLS (262144, incl. the "
                                        "cell of zero-radius particles)");
@@ -201,18 +225,32 @@ int dem_broad_phase_noalloc(const float *d_pos_radius, int32_t n, float x0, floa
     if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int c = gw * gh + 1;
-    int32_t *counts = scratch;
+    int32_t *counts = scratch;  // the cell histogram, then the sort passes' digit counts
     int32_t *tile_sums = scratch + DEM_NOALLOC_MAX_CELLS;
     const int ntiles = (c + NA_TILE - 1) / NA_TILE;
+    const float4 *pr = reinterpret_cast<const float4 *>(d_pos_radius);
+    const NaGrid g{x0, y0, inv_cell, gw, gh};
     k_na_zero<<<(c + 255) / 256, 256, 0, st>>>(counts, c);
-    if (n > 0)
-        k_na_keys<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float4 *>(d_pos_radius), n, x0,
-                                                   y0, inv_cell, gw, gh, d_keys, counts);
+    if (n > 0) k_na_count<<<na_grid(n), 256, 0, st>>>(pr, n, g, counts);
     k_na_scan_tiles<<<ntiles, NA_THREADS, 0, st>>>(counts, d_cell_start, c, tile_sums);
     k_na_scan_sums<<<1, NA_THREADS, 0, st>>>(tile_sums, ntiles, d_cell_start, c);
     k_na_scan_add<<<ntiles, NA_THREADS, 0, st>>>(d_cell_start, c, tile_sums);
-    if (n > 0) k_na_scatter<<<(n + 255) / 256, 256, 0, st>>>(d_keys, n, d_cell_start, counts, d_order);
-    k_na_cell_order<<<(c + 255) / 256, 256, 0, st>>>(d_cell_start, c, d_order);
+    if (n > 0) {
+        // passes ping-pong between d_keys and d_order and end in d_order
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+        const int grid = demgb::sort_grid(n, 2 * sms);
+        const int passes = demgb::sort_passes(c);
+        const int32_t *prev = nullptr;
+        for (int p = 0; p < passes; ++p) {
+            int32_t *out = ((passes - 1 - p) & 1) ? d_keys : d_order;
+            if (p == 0) demgb::launch_sort_pass(NaFirst{pr, n, g}, 0, grid, counts, nullptr, out, st, nullptr);
+            else demgb::launch_sort_pass(NaNext{pr, prev, n, g}, 8 * p, grid, counts, nullptr, out, st, nullptr);
+            prev = out;
+        }
+        k_na_write_keys<<<na_grid(n), 256, 0, st>>>(pr, n, g, d_keys);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return na_fail(DEM_E_CUDA, cudaGetErrorString(e));
     return DEM_OK;

@@ -139,6 +139,7 @@ struct DevWorld {
     uint32_t *keys;
     int32_t *cell_count, *cell_start, *sorted, *inv, *src, *scan_tmp;
     int32_t *wperm;             // rebuild: cell-order position -> position after grouping by contact count
+    int32_t *sort_counts;       // [SORT_GRID_MAX][256] digit counts / offsets of the cell sort's passes
     // bond breaks of the current step (applied after the Simulation pass)
     Pending *pend;
     uint32_t *pend_count;
@@ -200,6 +201,7 @@ constexpr int TICKET_MAX_N = 131072;
 int launch_lom(const DevWorld &w, int block, cudaStream_t st, bool in_graph,
                 cudaGraphConditionalHandle cond);
 void launch_keys(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
+// returns the number of kernels launched
 int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
 void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStream_t st,
                     const int32_t *gate);

@@ -10,6 +10,7 @@
 #include <memory>
 #include <thread>
 
+#include "dem_sort.cuh"
 #include "dem_world_host.h"
 
 namespace demgb {
@@ -495,6 +496,7 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
     w.inv = dalloc<int32_t>(owned, N, ok);
     w.src = dalloc<int32_t>(owned, N, ok);
     w.wperm = dalloc<int32_t>(owned, N, ok);
+    w.sort_counts = dalloc<int32_t>(owned, (size_t)SORT_GRID_MAX * SORT_BINS, ok);
     w.scan_tmp = dalloc<int32_t>(owned, scan_tmp_size(C), ok);
     w.pend_cap = (uint32_t)std::max<long long>(2LL * B + 64, 64);
     w.pend = dalloc<Pending>(owned, w.pend_cap, ok);
@@ -1550,10 +1552,10 @@ int World::kernel_time(int kind, double *ms, long long *n) {
 // rebuild is due (plain launches); otherwise they run only when it is due
 void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate, bool every_step) {
     launch_keys(d, block, st, gate);
-    launch_broad_phase(d, block, st, gate);
+    const int bp = launch_broad_phase(d, block, st, gate);
     launch_reorder(d, spare, block, st, gate);
     launch_list_build(d, block, st, gate, every_step);
-    rebuild_kernels = 1 + 6 + 3 + 2;
+    rebuild_kernels = 1 + bp + 3 + 2;
 }
 
 // One step with plain launches; the rebuild kernels run every step and

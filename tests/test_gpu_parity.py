@@ -214,6 +214,69 @@ def test_out_of_grid_and_nan_particles_bit_exact():
     assert_same_state(g, o)
 
 
+def _append_particles(sc, pos, radii, vel):
+    """The scene with particles appended (no contacts, no fixity, material 0)."""
+    m = radii.shape[0]
+    out = copy_scene(sc)
+    add = {"pos": pos.astype(np.float32).reshape(-1), "radii": radii.astype(np.float32),
+           "vel": vel.astype(np.float32).reshape(-1), "acc": np.zeros(2 * m, np.float32),
+           "rot": np.zeros(m, np.float32), "rot_vel": np.zeros(m, np.float32), "rot_acc": np.zeros(m, np.float32),
+           "forces": np.zeros(6 * m, np.float32), "fixity": np.zeros(6 * m, np.int32),
+           "del_pos": np.zeros(2 * m, np.float32), "del_rot": np.zeros(m, np.float32),
+           "contacts": np.full(6 * 14 * m, -1, np.int32), "material_pointers": np.zeros(m, np.int32),
+           "data": np.zeros(7 * m, np.float32)}
+    for k, v in add.items():
+        out[k] = np.concatenate([sc[k], v])
+    return out
+
+
+def test_crowded_cells_sort_in_linear_time():
+    """The cell order is a stable counting sort whose cost does not depend on
+    how many particles share a cell.  A packed bed plus 50,000 zero-radius
+    particles (one dead cell) and 50,000 particles thrown out of the search
+    grid at 1,000 units a step, so that every rebuild (one per step: they
+    move beyond the skin) clamps them all into the grid's corner cell: the
+    run takes well under a second of GPU time for 40 steps and equals the
+    oracle bit for bit (the thrown particles are beyond the reference's
+    bucket grid, so they find no partners in either)."""
+    import time
+    sc, p, ext = dem_scenes.dense_bed(2000, seed=5)
+    p = dict(p)
+    p["round_bounds"] = 1
+    p["bound_radius"] = 1.0e6
+    rng = np.random.default_rng(11)
+    nz = 50000
+    zpos = rng.uniform(-40.0, 40.0, size=(nz, 2))
+    side = 224
+    gx, gy = np.meshgrid(np.arange(side), np.arange(side))
+    x0 = sc["pos"].reshape(-1, 2).max(axis=0) + 10.0
+    tpos = np.stack([x0[0] + 4.0 * gx.ravel(), x0[1] + 4.0 * gy.ravel()], axis=1)
+    nt = tpos.shape[0]
+    tvel = np.full((nt, 2), 1.0e7)
+    sc = _append_particles(sc, zpos, np.zeros(nz), np.zeros((nz, 2)))
+    sc = _append_particles(sc, tpos, np.full(nt, 1.0), tvel)
+    n = sc["radii"].shape[0]
+    o = copy_scene(sc)
+    with dem.Context(sc, p) as ctx:
+        _, _, _, gw, gh = ctx.search_grid()
+        ctx.step(1)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.step(40)
+        ctx.synchronize()
+        dt = time.perf_counter() - t0
+        keys, order, cs = ctx.broad_phase()
+        g = ctx.download()
+        stats = ctx.stats()
+    oracle.step(o, p, 41)
+    assert stats["reorders"] >= 40
+    assert np.count_nonzero(keys == gw * gh - 1) == nt, "the thrown particles share the corner cell"
+    assert np.count_nonzero(keys == gw * gh) == nz
+    assert np.array_equal(order, np.lexsort((np.arange(n), keys)))
+    assert dt < 2.0, "40 steps with 40 rebuilds took %.2f s" % dt
+    assert_same_state(g, o)
+
+
 def test_large_scene_layout_on_host_threads_bit_exact():
     """Above 2^18 particles the layout is derived on host threads (the median
     radius from a histogram of the radii's float bits, then a selection in
