@@ -16,9 +16,9 @@
 //            in blocks < b (an exclusive scan over digit-major order);
 //   scatter  each block walks its range again in chunks of SORT_CHUNK; within a
 //            chunk each warp owns SORT_IPT rounds of 32 consecutive elements and
-//            ranks them by a warp multi-split (__match_any_sync on the digit,
-//            then popc of the lower lanes with the same digit, added to the
-//            warp's running digit count), the warps' digit counts are scanned
+//            ranks them by a warp multi-split (a ballot per digit bit gives
+//            the lanes with the same digit; popc of the lower ones, added to
+//            the warp's running digit count), the warps' digit counts are scanned
 //            in warp order, and every element is written to
 //            offset[digit] + (its rank among the chunk's equal digits).
 // Ranks therefore follow the sequence order inside warps, across warps and
@@ -60,6 +60,20 @@ inline int sort_grid(long long max_len, int cap) {
     return g > 0 ? (int)g : 1;
 }
 
+// The lanes of the warp holding the same digit as this lane (d in [0, 256);
+// d = 256 marks a lane without an element, whose result is not used): one
+// ballot per digit bit, each lane keeping the lanes that agree with it.
+__device__ __forceinline__ unsigned digit_peers(int d) {
+    unsigned m = __ballot_sync(0xffffffffu, d < SORT_BINS);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool bit = (d >> b) & 1;
+        const unsigned x = __ballot_sync(0xffffffffu, bit);
+        m &= bit ? x : ~x;
+    }
+    return m;
+}
+
 __device__ __forceinline__ bool sort_gated_off(const int32_t *gate) {
     return gate != nullptr && *(volatile const int32_t *)gate == 0;
 }
@@ -98,15 +112,24 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_count(In in, int shift, i
     int beg, end;
     sort_block_range(in.length(), beg, end);
     const int lane = threadIdx.x & 31;
-    // whole warps step through the range together (match_any needs every lane)
-    for (int base = beg + (int)(threadIdx.x & ~31u); base < end; base += SORT_THREADS) {
-        const int t = base + lane;
-        uint32_t k = 0;
-        int32_t v = 0;
-        const bool ok = t < end && in.get(t, k, v);
-        const int d = ok ? (int)((k >> shift) & 255u) : SORT_BINS;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        if (ok && lane == __ffs(peers) - 1) atomicAdd(&h[d], __popc(peers));
+    // chunks of SORT_CHUNK: every element of the thread is requested before
+    // any is counted, so the loads overlap instead of following one another;
+    // whole warps step together (the ballots need every lane)
+    for (int cb = beg; cb < end; cb += SORT_CHUNK) {
+        int dig[SORT_IPT];
+#pragma unroll
+        for (int k = 0; k < SORT_IPT; ++k) {
+            const int t = cb + k * SORT_THREADS + (int)threadIdx.x;
+            uint32_t kk = 0;
+            int32_t vv = 0;
+            const bool ok = t < end && in.get(t, kk, vv);
+            dig[k] = ok ? (int)((kk >> shift) & 255u) : SORT_BINS;
+        }
+#pragma unroll
+        for (int k = 0; k < SORT_IPT; ++k) {
+            const unsigned peers = digit_peers(dig[k]);
+            if (dig[k] < SORT_BINS && lane == __ffs(peers) - 1) atomicAdd(&h[dig[k]], __popc(peers));
+        }
     }
     __syncthreads();
     for (int d = threadIdx.x; d < SORT_BINS; d += SORT_THREADS) counts[blockIdx.x * SORT_BINS + d] = h[d];
@@ -124,7 +147,7 @@ static __global__ void __launch_bounds__(SORT_OFFSET_THREADS) k_sort_offsets(int
     const int per = (g + Q - 1) / Q;
     const int b0 = q * per, b1 = b0 + per < g ? b0 + per : g;
     int s = 0;
-#pragma unroll 4
+#pragma unroll 16
     for (int b = b0; b < b1; ++b) s += counts[b * SORT_BINS + d];
     part[q][d] = s;
     __syncthreads();
@@ -151,29 +174,44 @@ static __global__ void __launch_bounds__(SORT_OFFSET_THREADS) k_sort_offsets(int
     __syncthreads();
     int run = dbase[d];
     for (int x = 0; x < q; ++x) run += part[x][d];
-#pragma unroll 4
-    for (int b = b0; b < b1; ++b) {
-        const int c = counts[b * SORT_BINS + d];
-        counts[b * SORT_BINS + d] = run;
-        run += c;
+    // groups of 16 counts loaded together, then rewritten as offsets
+    for (int b = b0; b < b1; b += 16) {
+        int c[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) c[u] = b + u < b1 ? counts[(b + u) * SORT_BINS + d] : 0;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            if (b + u < b1) counts[(b + u) * SORT_BINS + d] = run;
+            run += c[u];
+        }
     }
 }
 
-// out_key may be null (last pass: only the values are needed)
+// out_key may be null (last pass: only the values are needed).
+// Each chunk is first put in digit order in shared memory (stable), then
+// written out by consecutive threads, so that the elements of one digit go
+// to consecutive addresses in whole runs instead of one scattered word per
+// lane.
 template <class In>
 __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(In in, int shift, const int32_t *__restrict__ offsets,
                                                                uint32_t *__restrict__ out_key,
                                                                int32_t *__restrict__ out_val, const int32_t *gate) {
     if (sort_gated_off(gate)) return;
-    __shared__ int wh[SORT_WARPS * SORT_BINS];  // per warp and digit: count, then the warp's offset
+    // per warp and digit: count, then the warp's offset in the digit (at most
+    // SORT_CHUNK, so 16 bits; the static shared memory stays under 48 KB)
+    __shared__ uint16_t wh[SORT_WARPS * SORT_BINS];
     __shared__ int run[SORT_BINS];              // next global position of each digit
+    __shared__ int cbase[SORT_BINS + 1];        // chunk: first staged position of each digit; [256] = total
+    __shared__ int wsum[SORT_BINS / 32];
+    __shared__ uint32_t skey[SORT_CHUNK];
+    __shared__ int32_t sval[SORT_CHUNK];
     int beg, end;
     sort_block_range(in.length(), beg, end);
     if (beg >= end) return;  // uniform for the block
     for (int d = threadIdx.x; d < SORT_BINS; d += SORT_THREADS) run[d] = offsets[blockIdx.x * SORT_BINS + d];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
-    int *my = wh + warp * SORT_BINS;
+    uint16_t *my = wh + warp * SORT_BINS;
     for (int cb = beg; cb < end; cb += SORT_CHUNK) {
         for (int d = lane; d < SORT_BINS; d += 32) my[d] = 0;
         __syncwarp();
@@ -181,46 +219,84 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(In in, int shift,
         int32_t val[SORT_IPT];
         int dig[SORT_IPT], off[SORT_IPT];
         const int w0 = cb + warp * (32 * SORT_IPT);
+        // every element of the thread requested before any is ranked
 #pragma unroll
         for (int k = 0; k < SORT_IPT; ++k) {
             const int t = w0 + k * 32 + lane;  // < end + SORT_CHUNK <= INT_MAX (lengths are at most 2^30)
             uint32_t kk = 0;
             int32_t vv = 0;
             const bool ok = t < end && in.get(t, kk, vv);
-            const int d = ok ? (int)((kk >> shift) & 255u) : SORT_BINS;
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-            int o = 0;
-            if (ok) o = my[d] + __popc(peers & below);
-            __syncwarp();
-            if (ok && lane == __ffs(peers) - 1) my[d] += __popc(peers);
-            __syncwarp();
             key[k] = kk;
             val[k] = vv;
-            dig[k] = d;
+            dig[k] = ok ? (int)((kk >> shift) & 255u) : SORT_BINS;
+        }
+        // rank among the warp's elements of the same digit, in sequence order
+#pragma unroll
+        for (int k = 0; k < SORT_IPT; ++k) {
+            const int d = dig[k];
+            const unsigned peers = digit_peers(d);
+            int o = 0;
+            if (d < SORT_BINS) o = my[d] + __popc(peers & below);
+            __syncwarp();
+            if (d < SORT_BINS && lane == __ffs(peers) - 1) my[d] = (uint16_t)(my[d] + __popc(peers));
+            __syncwarp();
             off[k] = o;
         }
         __syncthreads();
-        // per digit: the warps' counts become offsets, in warp (= sequence) order
-        for (int d = threadIdx.x; d < SORT_BINS; d += SORT_THREADS) {
-            int s = run[d];
+        // per digit: the warps' counts become offsets in warp (= sequence)
+        // order; the digit totals are scanned into the chunk's staging order
+        int tot = 0;
+        if (threadIdx.x < SORT_BINS) {
+            const int d = threadIdx.x;
+            int s2 = 0;
 #pragma unroll
             for (int x = 0; x < SORT_WARPS; ++x) {
                 const int c = wh[x * SORT_BINS + d];
-                wh[x * SORT_BINS + d] = s;
-                s += c;
+                wh[x * SORT_BINS + d] = (uint16_t)s2;
+                s2 += c;
             }
-            run[d] = s;
+            tot = s2;
+            int inc = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            if (lane == 31) wsum[d >> 5] = inc;
+            cbase[d] = inc - tot;
         }
         __syncthreads();
+        if (threadIdx.x < SORT_BINS) {
+            const int d = threadIdx.x;
+            int add = 0;
+            for (int x = 0; x < (d >> 5); ++x) add += wsum[x];
+            cbase[d] += add;
+            if (d == SORT_BINS - 1) cbase[SORT_BINS] = cbase[d] + tot;
+        }
+        __syncthreads();
+        // stage in digit order
 #pragma unroll
         for (int k = 0; k < SORT_IPT; ++k) {
             if (dig[k] < SORT_BINS) {
-                const int p = my[dig[k]] + off[k];
-                if (out_key) out_key[p] = key[k];
-                out_val[p] = val[k];
+                const int q = cbase[dig[k]] + my[dig[k]] + off[k];
+                skey[q] = key[k];
+                sval[q] = val[k];
             }
         }
-        __syncthreads();  // wh is rewritten by the next chunk
+        __syncthreads();
+        // write out: consecutive staged elements of a digit to consecutive places
+        const int staged = cbase[SORT_BINS];
+        for (int q = threadIdx.x; q < staged; q += SORT_THREADS) {
+            const uint32_t kk = skey[q];
+            const int d = (int)((kk >> shift) & 255u);
+            const int p = run[d] + (q - cbase[d]);
+            if (out_key) out_key[p] = kk;
+            out_val[p] = sval[q];
+        }
+        __syncthreads();
+        // the next chunk of each digit goes after this one's
+        if (threadIdx.x < SORT_BINS) run[threadIdx.x] += cbase[threadIdx.x + 1] - cbase[threadIdx.x];
+        __syncthreads();
     }
 }
 
