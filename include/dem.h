@@ -110,7 +110,12 @@ typedef struct dem_ext {
                                          device where it reaches pageable host memory through the host's
                                          page tables (Grace), else through a page-locked block; 1: always
                                          through the page-locked block */
-    int32_t reserved[2];
+    int32_t reorder_every;            /* rebuilds per reorder of the particle arrays into cell order; 0 =
+                                         default 8.  Every rebuild sorts by cell and rebuilds the candidate
+                                         lists; the reorder only restores memory locality, which particles
+                                         lose slowly (they move a skin between rebuilds, a cell takes
+                                         many); results do not depend on it */
+    int32_t reserved;
 } dem_ext;
 
 /* One scene in the reference's host layouts (state.rs:69-93).  Arrays hold
@@ -233,6 +238,17 @@ int dem_event(dem_ctx *ctx, int32_t kind, int32_t *selections, int32_t throw_par
  * reference's None, out untouched) or a negative DEM_E_* code. */
 int dem_get_datum(dem_ctx *ctx, const int32_t *selections, double out[10]);
 
+/* Advance with Record on (client.rs:931-974, gather_data): n_steps steps,
+ * each followed by dem_get_datum of the selected particles, without a state
+ * readback per step: the data are gathered on the device and read back in
+ * one copy.  rows[10 * n_steps] receives one datum row per step (the columns
+ * of dem_get_datum; the reference's CSV adds the timestamp dT * generation
+ * and its FPS, settings.rs:2014-2052).  Returns the number of selected
+ * particles (0: the steps run and rows is untouched, the reference's None)
+ * or a negative DEM_E_* code.  The reference's Advance runs one more step
+ * after the recorded ones; call dem_step(ctx, 1) for it. */
+int dem_record(dem_ctx *ctx, int32_t n_steps, const int32_t *selections, double *rows);
+
 /* ---- Batches: many independent scenes stepped together ------------------
  * No counterpart in the reference (one scene per program there).  A batch
  * holds n_scenes scenes resident on one GPU; dem_batch_step advances every
@@ -267,6 +283,8 @@ int dem_batch_break_events(dem_batch *b, dem_break_event *buf, int32_t cap, int3
 int dem_batch_event(dem_batch *b, int32_t scene, int32_t kind, int32_t *selections, int32_t throw_particles,
                     float del_x, float del_y, int32_t ticks);
 int dem_batch_get_datum(dem_batch *b, int32_t scene, const int32_t *selections, double out[10]);
+/* dem_record for one scene of a batch; every scene of the batch steps. */
+int dem_batch_record(dem_batch *b, int32_t scene, int32_t n_steps, const int32_t *selections, double *rows);
 int dem_batch_get_stats(dem_batch *b, dem_stats *out);
 void *dem_batch_stream(dem_batch *b);
 
@@ -317,9 +335,10 @@ const char *dem_bondgen_last_error(void);
 /* ---- Serving: continuous batching of scene requests --------------------
  * No counterpart in the reference.  A server owns device arenas sized once
  * from memory_budget_bytes (and at most ~1.25 x max_active_particles
- * particles, cells_per_particle cells and bonds_per_particle bonds per
- * particle).  Requests (scene + settings + extensions + horizon in steps) are
- * copied at submit and queue on the host.  dem_server_advance(sv, n): (1) the
+ * particles when that is > 0; 0 leaves the budget alone to size them),
+ * cells_per_particle cells and bonds_per_particle bonds per particle.
+ * Requests (scene + settings + extensions + horizon in steps) are copied at
+ * submit (or borrowed, dem_server_submit_borrowed) and queue on the host.  dem_server_advance(sv, n): (1) the
  * scenes that reached their horizon are copied back to host memory and their
  * device ranges freed; (2) queued requests are admitted first come first
  * served while their particles, cells and bonds fit in free ranges and the
@@ -344,6 +363,10 @@ typedef struct dem_server_stats {
     int64_t particle_steps;        /* particle-steps executed so far */
     int64_t capacity_particles, used_particles, device_bytes;
     int64_t steps;                 /* steps of the shared world so far */
+    /* advances at which the queue's head waited: for running particles to
+     * drop below max_active_particles, or for free device ranges (the arenas
+     * the memory budget paid for) */
+    int64_t waits_active, waits_memory;
 } dem_server_stats;
 void dem_server_config_defaults(dem_server_config *cfg);
 int dem_server_create(const dem_server_config *cfg, int device, dem_server **out);
@@ -351,6 +374,14 @@ void dem_server_destroy(dem_server *sv);
 const char *dem_server_last_error(const dem_server *sv);
 int dem_server_submit(dem_server *sv, const dem_scene *scene, const dem_params *params, const dem_ext *ext,
                       int64_t horizon_steps, int64_t *request_id);
+/* dem_server_submit without the copy: the request refers to the caller's
+ * scene arrays (and bond strengths are still copied), which must stay valid
+ * and unchanged until dem_server_poll reports the request, it is cancelled,
+ * or the server is destroyed.  For callers that keep their scenes resident
+ * -- a pool of prepared scenes, inputs mapped from files -- and may queue
+ * many requests: a queued request then holds no host copy of its scene. */
+int dem_server_submit_borrowed(dem_server *sv, const dem_scene *scene, const dem_params *params,
+                               const dem_ext *ext, int64_t horizon_steps, int64_t *request_id);
 int dem_server_advance(dem_server *sv, int32_t n_steps);
 int dem_server_poll(dem_server *sv, int64_t *done_ids, int32_t cap, int32_t *n);
 int dem_server_fetch(dem_server *sv, int64_t id, dem_scene *out, double times[3]);

@@ -31,8 +31,10 @@ int dem_debug_search_grid(dem_ctx *ctx, float *x0, float *y0, float *inv, int32_
 /* Kernel timing: while enabled, dem_step launches without CUDA graphs and
  * brackets every launch of the named kernels with CUDA events on the
  * context's stream.  dem_debug_kernel_time returns the summed device time
- * (milliseconds) and launch count of one kernel ("interact", "lom",
- * "broad_phase", "reorder", "end_step") since timing was enabled. */
+ * (milliseconds) and launch count of one kernel kind since timing was
+ * enabled: "interact", "lom", "end_step", and the rebuild's three phases
+ * "broad_phase" (keys, cell table, sort, grouping), "reorder" and
+ * "candidate_lists" (each launched, gated, at every step). */
 int dem_debug_kernel_timing(dem_ctx *ctx, int32_t enable);
 int dem_debug_kernel_time(dem_ctx *ctx, const char *kernel, double *total_ms, int64_t *launches);
 /* The same kernel timing for a batch. */

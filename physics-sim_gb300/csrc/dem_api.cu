@@ -198,6 +198,12 @@ int dem_get_datum(dem_ctx *ctx, const int32_t *selections, double out[10]) {
     return rc < 0 ? world_rc(ctx, rc) : rc;
 }
 
+int dem_record(dem_ctx *ctx, int32_t n_steps, const int32_t *selections, double *rows) {
+    CTX_GUARD(ctx);
+    const int rc = ctx->world.record(0, selections, n_steps, rows);
+    return rc < 0 ? world_rc(ctx, rc) : rc;
+}
+
 int dem_break_events(dem_ctx *ctx, dem_break_event *buf, int32_t cap, int32_t *n) {
     CTX_GUARD(ctx);
     if (cap < 0 || (cap > 0 && !buf)) return set_err(ctx, DEM_E_INVALID, "bad event buffer");
@@ -248,8 +254,8 @@ int dem_debug_kernel_timing(dem_ctx *ctx, int32_t enable) {
 int dem_debug_kernel_time(dem_ctx *ctx, const char *kernel, double *total_ms, int64_t *launches) {
     CTX_GUARD(ctx);
     if (!kernel) return set_err(ctx, DEM_E_INVALID, "kernel is NULL");
-    static const char *names[5] = {"interact", "lom", "broad_phase", "reorder", "end_step"};
-    for (int k = 0; k < 5; ++k) {
+    static const char *names[6] = {"interact", "lom", "broad_phase", "reorder", "end_step", "candidate_lists"};
+    for (int k = 0; k < 6; ++k) {
         if (std::strcmp(kernel, names[k]) == 0) {
             long long n = 0;
             int rc = ctx->world.kernel_time(k, total_ms, &n);

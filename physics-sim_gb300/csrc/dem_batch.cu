@@ -145,6 +145,12 @@ int dem_batch_get_datum(dem_batch *b, int32_t scene, const int32_t *selections, 
     return rc < 0 ? brc(b, rc) : rc;
 }
 
+int dem_batch_record(dem_batch *b, int32_t scene, int32_t n_steps, const int32_t *selections, double *rows) {
+    BATCH_GUARD(b);
+    const int rc = b->world.record(scene, selections, n_steps, rows);
+    return rc < 0 ? brc(b, rc) : rc;
+}
+
 int dem_batch_break_events(dem_batch *b, dem_break_event *buf, int32_t cap, int32_t *n) {
     BATCH_GUARD(b);
     if (cap < 0 || (cap > 0 && !buf)) return bset(b, DEM_E_INVALID, "bad event buffer");
@@ -175,8 +181,8 @@ int dem_batch_kernel_timing(dem_batch *b, int32_t enable) {
 int dem_batch_kernel_time(dem_batch *b, const char *kernel, double *total_ms, int64_t *launches) {
     BATCH_GUARD(b);
     if (!kernel) return bset(b, DEM_E_INVALID, "kernel is NULL");
-    static const char *names[5] = {"interact", "lom", "broad_phase", "reorder", "end_step"};
-    for (int k = 0; k < 5; ++k) {
+    static const char *names[6] = {"interact", "lom", "broad_phase", "reorder", "end_step", "candidate_lists"};
+    for (int k = 0; k < 6; ++k) {
         if (std::strcmp(kernel, names[k]) == 0) {
             long long n = 0;
             int rc = b->world.kernel_time(k, total_ms, &n);

@@ -69,13 +69,13 @@ __device__ __forceinline__ void search_xy(const ScenePar &P, float x, float y, i
     cy = b < 0 ? 0 : (b > P.g_h - 1 ? P.g_h - 1 : b);
 }
 
-// internal index range of the scene's large particles since the last rebuild
-// (the reorder leaves every cell's members contiguous, in cell order)
-__device__ __forceinline__ void big_range(const DevWorld &w, const ScenePar &P, int &beg, int &cnt) {
-    const int c0 = w.cell_start[P.cell_base];
-    const int b0 = w.cell_start[P.big_cell];
-    beg = P.particle_base + (b0 - c0);
-    cnt = w.cell_start[P.big_cell + 1] - b0;
+// The scene's large particles at the last rebuild: the members of its large
+// particles' cell, sorted[first + k] for k < cnt (in scene-local index
+// order).  The cell list names internal indices whether or not that rebuild
+// reordered the particle arrays.
+__device__ __forceinline__ void big_cell(const DevWorld &w, const ScenePar &P, int &first, int &cnt) {
+    first = w.cell_start[P.big_cell];
+    cnt = w.cell_start[P.big_cell + 1] - first;
 }
 
 struct F3 {
@@ -334,6 +334,13 @@ int launch_lom(const DevWorld &w, int block, cudaStream_t st, bool in_graph,
 // sits under a conditional node and the gate is always 1.
 __device__ __forceinline__ bool gated_off(const int32_t *gate) {
     return gate != nullptr && *(volatile const int32_t *)gate == 0;
+}
+// The reorder kernels (grouping, inverse, gather, copy back) run only in the
+// rebuilds that also reorder: every reorder_every-th, and the first after a
+// change of layout.  In the others the cell list keeps naming the particles
+// at their current internal indices.
+__device__ __forceinline__ bool reorder_off(const DevWorld &w, const int32_t *gate) {
+    return gated_off(gate) || *(volatile const int32_t *)w.reorder == 0;
 }
 
 // Grids of the rebuild kernels are capped at the blocks the SMs hold at
@@ -614,7 +621,7 @@ __device__ __forceinline__ void window_order_one(const DevWorld &w, int r0, int 
 
 template <int WIN>
 __global__ void __launch_bounds__(WIN) k_window_order(DevWorld w, const int32_t *gate) {
-    if (gated_off(gate)) return;
+    if (reorder_off(w, gate)) return;
     __shared__ uint32_t key[WIN];
     __shared__ uint32_t seg_id[WIN];
     __shared__ int wsum[WIN / 32];
@@ -696,7 +703,7 @@ __device__ __forceinline__ void inverse_one(const DevWorld &w, int t) {
 }
 
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_inverse(DevWorld w, const int32_t *gate) {
-    if (gated_off(gate)) return;
+    if (reorder_off(w, gate)) return;
     FOR_EACH_ITEM(t, w.N) inverse_one(w, t);
 }
 
@@ -732,7 +739,7 @@ __device__ __forceinline__ void gather_one(const DevWorld &w, const DevWorld &o,
 }
 
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_gather(DevWorld w, DevWorld o, const int32_t *gate) {
-    if (gated_off(gate)) return;
+    if (reorder_off(w, gate)) return;
     FOR_EACH_ITEM(i, w.N) gather_one(w, o, i);
 }
 
@@ -764,7 +771,7 @@ __device__ __forceinline__ void copy_back_one(const DevWorld &w, const DevWorld 
 }
 
 __global__ void __launch_bounds__(PK_MAX_THREADS) k_copy_back(DevWorld w, DevWorld o, const int32_t *gate) {
-    if (gated_off(gate)) return;
+    if (reorder_off(w, gate)) return;
     FOR_EACH_ITEM(i, w.N) copy_back_one(w, o, i);
 }
 
@@ -826,10 +833,10 @@ __device__ __forceinline__ void list_build_one(const DevWorld &w, int i) {
     }
     int flags = 0;
     if (P.n_big > 0) {
-        int bb, bn;
-        big_range(w, P, bb, bn);
-        for (int b = bb; b < bb + bn; ++b) {
-            const float4 pb = w.pr[b];
+        int bf, bn;
+        big_cell(w, P, bf, bn);
+        for (int k = 0; k < bn; ++k) {
+            const float4 pb = w.pr[w.sorted[bf + k]];
             const float dx = pb.x - pa.x, dy = pb.y - pa.y;
             const float t = (pa.z + pb.z + P.skin) * 1.00001f;
             if (pb.z != 0.0f && dx * dx + dy * dy <= t * t) {
@@ -850,7 +857,10 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_list_build(DevWorld w, const
 __global__ void k_rebuild_done(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     *w.rebuild = 0;
-    w.stats[4] += 1ull;
+    const unsigned long long n = w.stats[4] + 1ull;
+    w.stats[4] = n;
+    // the next rebuild reorders when it is the first of a new group of reorder_every
+    *w.reorder = (w.reorder_every <= 1 || n % (unsigned long long)w.reorder_every == 0ull) ? 1 : 0;
 }
 
 // every_step: launched at every step (plain launches), mostly to return at
@@ -1033,10 +1043,9 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         const int h0 = la.x & 0xFFFF;
         const int lc = h0 & 0xFF;
         if (lc == NL_BIG) {
-            // a large particle: k_big_narrow left its partners, in order
-            int bb, bn;
-            big_range(w, P, bb, bn);
-            const int32_t *acc_g = w.big_acc + 16 * (size_t)(P.big_base + (i - bb));
+            // a large particle: k_big_narrow left its partners, in order, in
+            // the record of the particle's rank in its cell (list word 1)
+            const int32_t *acc_g = w.big_acc + 16 * (size_t)(P.big_base + la.y);
             const int n = acc_g[15];
             for (int q = 0; q < n; ++q) nr_ci[q * IB + threadIdx.x] = acc_g[q];
             nr.cnt = n;
@@ -1089,16 +1098,16 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     accept_partner(w, i + nl_entry(la, lb, __ffs(pass) - 1), ax0, ax1, ay0, ay1, nr);
             }
             if (h0 & NL_NEAR_BIG) {
-                int bb, bn;
-                big_range(w, P, bb, bn);
-                for (int b = bb; b < bb + bn; ++b) narrow_test(w, i, b, pa, ax0, ax1, ay0, ay1, nr);
+                int bf, bn;
+                big_cell(w, P, bf, bn);
+                for (int k = 0; k < bn; ++k) narrow_test(w, i, w.sorted[bf + k], pa, ax0, ax1, ay0, ay1, nr);
             }
         } else {
             unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
             if (P.n_big > 0) {
-                int bb, bn;
-                big_range(w, P, bb, bn);
-                for (int b = bb; b < bb + bn; ++b) narrow_test(w, i, b, pa, ax0, ax1, ay0, ay1, nr);
+                int bf, bn;
+                big_cell(w, P, bf, bn);
+                for (int k = 0; k < bn; ++k) narrow_test(w, i, w.sorted[bf + k], pa, ax0, ax1, ay0, ay1, nr);
             }
             const int local = (int)w.kbuild[i] - P.cell_base;
             const int gx = local % P.g_w, gy = local / P.g_w;
@@ -1474,13 +1483,16 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
     if (s < 0 || !w.act[s]) return;
     const ScenePar &P = w.par[s];
     if (!(P.p.collisions == 1 && w.det[s] != 0)) return;
-    int bb, bn;
-    big_range(w, P, bb, bn);
+    int bf, bn;
+    big_cell(w, P, bf, bn);
     const int k = g - P.big_base;
     if (k >= bn) return;  // this record's particle left the big cell (radius 0)
-    const int i = bb + k;
+    const int i = w.sorted[bf + k];
     const float4 pa = w.pr[i];
     int32_t *out = w.big_acc + 16 * (size_t)g;
+    // the particle's rank in its cell, for its thread in the Simulation
+    // kernel (word 1 of its candidate list, unused by large particles)
+    if (threadIdx.x == 0) reinterpret_cast<int32_t *>(w.nl + 2 * (size_t)i)[1] = k;
     if (pa.z == 0.0f) {
         if (threadIdx.x == 0) out[15] = 0;
         return;
@@ -1519,7 +1531,7 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
         const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
         for (int q = beg + lane; q < end; q += 32) consider(w.sorted[q]);
     }
-    for (int b = bb + threadIdx.x; b < bb + bn; b += BIG_THREADS) consider(b);
+    for (int q = threadIdx.x; q < bn; q += BIG_THREADS) consider(w.sorted[bf + q]);
     __syncthreads();
     int n = scount;
     if (n > BIG_ACC_MAX) {

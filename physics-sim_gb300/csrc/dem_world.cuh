@@ -156,6 +156,8 @@ struct DevWorld {
     float2 *pbuild;             // [N] position at the last rebuild
     uint32_t *kbuild;           // [N] search cell at the last rebuild
     int32_t *rebuild;           // 1 = the next rebuild body runs
+    int32_t *reorder;           // 1 = that rebuild also reorders the particle arrays into cell order
+    int32_t reorder_every;      // rebuilds per reorder
     uint32_t *tickets;          // [2] last-warp counters of k_lom and k_interact
     int32_t ticket;             // 1: those kernels' last warps end the step; 0: separate one-warp kernels
     int32_t split;              // 1: the Simulation pass as k_narrow + k_forces instead of k_interact

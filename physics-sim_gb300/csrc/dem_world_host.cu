@@ -511,6 +511,8 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
     w.pbuild = dalloc<float2>(owned, N, ok);
     w.kbuild = dalloc<uint32_t>(owned, N, ok);
     w.rebuild = dalloc<int32_t>(owned, 1, ok);
+    w.reorder = dalloc<int32_t>(owned, 1, ok);
+    w.reorder_every = reorder_every;
     w.tickets = dalloc<uint32_t>(owned, 2, ok);
     w.fix_ref = dalloc<int32_t>(owned, 6 * (size_t)N, ok);
     w.force_ref = dalloc<float>(owned, 6 * (size_t)N, ok);
@@ -535,6 +537,10 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
     CK(cudaMemsetAsync(w.tickets, 0, 2 * sizeof(uint32_t), stream));
     CK(cudaMemsetAsync(w.nl, 0, sizeof(int4) * 2 * (size_t)(N > 0 ? N : 1), stream));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int32_t), stream));
+    {
+        static const int32_t one = 1;  // the first rebuild reorders
+        CK(cudaMemcpyAsync(w.reorder, &one, 4, cudaMemcpyHostToDevice, stream));
+    }
     CK(cudaMemsetAsync(w.big_scene, 0xFF, sizeof(int32_t) * (size_t)std::max(TB, 1), stream));
     CK(cudaMemsetAsync(w.big_acc, 0, sizeof(int32_t) * 16 * (size_t)std::max(TB, 1), stream));
     CK(cudaMemsetAsync(w.cc3, 0, sizeof(int32_t) * (size_t)S, stream));
@@ -843,9 +849,11 @@ int World::push_det() {
 }
 
 // the next step rebuilds the cell table, the particle order and the candidate lists
+// (and reorders the particle arrays into cell order: the layout changed)
 int World::force_rebuild() {
-    int32_t one = 1;
+    static const int32_t one = 1;
     CK(cudaMemcpyAsync(d.rebuild, &one, 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.reorder, &one, 4, cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
     return DEM_OK;
 }
@@ -1095,6 +1103,8 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
     if (ext.reorder_interval > 0) graph_steps = ext.reorder_interval;
     if (ext.list_skin < 0.0f) return fail(DEM_E_INVALID, "list_skin < 0");
     if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
+    if (ext.reorder_every < 0) return fail(DEM_E_INVALID, "reorder_every < 0");
+    if (ext.reorder_every > 0) reorder_every = ext.reorder_every;
     use_graphs = ext.plain_launches == 0;
     split_narrow = ext.split_narrow != 0;
     fuse_lom = ext.unfused_lom == 0;
@@ -1210,6 +1220,8 @@ int World::build_capacity(long long particles, long long cells, long long bonds,
     }
     if (ext.reorder_interval > 0) graph_steps = ext.reorder_interval;
     if (ext.list_skin > 0.0f) skin_factor = ext.list_skin;
+    if (ext.reorder_every < 0) return fail(DEM_E_INVALID, "reorder_every < 0");
+    if (ext.reorder_every > 0) reorder_every = ext.reorder_every;
     use_graphs = ext.plain_launches == 0;
     split_narrow = ext.split_narrow != 0;
     fuse_lom = ext.unfused_lom == 0;
@@ -1511,7 +1523,7 @@ int World::set_control(int s, const int32_t cc[4]) {
 }
 
 namespace {
-enum { T_INTERACT = 0, T_LOM = 1, T_BROAD = 2, T_REORDER = 3, T_END = 4 };
+enum { T_INTERACT = 0, T_LOM = 1, T_BROAD = 2, T_REORDER = 3, T_END = 4, T_LIST = 5 };
 }
 
 void World::set_timing(bool on) {
@@ -1527,7 +1539,7 @@ void World::set_timing(bool on) {
 }
 
 int World::kernel_time(int kind, double *ms, long long *n) {
-    if (kind < 0 || kind >= 5) return fail(DEM_E_INVALID, "unknown kernel");
+    if (kind < 0 || kind >= N_TIMERS) return fail(DEM_E_INVALID, "unknown kernel");
     CK(cudaStreamSynchronize(stream));
     Timer &t = timers[kind];
     for (size_t k = 0; k + 1 < t.ev.size(); k += 2) {
@@ -1550,12 +1562,29 @@ int World::kernel_time(int kind, double *ms, long long *n) {
 // it is 0); inside a conditional graph node it is always 1.
 // every_step: the kernels are launched at every step and do nothing unless a
 // rebuild is due (plain launches); otherwise they run only when it is due
+// With kernel timing on (plain launches), the three phases are bracketed by
+// events: "broad_phase" (keys, cell table, sort, grouping), "reorder",
+// "candidate_lists".
 void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate, bool every_step) {
+    rec_event(T_BROAD, st);
     launch_keys(d, block, st, gate);
     const int bp = launch_broad_phase(d, block, st, gate);
+    rec_event(T_BROAD, st);
+    rec_event(T_REORDER, st);
     launch_reorder(d, spare, block, st, gate);
+    rec_event(T_REORDER, st);
+    rec_event(T_LIST, st);
     launch_list_build(d, block, st, gate, every_step);
+    rec_event(T_LIST, st);
     rebuild_kernels = 1 + bp + 3 + 2;
+}
+
+void World::rec_event(int kind, cudaStream_t st) {
+    if (!timing) return;
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    cudaEventRecord(e, st);
+    timers[kind].ev.push_back(e);
 }
 
 // One step with plain launches; the rebuild kernels run every step and
@@ -1563,23 +1592,14 @@ void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate, bool every_ste
 // first step runs its own LOM pass; every step but the last runs the next
 // step's LOM pass inside its Simulation kernel.
 void World::enqueue_plain_step(bool first, bool last, bool next_last) {
-    auto rec = [&](int kind, bool begin) {
-        if (!timing) return;
-        cudaEvent_t e;
-        if (cudaEventCreate(&e) != cudaSuccess) return;
-        cudaEventRecord(e, stream);
-        timers[kind].ev.push_back(e);
-        (void)begin;
-    };
+    auto rec = [&](int kind, bool) { rec_event(kind, stream); };
     int k = 0;
     if (first || !fuse_lom) {
         rec(T_LOM, true);
         k += launch_lom(d, block, stream, false, cudaGraphConditionalHandle{});
         rec(T_LOM, false);
     }
-    rec(T_BROAD, true);
     enqueue_rebuild(stream, d.rebuild, true);
-    rec(T_BROAD, false);
     rec(T_INTERACT, true);
     const bool fuse = fuse_lom && !last;
     k += launch_interact(d, block, stream, has_bigs, fuse, next_last, false, cudaGraphConditionalHandle{}, kernel_form);
@@ -2094,6 +2114,68 @@ int World::get_datum(int s, const int32_t *selections, double out[10]) {
     }
     for (int q = 0; q < 10; ++q) out[q] = q == 6 ? sums[q] : sums[q] / (double)k;
     return k;
+}
+
+// Advance with Record on (client.rs:931-974, gather_data): n steps, one at a
+// time, each followed by the datum of the selected particles (get_datum,
+// state.rs:708-737).  Per step one graph launch and one gather launch into a
+// device buffer of rows; the rows come back in one copy per chunk of steps
+// (at most 2^24 floats), summed on the host in double in index order.
+// Returns the number of selected particles; rows[10 * n_steps] is written
+// when it is > 0 (none selected: the steps run and nothing is recorded, as
+// the reference clears its data then).
+int World::record(int s, const int32_t *selections, int n_steps, double *rows) {
+    if (s < 0 || s >= (int)sh.size()) return fail(DEM_E_INVALID, "scene index out of range");
+    if (!selections || (n_steps > 0 && !rows)) return fail(DEM_E_INVALID, "selections/rows is NULL");
+    if (n_steps < 0) return fail(DEM_E_INVALID, "n_steps < 0");
+    const SceneHost &h = sh[s];
+    std::vector<int32_t> idx;
+    for (int i = 0; i < h.n; ++i)
+        if (selections[i] != 0) idx.push_back(i);
+    const int k = (int)idx.size();
+    if (k == 0) {
+        for (int j = 0; j < n_steps; ++j) {
+            const int rc = step(1);
+            if (rc) return rc;
+        }
+        return 0;
+    }
+    const long long per = 10LL * k;  // floats per recorded step
+    const int chunk = (int)std::max<long long>(1, std::min<long long>(n_steps, (1LL << 24) / per));
+    void *dbuf = nullptr;
+    CK(cudaMalloc(&dbuf, sizeof(int32_t) * (size_t)k + sizeof(float) * (size_t)(per * chunk)));
+    int32_t *d_idx = static_cast<int32_t *>(dbuf);
+    float *d_rows = reinterpret_cast<float *>(d_idx + k);
+    std::vector<float> f((size_t)(per * chunk));
+    int rc = DEM_OK;
+    cudaError_t e = cudaMemcpyAsync(d_idx, idx.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) rc = fail(DEM_E_CUDA, std::string("record: ") + cudaGetErrorString(e));
+    for (int s0 = 0; rc == DEM_OK && s0 < n_steps; s0 += chunk) {
+        const int m = std::min(chunk, n_steps - s0);
+        for (int j = 0; j < m && rc == DEM_OK; ++j) {
+            rc = step(1);
+            if (rc == DEM_OK) launch_gather_datum(d, h.particle_base, d_idx, k, d_rows + per * j, stream);
+        }
+        if (rc) break;
+        e = cudaMemcpyAsync(f.data(), d_rows, sizeof(float) * (size_t)(per * m), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) {
+            rc = fail(DEM_E_CUDA, std::string("record: ") + cudaGetErrorString(e));
+            break;
+        }
+        for (int j = 0; j < m; ++j) {
+            double sums[10] = {0.0};
+            for (int t = 0; t < k; ++t) {
+                const float *g = &f[(size_t)(per * j + 10LL * t)];
+                for (int q = 0; q < 10; ++q) sums[q] += q == 6 ? std::fabs((double)g[q]) : (double)g[q];
+            }
+            double *out = rows + 10LL * (s0 + j);
+            for (int q = 0; q < 10; ++q) out[q] = q == 6 ? sums[q] : sums[q] / (double)k;
+        }
+    }
+    cudaStreamSynchronize(stream);
+    cudaFree(dbuf);
+    return rc ? rc : k;
 }
 
 int World::drain_events(std::vector<dem_break_event> &out) {

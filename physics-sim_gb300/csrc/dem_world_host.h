@@ -80,6 +80,7 @@ class World {
     int set_properties(int s, int32_t *selections, const int32_t *props);
     int fixity_event(int s, int kind, int32_t *selections, int throw_vel, float del_x, float del_y, int ticks);
     int get_datum(int s, const int32_t *selections, double out[10]);
+    int record(int s, const int32_t *selections, int n_steps, double *rows);
     int step(int n_steps);
     int sync();
     int drain_events(std::vector<dem_break_event> &out);
@@ -108,6 +109,7 @@ class World {
     int block = 256;
     int graph_steps = 35;          // steps per captured CUDA graph
     float skin_factor = 0.2f;      // candidate-list skin / r_max
+    int reorder_every = 8;         // rebuilds per reorder into cell order
     bool diagnostics = true;
     long long host_step = 0;
     std::vector<SceneHost> sh;
@@ -124,7 +126,9 @@ class World {
         double ms = 0.0;
         long long n = 0;
     };
-    Timer timers[5];
+    static constexpr int N_TIMERS = 6;
+    Timer timers[N_TIMERS];
+    void rec_event(int kind, cudaStream_t st);
     int kernel_time(int kind, double *ms, long long *n);
     void set_timing(bool on);
 

@@ -62,7 +62,7 @@ class Ext(C.Structure):
                 ("block_size", C.c_int32), ("search_cell_factor", C.c_float),
                 ("event_capacity", C.c_int32), ("list_skin", C.c_float),
                 ("plain_launches", C.c_int32), ("split_narrow", C.c_int32), ("unfused_lom", C.c_int32),
-                ("host_copies", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("host_copies", C.c_int32), ("reorder_every", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Scene(C.Structure):
@@ -99,7 +99,7 @@ class ServerConfig(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_int64) for k in ("queued", "running", "completed", "active_particles",
                                          "particle_steps", "capacity_particles", "used_particles",
-                                         "device_bytes", "steps")]
+                                         "device_bytes", "steps", "waits_active", "waits_memory")]
 
 
 class TuneResult(C.Structure):
@@ -127,11 +127,13 @@ SYMBOLS = ["dem_abi_version", "dem_ext_defaults", "dem_last_error", "dem_grid_ca
            "dem_batch_set_params", "dem_batch_set_properties", "dem_batch_break_events",
            "dem_batch_get_stats", "dem_batch_stream", "dem_batch_kernel_timing",
            "dem_batch_kernel_time", "dem_server_config_defaults", "dem_server_create",
-           "dem_server_destroy", "dem_server_last_error", "dem_server_submit", "dem_server_advance",
+           "dem_server_destroy", "dem_server_last_error", "dem_server_submit", "dem_server_submit_borrowed",
+           "dem_server_advance",
            "dem_server_poll", "dem_server_fetch", "dem_server_events", "dem_server_release",
            "dem_server_get_stats", "dem_server_stream", "dem_batch_autotune", "dem_tune_last_error",
            "dem_generate_bonds", "dem_bondgen_last_error", "dem_event", "dem_get_datum",
            "dem_batch_event", "dem_batch_get_datum", "dem_batch_upload_many", "dem_batch_download_many",
+           "dem_record", "dem_batch_record",
            "dem_server_cancel"]
 
 _lib = None
@@ -216,6 +218,8 @@ def lib(path=None):
     L.dem_batch_event.argtypes = [C.c_void_p, C.c_int32, C.c_int32, _IP, C.c_int32, C.c_float, C.c_float,
                                   C.c_int32]
     L.dem_batch_get_datum.argtypes = [C.c_void_p, C.c_int32, _IP, C.POINTER(C.c_double)]
+    L.dem_record.argtypes = [C.c_void_p, C.c_int32, _IP, C.POINTER(C.c_double)]
+    L.dem_batch_record.argtypes = [C.c_void_p, C.c_int32, C.c_int32, _IP, C.POINTER(C.c_double)]
     L.dem_bondgen_last_error.argtypes = []
     L.dem_bondgen_last_error.restype = C.c_char_p
     L.dem_generate_bonds.argtypes = [_FP, _FP, C.c_int32, C.c_int32, C.c_int32, _IP, C.c_int64,
@@ -224,6 +228,7 @@ def lib(path=None):
                                      C.c_int32, C.POINTER(TuneResult)]
     L.dem_server_submit.argtypes = [C.c_void_p, C.POINTER(Scene), C.POINTER(Params), C.POINTER(Ext),
                                     C.c_int64, C.POINTER(C.c_int64)]
+    L.dem_server_submit_borrowed.argtypes = L.dem_server_submit.argtypes
     L.dem_server_advance.argtypes = [C.c_void_p, C.c_int32]
     L.dem_server_poll.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32)]
     L.dem_server_fetch.argtypes = [C.c_void_p, C.c_int64, C.POINTER(Scene), C.POINTER(C.c_double)]
@@ -253,7 +258,8 @@ def make_params(d):
 
 def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnostics=True,
              reorder_interval=0, block_size=0, search_cell_factor=0.0, event_capacity=0,
-             list_skin=0.0, plain_launches=False, split_narrow=0, unfused_lom=0, host_copies=0, keep=None):
+             list_skin=0.0, plain_launches=False, split_narrow=0, unfused_lom=0, host_copies=0, reorder_every=0,
+             keep=None):
     e = Ext()
     lib().dem_ext_defaults(C.byref(e))
     e.use_f64 = 1 if use_f64 else 0
@@ -268,6 +274,7 @@ def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnos
     e.split_narrow = 1 if split_narrow else 0
     e.unfused_lom = 1 if unfused_lom else 0
     e.host_copies = 1 if host_copies else 0
+    e.reorder_every = int(reorder_every)
     for attr, arr in (("bond_normal_strength", bond_sn), ("bond_shear_strength", bond_ss)):
         if arr is not None:
             a = np.ascontiguousarray(arr, dtype=np.float32)
@@ -463,6 +470,19 @@ class Context:
         if rc < 0:
             _check(L, self.h, rc)
         return None if rc == 0 else np.array(out[:], np.float64)
+
+    def record(self, n_steps, selections):
+        """Advance with Record on: n_steps steps, each followed by the datum
+        of the selected particles, gathered on the device and read back once
+        (dem_record).  Returns an (n_steps, 10) float64 array, or None when
+        nothing is selected (the steps still run)."""
+        L = lib()
+        sel = np.ascontiguousarray(selections, dtype=np.int32)
+        rows = np.zeros((max(int(n_steps), 1), 10), np.float64)
+        rc = L.dem_record(self.h, int(n_steps), sel.ctypes.data_as(_IP), rows.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc < 0:
+            _check(L, self.h, rc)
+        return None if rc == 0 else rows[: int(n_steps)]
 
     def break_events(self, cap=1 << 16):
         L = lib()
@@ -690,6 +710,16 @@ class Batch:
         self._check(L.dem_batch_kernel_time(self.h, kernel.encode(), C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
+    def record(self, scene, n_steps, selections):
+        """dem_batch_record: Context.record for one scene (every scene steps)."""
+        sel = np.ascontiguousarray(selections, dtype=np.int32)
+        rows = np.zeros((max(int(n_steps), 1), 10), np.float64)
+        rc = lib().dem_batch_record(self.h, int(scene), int(n_steps), sel.ctypes.data_as(_IP),
+                                    rows.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc < 0:
+            self._check(rc)
+        return None if rc == 0 else rows[: int(n_steps)]
+
     def break_events(self, cap=1 << 18):
         buf = np.zeros(cap, dtype=BREAK_DTYPE)
         n = C.c_int32(0)
@@ -753,17 +783,32 @@ class Server:
         if rc != 0:
             raise DemError(rc, (lib().dem_server_last_error(self.h) or b"").decode())
 
-    def submit(self, scene, params, horizon, **ext_kw):
+    def submit(self, scene, params, horizon, borrow=False, **ext_kw):
+        """Queue a request; returns its id.  borrow=True (dem_server_submit_borrowed):
+        the server refers to `scene`'s arrays instead of copying them, so they
+        must stay unchanged until the request is polled done or cancelled."""
         keep = []
         st = make_scene(scene)
         p = make_params(params)
         e = make_ext(keep=keep, **ext_kw)
         rid = C.c_int64(0)
-        self._check(lib().dem_server_submit(self.h, C.byref(st), C.byref(p), C.byref(e), int(horizon),
-                                            C.byref(rid)))
-        self._templates[rid.value] = {k: (v.copy() if hasattr(v, "copy") else v) for k, v in scene.items()
-                                      if k in F32_KEYS + I32_KEYS + ("grid",)}
+        fn = lib().dem_server_submit_borrowed if borrow else lib().dem_server_submit
+        self._check(fn(self.h, C.byref(st), C.byref(p), C.byref(e), int(horizon), C.byref(rid)))
+        if borrow:
+            self._templates[rid.value] = scene   # the caller's arrays, also the result's shapes
+        else:
+            self._templates[rid.value] = {k: (v.copy() if hasattr(v, "copy") else v) for k, v in scene.items()
+                                          if k in F32_KEYS + I32_KEYS + ("grid",)}
         return rid.value
+
+    def finish(self, rid):
+        """Completion times (submit, admit, done) of a finished request, then
+        release it without copying its result out."""
+        times = (C.c_double * 3)()
+        self._check(lib().dem_server_fetch(self.h, int(rid), None, times))
+        self._check(lib().dem_server_release(self.h, int(rid)))
+        self._templates.pop(rid, None)
+        return times[0], times[1], times[2]
 
     def advance(self, n):
         self._check(lib().dem_server_advance(self.h, int(n)))

@@ -97,7 +97,8 @@ pub struct dem_ext {
     pub split_narrow: i32,
     pub unfused_lom: i32,
     pub host_copies: i32,
-    pub reserved: [i32; 2],
+    pub reorder_every: i32,
+    pub reserved: i32,
 }
 
 /// One scene in the reference's host layouts.
@@ -237,6 +238,7 @@ extern "C" {
     pub fn dem_event(ctx: *mut dem_ctx, kind: i32, selections: *mut i32, throw_particles: i32, del_x: f32,
                      del_y: f32, ticks: i32) -> c_int;
     pub fn dem_get_datum(ctx: *mut dem_ctx, selections: *const i32, out: *mut f64) -> c_int;
+    pub fn dem_record(ctx: *mut dem_ctx, n_steps: i32, selections: *const i32, rows: *mut f64) -> c_int;
 
     pub fn dem_batch_create(scenes: *const *const dem_scene, params: *const dem_params, exts: *const dem_ext,
                             n_scenes: i32, device: c_int, out: *mut *mut dem_batch) -> c_int;
@@ -258,6 +260,8 @@ extern "C" {
     pub fn dem_batch_event(b: *mut dem_batch, scene: i32, kind: i32, selections: *mut i32, throw_particles: i32,
                            del_x: f32, del_y: f32, ticks: i32) -> c_int;
     pub fn dem_batch_get_datum(b: *mut dem_batch, scene: i32, selections: *const i32, out: *mut f64) -> c_int;
+    pub fn dem_batch_record(b: *mut dem_batch, scene: i32, n_steps: i32, selections: *const i32, rows: *mut f64)
+                            -> c_int;
     pub fn dem_batch_get_stats(b: *mut dem_batch, out: *mut dem_stats) -> c_int;
     pub fn dem_batch_stream(b: *mut dem_batch) -> *mut c_void;
 

@@ -40,6 +40,31 @@ def test_texps_replay_equals_oracle_and_golden(golden_dir):
     assert np.array_equal(gx["TEXP_1"][:, 7], traces["TEXP_1"][:, 7])
 
 
+def test_record_path_reproduces_the_texp_exports(golden_dir, tmp_path):
+    """Advance with Record on through the device record path (dem_record:
+    the datum of every step gathered on the device, read back once per
+    call) gives every exported trace of the TEXPS experiments exactly as a
+    state readback after every step does; TEXP_1's Data1 equals the
+    reference's export bit for bit, and the CSV export reads back to the
+    same numbers."""
+    import record
+    from gpu_backend import RecordingGpuBackend
+    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "TEXPS.bin"))
+    n = len(scene["radii"])
+    gx = replay.Replayer(GpuBackend(scene, uni, info["use_f64"]), info["scripts"], n).run()
+    rx = replay.Replayer(RecordingGpuBackend(scene, uni, info["use_f64"]), info["scripts"], n).run()
+    assert set(gx) == set(rx) and len(rx) >= 13
+    for k in gx:
+        assert np.array_equal(gx[k], rx[k]), k
+    traces = np.load(os.path.join(golden_dir, "traces.npz"))
+    assert np.array_equal(rx["TEXP_1"][:, 7], traces["TEXP_1"][:, 7])
+    path = tmp_path / "TEXP_1.csv"
+    record.write_csv(str(path), rx["TEXP_1"])
+    assert open(path).readline().strip() == record.HEADER
+    back = np.loadtxt(str(path), delimiter=",", skiprows=1, dtype=np.float64, ndmin=2)
+    assert np.array_equal(back[:, :11], rx["TEXP_1"])
+
+
 def test_chain_texp_replay_equals_oracle(golden_dir):
     scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "Chain_TEXP.bin"))
     gx = replay.Replayer(GpuBackend(scene, uni, info["use_f64"]), info["scripts"], 3).run()
@@ -111,6 +136,24 @@ def test_large_particle_impact_bit_exact(projectiles):
     assert (c[:, :, 1] == n - 1).sum() > 14
     if projectiles > 1:
         assert (c[n - 1, :, 1] >= n - projectiles).any() or (c[n - 2, :, 1] >= n - projectiles).any()
+
+
+@pytest.mark.parametrize("reorder_every", [1, 100000])
+def test_rebuilds_with_and_without_reorder_bit_exact(reorder_every):
+    """A rebuild every one or two steps (skin 0.02 r_max) on a bonded bed hit
+    by two projectiles: with the particle arrays reordered into cell order at
+    every rebuild, or only at the first (the large particles then found
+    through the cell list, not by position), the run equals the oracle."""
+    sc, p, ext = dem_scenes.c2_impact(cols=48, rows=64, seed=7, projectile_radius=10.0,
+                                      projectile_speed=300.0, projectiles=2)
+    g, o, gev, oev = run_both(sc, p, 300, chunk=100, list_skin=0.02, reorder_every=reorder_every, **ext)
+    assert_same_state(g, o)
+    got = sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in gev)
+    ref = sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in oev)
+    assert got == ref
+    with dem.Context(sc, p, list_skin=0.02, reorder_every=reorder_every, **ext) as ctx:
+        ctx.step(50)
+        assert ctx.stats()["reorders"] >= 20
 
 
 @pytest.mark.parametrize("model", [1, 2, 3])

@@ -2,7 +2,8 @@
 searches), candidate-list skin (re-sort frequency), particle-kernel block
 size, steps per captured graph and the one- or two-kernel Simulation pass
 change speed only -- every scene's state and bond-break events are the same
-bit for bit under any setting."""
+bit for bit under any setting.  So does how often a rebuild reorders the
+particle arrays into cell order (every rebuild, or only the first)."""
 import pytest
 
 import dem
@@ -40,6 +41,8 @@ def _run(items, steps, **kw):
 @pytest.mark.parametrize("knobs", [
     dict(search_cell_factor=0.68, list_skin=0.45, block_size=128, reorder_interval=21, split_narrow=1),
     dict(search_cell_factor=1.36, list_skin=0.1, block_size=512, reorder_interval=70, unfused_lom=1),
+    dict(list_skin=0.1, reorder_every=1),
+    dict(list_skin=0.1, reorder_every=100000, plain_launches=1),
 ])
 def test_knobs_do_not_change_results(knobs):
     items = _items()
