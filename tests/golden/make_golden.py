@@ -1,8 +1,8 @@
 """Generate the golden fixtures under tests/golden/ from the reference checkout.
 
-Run once in a checkout that has the reference at REFERENCE (default
-/root/reference); the outputs are committed, so tests never read the reference
-at run time.  Outputs:
+Run once with REFERENCE set to a checkout of the reference (required; the
+script has no default); the outputs are committed, so tests never read the
+reference at run time.  Outputs:
 
   *.bin        byte copies of the reference's small experiment saved states
                (saved_states/TEXPS.bin, Chain_TEXP.bin, PBEXPS.bin,
@@ -16,6 +16,8 @@ at run time.  Outputs:
                Settings::save_data (settings.rs:2014-2052):
                Timestamp, X/Y Position, X/Y Velocity, Rotation,
                Rotation Velocity, Data1..Data4, FPS
+  TEXP_1_head.csv  the first 12 lines of data/TEXP_1.csv as text: the
+               reference's own CSV formatting of those numbers
 """
 import glob
 import os
@@ -25,12 +27,14 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = os.environ.get("REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("REFERENCE")
 STATES = ["TEXPS.bin", "Chain_TEXP.bin", "PBEXPS.bin", "Chain_EXP.bin", "Strings.bin", "MicroStrings.bin"]
 TRACE_GLOBS = ["TEXP_*.csv", "Chain_T_*.csv", "pb_experiment_*_1.csv", "Chain_[0-9]*.csv"]
 
 
 def main():
+    if not REFERENCE:
+        sys.exit("set REFERENCE to the reference checkout")
     src_states = os.path.join(REFERENCE, "saved_states")
     src_data = os.path.join(REFERENCE, "data")
     if not os.path.isdir(src_states):
@@ -44,6 +48,10 @@ def main():
             rows = np.loadtxt(path, delimiter=",", skiprows=1, dtype=np.float64, ndmin=2)
             traces[key] = rows
     np.savez_compressed(os.path.join(HERE, "traces.npz"), **traces)
+    with open(os.path.join(src_data, "TEXP_1.csv")) as f:
+        head = [next(f) for _ in range(12)]
+    with open(os.path.join(HERE, "TEXP_1_head.csv"), "w") as f:
+        f.writelines(head)
     print("wrote %d states, %d traces" % (len(STATES), len(traces)))
 
 

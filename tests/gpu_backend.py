@@ -27,6 +27,14 @@ class GpuBackend:
         self.ctx.step(n)
 
 
+class RecordingGpuBackend(GpuBackend):
+    """The same backend with the device record path (dem_record) for
+    Advance with Record on, instead of a state readback per step."""
+
+    def record(self, ticks, selections):
+        return self.ctx.record(ticks, selections)
+
+
 def copy_scene(sc):
     return {k: (v.copy() if hasattr(v, "copy") else v) for k, v in sc.items()}
 

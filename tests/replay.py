@@ -110,7 +110,17 @@ class Replayer:
             advanced = False
             if advance is not None:
                 ticks, advance = advance, None
-                if gather:
+                if gather and hasattr(b, "record"):
+                    # the device record path: the same rows, read back once
+                    data = b.record(ticks, selections)
+                    if data is None:
+                        rows = []
+                    for j in range(ticks):
+                        generation += 1
+                        if data is not None:
+                            rows.append([float(np.float32(dt * np.float32(generation)))] + list(data[j]))
+                    b.step(1)
+                elif gather:
                     for _ in range(ticks):
                         b.step(1)
                         generation += 1

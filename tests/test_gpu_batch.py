@@ -238,3 +238,21 @@ def test_bulk_upload_rejects_a_bad_scene_and_writes_nothing():
         after = [b.download(k) for k in range(3)]
     for k in range(3):
         assert_same_state(after[k], before[k], "scene %d: " % k)
+
+
+def test_record_one_scene_of_a_batch_equals_the_scene_alone():
+    """dem_batch_record of one scene (every scene steps) gives the rows
+    dem_record gives for that scene alone."""
+    a = dem_scenes.dense_bed(n=800, seed=21)
+    b = dem_scenes.c3_mix_scene(1200, 0.3, 22)
+    sel = np.zeros(800, np.int32)
+    sel[[3, 100, 555]] = 1
+    with dem.Batch([a, b]) as bt:
+        bt.step(10)
+        got = bt.record(0, 60, sel)
+        none = bt.record(1, 5, np.zeros(1200, np.int32))
+    with dem.Context(a[0], a[1], **a[2]) as ctx:
+        ctx.step(10)
+        ref = ctx.record(60, sel)
+    assert none is None
+    assert got.shape == (60, 10) and np.array_equal(got, ref)
