@@ -47,9 +47,13 @@ def parse_args():
     ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--horizon", type=int, default=5000,
+                    help="c3: simulation steps per scene the timed frames cover from the initial states")
+    ap.add_argument("--settle-steps", type=int, default=20000,
+                    help="c3: also time two frames after the mix has run this many steps (0: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
-    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--serve-min", type=int, default=2000)
     ap.add_argument("--serve-max", type=int, default=256000)
     ap.add_argument("--serve-hmin", type=int, default=1000)
@@ -57,7 +61,7 @@ def parse_args():
     ap.add_argument("--serve-pool", type=int, default=48)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-active", type=int, default=16 << 20)
-    ap.add_argument("--serve-timeout", type=float, default=240.0)
+    ap.add_argument("--serve-timeout", type=float, default=900.0)
     ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuner's picks")
     ap.add_argument("--plain", action="store_true",
                     help="plain kernel launches instead of CUDA graphs, so that ncu can list every "
@@ -243,6 +247,40 @@ def slot_counts(st):
     occ = c[:, 1] != -1
     bonded = occ & (c[:, 5] >= 0)
     return int((occ & ~bonded).sum()), int(bonded.sum())
+
+
+def fp64_twin_error(samples, device):
+    """Error of the FP32 path against the FP64 transcription of the same step
+    (the oracle's twin, a checker run on the host): for each sampled state,
+    one step through the library (a Context on that state) and one step of
+    the twin; per particle |a32 - a64| / scale with scale = (|data[0]| +
+    m g) / m, i.e. the particle's normal-force total (data[0] = sum of F_n)
+    plus its weight, as an acceleration.  `samples` are (state, params, ext)."""
+    import dem
+    import oracle
+    errs = []
+    for st, p, ext in samples:
+        with dem.Context({k: (v.copy() if hasattr(v, "copy") else v) for k, v in st.items()}, p,
+                         device=device, **ext) as ctx:
+            ctx.step(1)
+            s1 = ctx.download()
+        twin = oracle.step_f64(st, p, 1, **_okw(ext))
+        r = st["radii"].astype(np.float64)
+        dens = st["materials"].reshape(-1, 6)[st["material_pointers"], 3].astype(np.float64)
+        mass = dens * np.pi * r * r
+        live = r > 0
+        a32 = s1["acc"].reshape(-1, 2).astype(np.float64)[live]
+        a64 = twin["acc"].reshape(-1, 2)[live]
+        fsum = np.abs(s1["data"].reshape(-1, 7)[live, 0].astype(np.float64))
+        g = 9.81 * float(p.get("gravity_acc", 1.0)) if p.get("gravity", 0) else 0.0
+        scale = (fsum + mass[live] * g) / mass[live]
+        ok = scale > 0
+        errs.append(np.linalg.norm(a32 - a64, axis=1)[ok] / scale[ok])
+    e = np.concatenate(errs) if errs else np.zeros(1)
+    return {"max": float(e.max()), "median": float(np.median(e)), "p99": float(np.percentile(e, 99)),
+            "particles": int(e.size), "states": len(samples),
+            "scale": "per particle (|sum F_n| + m g) / m: one FP32 step of the library vs one step of the "
+                     "oracle's FP64 twin from the same state"}
 
 
 def cpu_baseline(sc, p, ext, seconds, frame):
@@ -479,7 +517,7 @@ def run_reference_batch(args):
         done[k] += steps
         return int(sc["radii"].shape[0]) * steps
 
-    sub = args.frame
+    sub = args.frame if args.frame_given else max(1, args.horizon // max(args.steps, 1))
     for w in range(args.warmup):
         one(w % len(items), 1)
     tot = 0
@@ -490,7 +528,8 @@ def run_reference_batch(args):
     value = tot / dt
     cores = os.cpu_count() or 1
     cfg = dict(desc)
-    cfg.update({"frame_steps": args.frame, "sample": "scene k mod %d advanced %d steps per bench step"
+    cfg.update({"frame_steps": sub, "horizon": "%d steps per scene from the initial states" % args.horizon,
+                "sample": "scene k mod %d advanced %d steps per bench step from its initial state"
                 % (len(items), sub)})
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
@@ -505,6 +544,12 @@ def run_reference_batch(args):
 
 
 def run_ours_batch(args):
+    """c3: the 512-scene mix in one batch.  The timed frames run every scene
+    from its initial state over the configured horizon (frames of F steps, F
+    a multiple of the autotuned graph length, K frames covering at least
+    --horizon steps); warm-up frames run first on the same batch, which is
+    then restored to the initial states (dem_batch_upload_many) before the
+    timed region."""
     import torch
     import build_lib
     import dem
@@ -523,10 +568,14 @@ def run_ours_batch(args):
     if not args.no_tune and not args.plain:
         knobs, tune_info = dem.autotune(items, device=local)
     g = knobs["reorder_interval"]
-    F = args.frame if args.frame_given else g * max(1, -(-35 // g))
+    if args.frame_given:
+        F = args.frame
+    else:
+        F = g * max(1, -(-args.horizon // (args.steps * g)))
     batch = dem.Batch(items, device=local, plain_launches=args.plain, **knobs)
     stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    initial = dem.SceneTable([(k, it[0]) for k, it in enumerate(items)])
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -534,13 +583,25 @@ def run_ours_batch(args):
         if ws > 1:
             torch.distributed.barrier()
 
+    def slots_now():
+        su = sb = 0
+        for k in range(len(items)):
+            a, b2 = slot_counts(batch.download(k))
+            su += a
+            sb += b2
+        return su, sb
+
     for _ in range(args.warmup):
         batch.step(F)
     barrier()
+    batch.upload_many(initial)        # back to the initial states: the timed frames cover the horizon
+    barrier()
+    slots_start = slots_now()
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
     launches0 = batch.stats()["kernel_launches"]
+    rebuilds0 = batch.stats()["reorders"]
     sampler.mark()
     barrier()
     evs = []
@@ -561,14 +622,40 @@ def run_ours_batch(args):
     launches = st["kernel_launches"] - launches0
     sampler.stop()
     dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    frame_ms = [a.elapsed_time(b) for a, b in evs]
     value, max_ms, _ = job_rate(ntot * F * args.steps, dev_ms, ws, dev)
     clocks = sampler.summary()
+    states = [batch.download(k) for k in range(len(items))]
+    s_u = s_b = 0
+    for stt in states:
+        a, b2 = slot_counts(stt)
+        s_u += a
+        s_b += b2
 
-    # the same scenes through the plain single-scene path, one after another
+    # roofline of the Simulation kernel on the state at the end of the
+    # horizon (plain launches with events around every launch)
+    fused = not knobs.get("unfused_lom", 0)
+    alg_bytes = interact_bytes(s_u, s_b, ntot, fused)
+    peak, peak_kind = measured_peaks()
+    roofline = {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
+                "kernel": "k_interact + next step's LOM pass" if fused else "k_interact",
+                "state": "end of the timed horizon (step %d)" % (F * args.steps),
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "slots_unbonded": s_u, "slots_bonded": s_b, "traffic": profiled_traffic(args.workload)}
+    try:
+        kt = BatchKernelTimer(batch)
+        kt.run(2 * F)
+        roofline.update(kt.figures(alg_bytes, peak))
+    except Exception as exc:  # timing is diagnostic; the value above stands
+        roofline["error"] = str(exc)
+    states = [batch.download(k) for k in range(len(items))]
+
+    # the same scenes through the plain single-scene path, one after another,
+    # each from its state at the end of the horizon (F steps)
     plain_ms = 0.0
     plain_ps = 0
-    for sc, p, ext in items:
-        ctx = dem.Context(sc, p, device=local, reorder_interval=35, plain_launches=args.plain, **ext)
+    for (sc, p, ext), stt in zip(items, states):
+        ctx = dem.Context(stt, p, device=local, reorder_interval=35, plain_launches=args.plain, **ext)
         cst = torch.cuda.ExternalStream(ctx.stream(), device=dev)
         ctx.step(35)
         ctx.synchronize()
@@ -582,27 +669,6 @@ def run_ours_batch(args):
         plain_ps += int(sc["radii"].shape[0]) * F
         ctx.close()
     plain_value = plain_ps / (plain_ms / 1e3)
-
-    # roofline of k_interact over the whole batch (plain launches with events)
-    states = [batch.download(k) for k in range(len(items))]
-    s_u = s_b = 0
-    for stt in states:
-        a, b2 = slot_counts(stt)
-        s_u += a
-        s_b += b2
-    fused = not knobs.get("unfused_lom", 0)
-    alg_bytes = interact_bytes(s_u, s_b, ntot, fused)
-    peak, peak_kind = measured_peaks()
-    roofline = {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
-                "kernel": "k_interact + next step's LOM pass" if fused else "k_interact",
-                "algorithmic_bytes_per_launch": alg_bytes,
-                "slots_unbonded": s_u, "slots_bonded": s_b, "traffic": profiled_traffic(args.workload)}
-    try:
-        kt = BatchKernelTimer(batch)
-        kt.run(2 * F)
-        roofline.update(kt.figures(alg_bytes, peak))
-    except Exception as exc:  # timing is diagnostic; the value above stands
-        roofline["error"] = str(exc)
 
     # end to end through the batch API: restore every scene from host arrays,
     # one frame, read every scene back
@@ -631,23 +697,72 @@ def run_ours_batch(args):
            "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": h2d,
            "note": "dem_batch_upload_many of all scenes + dem_batch_step(frame) + dem_batch_download_many of all "
-                   "scenes, from and into the callers' host arrays (scene struct tables built once)"}
+                   "scenes, from and into the callers' host arrays (scene struct tables built once), from the "
+                   "states at the end of the horizon"}
+
+    # settled states: the mix run on (untimed) to --settle-steps, then frames timed there
+    settled = None
+    if args.settle_steps > F * args.steps:
+        batch.upload_many(dem.SceneTable(list(enumerate(states))))
+        left = args.settle_steps - F * args.steps - F
+        batch.step(max(left - left % g, 0))
+        barrier()
+        su2, sb2 = slots_now()
+        sev = []
+        for k in range(2):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            batch.step(F)
+            e1.record(stream)
+            sev.append((e0, e1))
+        barrier()
+        sms = sum(a.elapsed_time(b) for a, b in sev)
+        alg2 = interact_bytes(su2, sb2, ntot, fused)
+        settled = {"after_steps": int(args.settle_steps), "particle_steps_per_s": ntot * F * 2 / (sms / 1e3),
+                   "slots_unbonded": su2, "slots_bonded": sb2, "frames": 2, "frame_steps": F}
+        try:
+            kt = BatchKernelTimer(batch)
+            kt.run(2 * F)
+            fig = kt.figures(alg2, peak)
+            settled.update({"interact_launch_us": fig["launch_us"], "interact_frac": fig["frac"],
+                            "algorithmic_bytes_per_launch": alg2})
+        except Exception as exc:
+            settled["error"] = str(exc)
+        states = [batch.download(k) for k in range(len(items))]
 
     base = None
+    fp64 = None
     if rank == 0 and ws == 1:
         base = cpu_baseline_batch(items, args.cpu_seconds)
+        pick = sorted(set(np.linspace(0, len(items) - 1, 8).astype(int).tolist()))
+        fp64 = fp64_twin_error([(states[k], items[k][1], items[k][2]) for k in pick], local)
+        fp64["sampled_scenes"] = pick
     cfg = dict(desc)
-    cfg.update({"frame_steps": F, "parallelism": "replicas" if ws > 1 else "single",
+    cfg.update({"frame_steps": F, "horizon": "%d steps per scene from the initial states (%d frames of %d)"
+                % (F * args.steps, args.steps, F),
+                "frame_ms": {"first": frame_ms[0], "last": frame_ms[-1], "min": min(frame_ms),
+                             "max": max(frame_ms)},
+                "slots_at_start": {"unbonded": slots_start[0], "bonded": slots_start[1]},
+                "slots_at_end": {"unbonded": s_u, "bonded": s_b},
+                "parallelism": "replicas" if ws > 1 else "single",
                 "l2": "inputs larger than L2 (and a %d MiB write between frames, untimed)" % (FLUSH_BYTES >> 20),
                 "graph_steps": g, "knobs": knobs, "autotune": tune_info,
                 "plain_path_particle_steps_per_s": plain_value,
+                "plain_path_sample": "each scene alone (dem_create per scene), one frame from its end-of-horizon "
+                                     "state",
                 "batched_over_plain": value / plain_value if plain_value else None,
-                "rebuilds": st["reorders"], "list_overflows": st["list_overflows"]})
+                "rebuilds": st["reorders"] - rebuilds0, "list_overflows": st["list_overflows"],
+                "settled": settled})
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": cfg, "clocks": clocks, "roofline": roofline,
             "e2e": e2e, "gpu_launches": int(launches), "wall_s": wall}
+    if fp64 is not None:
+        line["fp64_error"] = fp64
     if base is not None:
         line["cpu_baseline"] = base
     batch.close()
@@ -713,9 +828,12 @@ def cpu_baseline_batch(items, seconds):
 def run_serve(args):
     """c4: Poisson arrivals of scene requests (sizes log-uniform, horizons
     uniform) served by continuous batching; reports aggregate particle-steps/s
-    and completion-latency percentiles of the requests that arrived in the
-    window.  Scene contents come from a seeded pool of pre-built scenes (the
-    cost of building 12k scenes on the host is not part of serving)."""
+    and completion-latency percentiles (arrival to completion) of every
+    request that arrived in the window, with the queue depth over time.
+    Scene contents come from a seeded pool of pre-built scenes (the cost of
+    building 12k scenes on the host is not part of serving); requests refer
+    to the pool's arrays (dem_server_submit_borrowed), so a queued request
+    holds no host copy."""
     import torch
     import build_lib
     import dem
@@ -734,6 +852,7 @@ def run_serve(args):
             for k, n in enumerate(pool_n)]
     pick = rng.integers(0, len(pool), size=len(arrivals))
     horizons = rng.integers(args.serve_hmin, args.serve_hmax + 1, size=len(arrivals))
+    offered = float(sum(int(pool[pick[k]][0]["radii"].shape[0]) * int(horizons[k]) for k in range(len(arrivals))))
     sv = dem.Server(device=local, memory_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
                     max_active_particles=args.serve_active, reorder_interval=35)
     t0 = time.perf_counter()
@@ -741,13 +860,15 @@ def run_serve(args):
     submitted = {}
     done = {}
     max_queue = max_running = 0
+    series = []
+    next_sample = 0.0
     chunk = 35
     limit = t0 + args.serve_timeout
     while len(done) < len(arrivals) and time.perf_counter() < limit:
         now = time.perf_counter() - t0
         while nxt < len(arrivals) and arrivals[nxt] <= now:
             sc, p, ext = pool[pick[nxt]]
-            rid = sv.submit(sc, p, int(horizons[nxt]), **ext)
+            rid = sv.submit(sc, p, int(horizons[nxt]), borrow=True, **ext)
             submitted[rid] = (nxt, int(sc["radii"].shape[0]) * int(horizons[nxt]))
             nxt += 1
         sv.advance(chunk)
@@ -755,9 +876,12 @@ def run_serve(args):
         max_queue = max(max_queue, st["queued"])
         max_running = max(max_running, st["running"])
         tp = time.perf_counter() - t0
+        if tp >= next_sample:
+            series.append([round(tp, 2), int(st["queued"]), int(st["running"]), int(st["active_particles"])])
+            next_sample = tp + 1.0
         for rid in sv.poll():
             k, work = submitted[rid]
-            sv.fetch(rid)
+            sv.finish(rid)
             done[rid] = (k, tp - arrivals[k], work)
         if st["running"] == 0 and st["queued"] == 0 and nxt < len(arrivals):
             time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
@@ -765,22 +889,32 @@ def run_serve(args):
     st = sv.stats()
     sv.close()
     lat = np.array([v[1] for v in done.values()]) if done else np.zeros(1)
+    in_window = [v[1] for v in done.values() if arrivals[v[0]] < window]
     value = st["particle_steps"] / elapsed
+    step_every = max(1, len(series) // 60)
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": 1,
             "steps": int(st["steps"]), "warmup": 0, "ms_per_step": elapsed / max(st["steps"], 1) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "c4 served stream", "arrival_rate_per_s": rate, "arrival_window_s": window,
                        "requests": int(len(arrivals)), "completed": int(len(done)),
+                       "offered_particle_steps": offered,
+                       "offered_particle_steps_per_s_over_window": offered / window,
                        "particles_per_request": "log-uniform [%d, %d] (pool of %d seeded scenes)"
                        % (args.serve_min, args.serve_max, args.serve_pool),
                        "horizon_steps": "uniform [%d, %d]" % (args.serve_hmin, args.serve_hmax),
                        "memory_budget_gb": args.serve_budget_gb, "max_active_particles": args.serve_active,
                        "capacity_particles": st["capacity_particles"], "device_bytes": st["device_bytes"],
+                       "admission_waits": {"on_max_active_particles": int(st["waits_active"]),
+                                           "on_device_ranges": int(st["waits_memory"])},
                        "max_queue": int(max_queue), "max_running": int(max_running),
-                       "advance_chunk_steps": chunk, "elapsed_s": elapsed},
+                       "queue_depth_series": {"columns": ["t_s", "queued", "running", "active_particles"],
+                                              "rows": series[::step_every]},
+                       "advance_chunk_steps": chunk, "elapsed_s": elapsed,
+                       "drained": bool(len(done) == len(arrivals))},
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
-                          "p99": float(np.percentile(lat, 99)), "max": float(lat.max())}}
+                          "p99": float(np.percentile(lat, 99)), "max": float(lat.max()),
+                          "of": "arrival to completion, every completed request (%d)" % len(in_window)}}
     print(json.dumps(line), flush=True)
 
 

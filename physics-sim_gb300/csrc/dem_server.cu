@@ -97,6 +97,7 @@ struct dem_server {
     int64_t active_particles = 0;
     int64_t particle_steps = 0;
     int64_t completed = 0;
+    int64_t waits_active = 0, waits_memory = 0;
 };
 
 namespace {
@@ -153,13 +154,18 @@ int admit_queued(dem_server *sv) {
         Request &r = *sv->reqs[sv->queue.front()];
         if (sv->cfg.max_active_particles > 0 &&
             sv->active_particles + r.in.view.n_particles > sv->cfg.max_active_particles &&
-            sv->active_particles > 0)
+            sv->active_particles > 0) {
+            sv->waits_active++;
             break;
+        }
         dem_ext e = r.ext;
         e.bond_normal_strength = r.sn.empty() ? nullptr : r.sn.data();
         e.bond_shear_strength = r.ss.empty() ? nullptr : r.ss.data();
         int slot = sv->world.admit(&r.in.view, r.params, e, r.horizon);
-        if (slot == DEM_E_CAPACITY && sv->active_particles > 0) break;  // waits for ranges to free
+        if (slot == DEM_E_CAPACITY && sv->active_particles > 0) {  // waits for ranges to free
+            sv->waits_memory++;
+            break;
+        }
         if (slot == DEM_E_CAPACITY || slot == DEM_E_INVALID || slot == DEM_E_UNSUPPORTED) {
             // the request itself cannot run here: fail it, keep serving the rest
             fail_request(sv, r, slot, sv->world.err);
@@ -271,16 +277,21 @@ void dem_server_destroy(dem_server *sv) {
     if (st) cudaStreamDestroy(st);
 }
 
-int dem_server_submit(dem_server *sv, const dem_scene *scene, const dem_params *params, const dem_ext *ext,
-                      int64_t horizon_steps, int64_t *request_id) {
-    SERVER_GUARD(sv);
+}  // extern "C"
+
+namespace {
+// a request queued with its own copy of the scene (borrow = false) or
+// referring to the caller's arrays until it is done (borrow = true)
+int submit(dem_server *sv, const dem_scene *scene, const dem_params *params, const dem_ext *ext,
+           int64_t horizon_steps, int64_t *request_id, bool borrow) {
     if (!scene || !params || horizon_steps <= 0) return sset(sv, DEM_E_INVALID, "bad request");
     if (scene->n_particles < 0 || (long long)scene->n_particles > sv->world.a_part.capacity())
         return sset(sv, DEM_E_CAPACITY, "request has more particles than the server's arena (" +
                                             std::to_string(sv->world.a_part.capacity()) + ")");
     auto r = std::make_unique<Request>();
     r->id = sv->next_id++;
-    r->in.from(*scene, true);
+    if (borrow) r->in.view = *scene;
+    else r->in.from(*scene, true);
     r->params = *params;
     if (ext) r->ext = *ext;
     else dem_ext_defaults(&r->ext);
@@ -296,6 +307,21 @@ int dem_server_submit(dem_server *sv, const dem_scene *scene, const dem_params *
     sv->queue.push_back(r->id);
     sv->reqs[r->id] = std::move(r);
     return DEM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int dem_server_submit(dem_server *sv, const dem_scene *scene, const dem_params *params, const dem_ext *ext,
+                      int64_t horizon_steps, int64_t *request_id) {
+    SERVER_GUARD(sv);
+    return submit(sv, scene, params, ext, horizon_steps, request_id, false);
+}
+
+int dem_server_submit_borrowed(dem_server *sv, const dem_scene *scene, const dem_params *params,
+                               const dem_ext *ext, int64_t horizon_steps, int64_t *request_id) {
+    SERVER_GUARD(sv);
+    return submit(sv, scene, params, ext, horizon_steps, request_id, true);
 }
 
 int dem_server_advance(dem_server *sv, int32_t n_steps) {
@@ -419,6 +445,8 @@ int dem_server_get_stats(dem_server *sv, dem_server_stats *out) {
     out->used_particles = sv->world.a_part.used();
     out->device_bytes = (int64_t)(sv->world.a_part.capacity() * sv->world.bytes_per_particle());
     out->steps = sv->world.host_step;
+    out->waits_active = sv->waits_active;
+    out->waits_memory = sv->waits_memory;
     return DEM_OK;
 }
 

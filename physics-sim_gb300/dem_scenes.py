@@ -155,7 +155,11 @@ def c3_mix_scene(n, bond_fraction, seed):
             pos[b0:b0 + chain_len, 0] = x0 + 2.0 * np.arange(chain_len)
             pos[b0:b0 + chain_len, 1] = y
             starts.append(b0)
-        H = max(H, 2.0 * (pos[:, 1].max() + 2.0))
+        # a taller box for the chains: everything moves down with the floor,
+        # so the loose lattice still starts 1.4 above it and lands at once
+        H_new = max(H, 2.0 * (pos[:, 1].max() + 2.0))
+        pos[:, 1] -= (H_new - H) / 2.0
+        H = H_new
     sc = empty_scene(n, [1, 1, 1, 1.0, 1e5, 5e4])
     sc["pos"] = pos.astype(np.float32).reshape(-1)
     sc["radii"] = radii
@@ -175,13 +179,16 @@ def c3_mix_scene(n, bond_fraction, seed):
     return sc, p, ext
 
 
-def c3_batch(n_scenes=512, seed=0, n_min=1000, n_max=64000):
+def c3_batch(n_scenes=512, seed=0, n_min=1000, n_max=64000, indices=None):
     """The batched mix: n_scenes scenes with log-uniform particle counts in
-    [n_min, n_max] and bond fractions uniform in [0, 0.5], each seeded."""
+    [n_min, n_max] and bond fractions uniform in [0, 0.5], each seeded.
+    `indices` builds only those scenes of the mix (the same scenes the whole
+    mix holds at those positions)."""
     rng = np.random.default_rng(seed)
     ns = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_scenes)).astype(int)
     fr = rng.uniform(0.0, 0.5, n_scenes)
-    return [c3_mix_scene(int(n), float(f), seed * 100003 + k) for k, (n, f) in enumerate(zip(ns, fr))]
+    ks = range(n_scenes) if indices is None else indices
+    return [c3_mix_scene(int(ns[k]), float(fr[k]), seed * 100003 + k) for k in ks]
 
 
 def add_chain_bonds(scene, chains):

@@ -26,7 +26,11 @@ def _ev(ev):
     return sorted((int(e["step"]), int(e["bond"]), int(e["code"]), int(e["a"]), int(e["b"])) for e in ev)
 
 
-def test_each_result_equals_the_scene_alone():
+@pytest.mark.parametrize("borrow", [False, True])
+def test_each_result_equals_the_scene_alone(borrow):
+    """Requests admitted while others run equal each scene run alone, whether
+    the server copies each request's scene at submit or refers to the
+    caller's arrays until the request is done (dem_server_submit_borrowed)."""
     reqs = [
         (dem_scenes.c3_mix_scene(1500, 0.3, 11), 100),
         (dem_scenes.dense_bed(900, seed=12), 70),
@@ -40,14 +44,14 @@ def test_each_result_equals_the_scene_alone():
         # two requests up front, the others arrive while those run
         for k in (0, 1):
             (sc, p, ext), h = reqs[k]
-            ids[sv.submit(sc, p, h, **ext)] = k
+            ids[sv.submit(sc, p, h, borrow=borrow, **ext)] = k
         sv.advance(35)
         (sc, p, ext), h = reqs[2]
-        ids[sv.submit(sc, p, h, **ext)] = 2
+        ids[sv.submit(sc, p, h, borrow=borrow, **ext)] = 2
         sv.advance(35)
         for k in (3, 4):
             (sc, p, ext), h = reqs[k]
-            ids[sv.submit(sc, p, h, **ext)] = k
+            ids[sv.submit(sc, p, h, borrow=borrow, **ext)] = k
         done = {}
         for _ in range(40):
             sv.advance(35)
