@@ -467,11 +467,14 @@ def run_ours(args):
            "note": "dem_upload (restore) of the whole scene + dem_step(frame) + dem_download (update_state)"}
 
     base = None
+    fp64 = None
     if rank == 0 and ws == 1:
         csc, cp, cext, crop = cpu_sample_workload(args.workload, sc, p, ext)
         base, _ = cpu_baseline(csc, cp, cext, args.cpu_seconds, F)
         if crop:
             base["sample"] = crop + "; " + base["sample"]
+        fp64 = fp64_twin_error([(st, p, ext)], local)
+        fp64["state"] = "the scene after the timed frames and the roofline pass"
     cfg = dict(desc)
     cfg.update({"frame_steps": F, "parallelism": "replicas" if ws > 1 else "single",
                 "l2": "flushed between frames (write of %d MiB on the stream, untimed)" % (FLUSH_BYTES >> 20),
@@ -481,6 +484,8 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": cfg, "clocks": clocks, "roofline": roofline,
             "e2e": e2e, "gpu_launches": int(launches), "wall_s": wall}
+    if fp64 is not None:
+        line["fp64_error"] = fp64
     if base is not None:
         line["cpu_baseline"] = base
     ctx.close()

@@ -418,10 +418,13 @@ def test_set_properties_matches_oracle():
 
 def test_fp64_twin_error_is_reported():
     """Per-particle FP32 accelerations of one step against the FP64 twin of the
-    same step, scaled by the particle's force magnitude (sum |F_n| + m g).  The
-    figure is reported; the bound only guards against gross errors, since FP32
-    positions of magnitude ~30 already carry ~2e-6 absolute rounding, i.e.
-    ~1e-3 of a 1e-3 overlap."""
+    same step, scaled by the particle's force magnitude (sum |F_n| + m g).
+    Against the reference's own FP32 arithmetic the path is exact (every
+    other parity test); against FP64 it carries FP32's rounding.  Bounds, on
+    a packed bed in contact: median 1e-5 (the workload definition's
+    tolerance), 99th percentile 1e-3 and maximum 1e-2 -- FP32 positions of
+    magnitude ~30 carry ~2e-6 absolute rounding, so the overlap of a
+    near-grazing contact (~1e-3) is only known to ~1e-3 relative."""
     sc, p, ext = dem_scenes.dense_bed(n=1500, seed=9)
     with dem.Context(sc, p) as ctx:
         ctx.step(30)
@@ -436,9 +439,11 @@ def test_fp64_twin_error_is_reported():
     f_abs = np.abs(s31["data"].reshape(-1, 7)[:, 0]).astype(np.float64)
     scale = (f_abs + mass * 9.81) / mass
     err = np.linalg.norm(a32 - a64, axis=1) / scale
-    print("fp32 vs fp64 one-step acceleration error: max %.3g median %.3g" % (err.max(), np.median(err)))
-    assert np.median(err) < 1e-4
-    assert err.max() < 5e-2
+    print("fp32 vs fp64 one-step acceleration error: max %.3g p99 %.3g median %.3g"
+          % (err.max(), np.percentile(err, 99), np.median(err)))
+    assert np.median(err) < 1e-5
+    assert np.percentile(err, 99) < 1e-3
+    assert err.max() < 1e-2
 
 
 def test_zero_radius_and_empty_slots_edge_cases():
