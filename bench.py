@@ -7,7 +7,12 @@ gen_per_frame steps, src/wgpu_prog.rs:1420-1473; the reference default is
 simulation steps / device time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c3_batch|c4_serve|c1_chains|c0_settle|dense_bed] [--frame F]
+                  [--workload c3_batch|c4_serve|c1_chains|c0_settle|c2_impact|dense_bed] [--frame F]
+
+  python bench.py --profile-steps K [--workload ...] [knobs] -- a profiling
+  target, not a bench: K steps of the workload with plain kernel launches
+  (profilers cannot see kernels inside graphs with conditional nodes) and
+  the given knobs, then exit; nothing is timed.
 
 --impl reference times the reference's algorithm on the host cores: the CPU
 restatement under oracle/ (the reference's own WGSL-through-wgpu step cannot
@@ -63,13 +68,24 @@ def parse_args():
     ap.add_argument("--serve-active", type=int, default=16 << 20)
     ap.add_argument("--serve-timeout", type=float, default=900.0)
     ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuner's picks")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="profiling target: run this many steps with plain launches and exit (nothing timed)")
+    ap.add_argument("--particles", type=int, default=0, help="dense_bed: particles")
+    ap.add_argument("--c2-cols", type=int, default=1024, help="c2_impact: lattice columns (a crop when < 1024)")
+    ap.add_argument("--c2-rows", type=int, default=4096, help="c2_impact: lattice rows (a crop when < 4096)")
+    ap.add_argument("--cell-factor", type=float, default=0.0, help="--profile-steps: search_cell_factor")
+    ap.add_argument("--skin", type=float, default=0.0, help="--profile-steps: list_skin")
+    ap.add_argument("--block", type=int, default=0, help="--profile-steps: block_size")
+    ap.add_argument("--graph-steps", type=int, default=35, help="--profile-steps: reorder_interval")
+    ap.add_argument("--split", action="store_true", help="--profile-steps: k_narrow + k_forces")
+    ap.add_argument("--unfused", action="store_true", help="--profile-steps: a LOM kernel every step")
     ap.add_argument("--plain", action="store_true",
                     help="plain kernel launches instead of CUDA graphs, so that ncu can list every "
                          "launch (a profiling aid, not a bench configuration)")
     return ap.parse_args()
 
 
-def build_workload(name):
+def build_workload(name, args=None):
     import dem_scenes
     if name == "c1_chains":
         sc, p, ext = dem_scenes.c1_chains()
@@ -80,14 +96,17 @@ def build_workload(name):
         sc, p, ext = dem_scenes.c0_settle()
         desc = {"workload": "c0 granular settle", "particles": 4096, "box": [128, 256], "dt": 1e-4}
     elif name == "dense_bed":
-        n = 1 << 20
+        n = (args.particles if args is not None and args.particles > 0 else 0) or (1 << 20)
         sc, p, ext = dem_scenes.dense_bed(n=n)
         desc = {"workload": "dense bed (c0 particle model, packed)", "particles": n, "dt": 1e-4}
     elif name == "c2_impact":
-        sc, p, ext = dem_scenes.c2_impact()
+        cols, rows = (args.c2_cols, args.c2_rows) if args is not None else (1024, 4096)
+        sc, p, ext = dem_scenes.c2_impact(cols=cols, rows=rows)
         nb = int(sc["bonds"].shape[0] // 3)
-        desc = {"workload": "c2 single large impact scene", "particles": int(sc["radii"].shape[0]),
-                "bed": [2048, 8192], "lattice": "1024 x 4096, pitch 2", "radii": "log-normal, median 1, sigma 0.15",
+        desc = {"workload": "c2 single large impact scene" + ("" if (cols, rows) == (1024, 4096) else " (crop)"),
+                "particles": int(sc["radii"].shape[0]),
+                "bed": [2 * cols, 2 * rows], "lattice": "%d x %d, pitch 2" % (cols, rows),
+                "radii": "log-normal, median 1, sigma 0.15",
                 "bonded_fraction": 0.3, "clusters": "horizontal runs of 4-32", "bonds": nb,
                 "bond_model": "parallel (bonds=3), factor 0.8, Weibull(8, 5e3) strengths",
                 "projectile": {"radius": 40, "speed": 50}, "dt": 5e-5}
@@ -312,7 +331,7 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    sc, p, ext, desc = build_workload(args.workload)
+    sc, p, ext, desc = build_workload(args.workload, args)
     sc, p, ext, crop = cpu_sample_workload(args.workload, sc, p, ext)
     if crop:
         desc = dict(desc)
@@ -371,7 +390,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    sc, p, ext, desc = build_workload(args.workload)
+    sc, p, ext, desc = build_workload(args.workload, args)
     n = int(sc["radii"].shape[0])
     F = args.frame
     # autotuner (cell size, skin, block size, steps per graph, one or two
@@ -923,8 +942,35 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_target(args):
+    """K steps of the workload with plain launches and the given knobs (the
+    target of an ncu capture); prints the stats and exits."""
+    import build_lib
+    import dem
+    build_lib.build()
+    knobs = {"split_narrow": int(args.split), "unfused_lom": int(args.unfused),
+             "search_cell_factor": args.cell_factor, "list_skin": args.skin, "block_size": args.block,
+             "reorder_interval": args.graph_steps, "plain_launches": True}
+    if args.workload == "c3_batch":
+        items, _ = build_batch_workload(args.scenes, args.seed)
+        with dem.Batch(items, **knobs) as b:
+            b.step(args.profile_steps)
+            b.synchronize()
+            print("ok", len(items), "scenes", args.profile_steps, "steps", b.stats(), flush=True)
+        return
+    sc, p, ext, desc = build_workload(args.workload, args)
+    with dem.Context(sc, p, **knobs, **ext) as ctx:
+        ctx.step(args.profile_steps)
+        ctx.synchronize()
+        print("ok", desc["workload"], desc["particles"], "particles", args.profile_steps, "steps", ctx.stats(),
+              flush=True)
+
+
 def main():
     args = parse_args()
+    if args.profile_steps > 0:
+        run_profile_target(args)
+        return
     if args.workload == "c4_serve":
         run_serve(args)
         return

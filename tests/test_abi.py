@@ -10,7 +10,7 @@ import pytest
 
 import dem
 import dem_scenes
-import fbs_state
+import state_io
 import oracle
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -62,8 +62,8 @@ def test_struct_layouts(L):
 
 @pytest.mark.parametrize("fixture", ["TEXPS.bin", "Chain_TEXP.bin", "PBEXPS.bin", "Strings.bin"])
 def test_grid_capacity_matches_reference_formula(L, golden_dir, fixture):
-    raw = fbs_state.parse(open(os.path.join(golden_dir, fixture), "rb").read())
-    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, fixture))
+    raw = state_io.parse(open(os.path.join(golden_dir, fixture), "rb").read())
+    scene, uni, info = state_io.load_state(os.path.join(golden_dir, fixture))
     got = dem.grid_capacity(uni, raw["radii"], info["particles"])
     assert got[0] == pytest.approx(scene["grid"][0], rel=0, abs=0)
     assert got[1:] == tuple(scene["grid"][1:])

@@ -13,7 +13,7 @@ import pytest
 
 import dem
 import dem_scenes
-import fbs_state
+import state_io
 import oracle
 import replay
 from gpu_backend import GpuBackend, assert_same_state, contact_pairs, copy_scene, run_both
@@ -28,7 +28,7 @@ def _built():
 
 
 def test_texps_replay_equals_oracle_and_golden(golden_dir):
-    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "TEXPS.bin"))
+    scene, uni, info = state_io.load_state(os.path.join(golden_dir, "TEXPS.bin"))
     gb = GpuBackend(scene, uni, info["use_f64"])
     gx = replay.Replayer(gb, info["scripts"], len(scene["radii"])).run()
     ob = replay.OracleBackend(scene, uni, info["use_f64"])
@@ -49,7 +49,7 @@ def test_record_path_reproduces_the_texp_exports(golden_dir, tmp_path):
     same numbers."""
     import record
     from gpu_backend import RecordingGpuBackend
-    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "TEXPS.bin"))
+    scene, uni, info = state_io.load_state(os.path.join(golden_dir, "TEXPS.bin"))
     n = len(scene["radii"])
     gx = replay.Replayer(GpuBackend(scene, uni, info["use_f64"]), info["scripts"], n).run()
     rx = replay.Replayer(RecordingGpuBackend(scene, uni, info["use_f64"]), info["scripts"], n).run()
@@ -66,7 +66,7 @@ def test_record_path_reproduces_the_texp_exports(golden_dir, tmp_path):
 
 
 def test_chain_texp_replay_equals_oracle(golden_dir):
-    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "Chain_TEXP.bin"))
+    scene, uni, info = state_io.load_state(os.path.join(golden_dir, "Chain_TEXP.bin"))
     gx = replay.Replayer(GpuBackend(scene, uni, info["use_f64"]), info["scripts"], 3).run()
     ox = replay.Replayer(replay.OracleBackend(scene, uni, info["use_f64"]), info["scripts"], 3).run()
     for k in ox:
@@ -219,7 +219,7 @@ def test_setting_variants_bit_exact(variant):
 
 
 def test_strings_scene_bit_exact(golden_dir):
-    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "Strings.bin"))
+    scene, uni, info = state_io.load_state(os.path.join(golden_dir, "Strings.bin"))
     g, o, gev, oev = run_both(scene, uni, 300, chunk=60, use_f64=info["use_f64"])
     assert_same_state(g, o)
     assert len(gev) == len(oev)
@@ -229,7 +229,7 @@ def test_nan_velocity_and_broken_bonds_scene_bit_exact(golden_dir):
     """The reference's MicroStrings state: 2048 particles in strings, 4193
     bonds already broken (code -9) and one NaN velocity; NaN compares equal
     to NaN, every other bit must match."""
-    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "MicroStrings.bin"))
+    scene, uni, info = state_io.load_state(os.path.join(golden_dir, "MicroStrings.bin"))
     assert np.isnan(scene["vel"]).any()
     g, o, gev, oev = run_both(scene, uni, 200, chunk=50, use_f64=info["use_f64"])
     assert_same_state(g, o)
@@ -377,7 +377,7 @@ def test_broad_phase_keys_and_order():
 
 
 def test_upload_download_roundtrip(golden_dir):
-    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, "Strings.bin"))
+    scene, uni, info = state_io.load_state(os.path.join(golden_dir, "Strings.bin"))
     with dem.Context(scene, uni, use_f64=info["use_f64"]) as ctx:
         d = ctx.download()
         for k in ("pos", "radii", "vel", "acc", "rot", "rot_vel", "rot_acc", "forces", "fixity",

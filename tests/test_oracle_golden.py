@@ -13,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-import fbs_state
+import state_io
 import replay
 
 TRACES = np.load(os.path.join(os.path.dirname(__file__), "golden", "traces.npz"))
@@ -25,7 +25,7 @@ RTOL = 2e-3
 
 
 def _run(fixture, golden_dir, long_wait_frames=1):
-    scene, uni, info = fbs_state.load_state(os.path.join(golden_dir, fixture))
+    scene, uni, info = state_io.load_state(os.path.join(golden_dir, fixture))
     be = replay.OracleBackend(scene, uni, info["use_f64"])
     r = replay.Replayer(be, info["scripts"], len(scene["radii"]), long_wait_frames)
     return r.run(), be
