@@ -78,6 +78,8 @@ def parse_args():
     ap.add_argument("--block", type=int, default=0, help="--profile-steps: block_size")
     ap.add_argument("--graph-steps", type=int, default=35, help="--profile-steps: reorder_interval")
     ap.add_argument("--split", action="store_true", help="--profile-steps: k_narrow + k_forces")
+    ap.add_argument("--reorder-every", type=int, default=0,
+                    help="rebuilds per reorder into cell order (dem_ext.reorder_every; 0: library default)")
     ap.add_argument("--unfused", action="store_true", help="--profile-steps: a LOM kernel every step")
     ap.add_argument("--plain", action="store_true",
                     help="plain kernel launches instead of CUDA graphs, so that ncu can list every "
@@ -400,6 +402,8 @@ def run_ours(args):
         knobs, tune_info = dem.autotune([(sc, p, ext)], device=local)
     g = knobs["reorder_interval"]
     F = args.frame if args.frame_given else g * max(1, -(-105 // g))
+    if args.reorder_every > 0:
+        knobs = dict(knobs, reorder_every=args.reorder_every)
     ctx = dem.Context(sc, p, device=local, plain_launches=args.plain, **knobs, **ext)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
@@ -596,6 +600,8 @@ def run_ours_batch(args):
         F = args.frame
     else:
         F = g * max(1, -(-args.horizon // (args.steps * g)))
+    if args.reorder_every > 0:
+        knobs = dict(knobs, reorder_every=args.reorder_every)
     batch = dem.Batch(items, device=local, plain_launches=args.plain, **knobs)
     stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
@@ -950,7 +956,7 @@ def run_profile_target(args):
     build_lib.build()
     knobs = {"split_narrow": int(args.split), "unfused_lom": int(args.unfused),
              "search_cell_factor": args.cell_factor, "list_skin": args.skin, "block_size": args.block,
-             "reorder_interval": args.graph_steps, "plain_launches": True}
+             "reorder_interval": args.graph_steps, "plain_launches": True, "reorder_every": args.reorder_every}
     if args.workload == "c3_batch":
         items, _ = build_batch_workload(args.scenes, args.seed)
         with dem.Batch(items, **knobs) as b:

@@ -115,7 +115,13 @@ typedef struct dem_ext {
                                          lists; the reorder only restores memory locality, which particles
                                          lose slowly (they move a skin between rebuilds, a cell takes
                                          many); results do not depend on it */
-    int32_t reserved;
+    float restitution;                /* particle-particle normal dashpot (an extension: the reference's
+                                         contacts are springs only; its one restitution is the walls' 0.5,
+                                         2D_LOM.wgsl:110-126).  0 = off, the reference's arithmetic; e in
+                                         (0, 1]: linear_model's normal force gains -c v_n with damping
+                                         ratio zeta = -ln e / sqrt(pi^2 + ln^2 e), c = 2 zeta sqrt(k_n
+                                         m_eff), v_n the normal approach speed of the step's displacements,
+                                         and the sum is kept >= 0 (no pull between touching disks) */
 } dem_ext;
 
 /* One scene in the reference's host layouts (state.rs:69-93).  Arrays hold

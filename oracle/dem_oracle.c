@@ -27,6 +27,15 @@ static inline int32_t orc_i32(float x) {
 static inline float orc_len_f32(float x, float y) { return sqrtf(x * x + y * y); }
 static inline double orc_len_f64(double x, double y) { return sqrt(x * x + y * y); }
 
+/* 2 zeta of the normal dashpot for restitution e (0: off, and e >= 1 is no
+ * damping): zeta = -ln e / sqrt(pi^2 + ln^2 e) in double; the reference-mode
+ * step rounds it to float once, the twin keeps the double */
+static inline double orc_dashpot_2zeta(float e) {
+    if (!(e > 0.0f) || e >= 1.0f) return 0.0;
+    const double l = log((double)e);
+    return 2.0 * (-l / sqrt(ORC_PI * ORC_PI + l * l));
+}
+
 /* ---- reference-mode instantiation (float) ---- */
 #define REAL float
 #define REAL_IS_FLOAT 1

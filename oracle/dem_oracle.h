@@ -77,6 +77,8 @@ typedef struct orc_ext {
     float bond_lambda;      /* parallel-bond radius factor, reference 0.5 (2D_Simulation.wgsl:290) */
     const float *bond_sn;   /* optional per-bond normal strength [n_bonds], NULL = global */
     const float *bond_ss;   /* optional per-bond shear strength [n_bonds], NULL = global */
+    float restitution;      /* particle-particle normal dashpot, an extension (0 = off, the
+                               reference's springs only); same definition as dem_ext.restitution */
 } orc_ext;
 
 typedef struct orc_state {

@@ -52,7 +52,8 @@ class Settings(C.Structure):
 
 class Ext(C.Structure):
     _fields_ = [("use_f64", C.c_int32), ("bond_lambda", C.c_float),
-                ("bond_sn", C.POINTER(C.c_float)), ("bond_ss", C.POINTER(C.c_float))]
+                ("bond_sn", C.POINTER(C.c_float)), ("bond_ss", C.POINTER(C.c_float)),
+                ("restitution", C.c_float)]
 
 
 _FP = C.POINTER(C.c_float)
@@ -155,10 +156,11 @@ def make_state(scene):
     return st
 
 
-def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, keep=None):
+def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, keep=None, restitution=0.0):
     e = Ext()
     e.use_f64 = 1 if use_f64 else 0
     e.bond_lambda = bond_lambda
+    e.restitution = restitution
     if bond_sn is not None:
         bond_sn = np.ascontiguousarray(bond_sn, dtype=np.float32)
         e.bond_sn = _ptr(bond_sn, _FP)
@@ -173,11 +175,13 @@ def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, keep=No
 
 
 def step(scene, settings, nsteps, *, use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None,
-         step_base=0, threads=0, ev_cap=1 << 16):
-    """Advance `scene` in place by nsteps; return (break events, stats[4])."""
+         step_base=0, threads=0, ev_cap=1 << 16, restitution=0.0):
+    """Advance `scene` in place by nsteps; return (break events, stats[4]).
+    restitution > 0 switches on the normal dashpot extension (not in the
+    reference)."""
     keep = []
     st = make_state(scene)
-    ext = make_ext(use_f64, bond_lambda, bond_sn, bond_ss, keep)
+    ext = make_ext(use_f64, bond_lambda, bond_sn, bond_ss, keep, restitution)
     s = make_settings(settings)
     ev = np.zeros(ev_cap, dtype=BREAK_DTYPE)
     nev = C.c_int(0)
@@ -192,11 +196,11 @@ def step(scene, settings, nsteps, *, use_f64=False, bond_lambda=0.5, bond_sn=Non
 
 
 def step_f64(scene, settings, nsteps=1, *, use_f64=False, bond_lambda=0.5, bond_sn=None,
-             bond_ss=None, threads=0):
+             bond_ss=None, threads=0, restitution=0.0):
     """FP64 twin: evolve a copy of `scene` in double; return a dict of float64 arrays."""
     keep = []
     st = make_state(scene)
-    ext = make_ext(use_f64, bond_lambda, bond_sn, bond_ss, keep)
+    ext = make_ext(use_f64, bond_lambda, bond_sn, bond_ss, keep, restitution)
     s = make_settings(settings)
     n = int(scene["radii"].shape[0])
     out = {"pos": np.zeros(2 * n), "vel": np.zeros(2 * n), "acc": np.zeros(2 * n),

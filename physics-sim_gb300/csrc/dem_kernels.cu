@@ -111,14 +111,20 @@ struct Acc3 {
 // with the same float operations
 // L = len2f(pa - pb), which the caller computes once per slot (every float
 // distance of the slot is this same value)
-// F64: the scene may use the F64 distance (read from its settings); false
-// compiles the FP32 form only
-template <bool F64>
+// GEN: the generic form -- the scene may use the F64 distance and the
+// normal dashpot (read from its parameters); false compiles the reference's
+// FP32 arithmetic only.
+// meff: m_a m_b / (m_a + m_b), read only by the dashpot.
+// The dashpot (an extension, off unless the scene asks for it): after the
+// normal direction is known, Fn -= c v_n with c = 2 zeta sqrt(kn meff) and
+// v_n = ((da - db) . n) / dT, the step's normal approach speed (negative
+// while closing), then Fn = max(Fn, 0).
+template <bool GEN>
 __device__ __forceinline__ F3 linear_model(const ScenePar &P, float2 kns, float4 pa,
                                            float4 da, float4 pb, float4 db, float length, float L, float &tf,
-                                           Acc3 &acc) {
+                                           Acc3 &acc, float meff) {
     F3 out = {0.0f, 0.0f, 0.0f};
-    float d2 = (F64 && P.use_f64) ? distance2(1, pa, pb, length) : L - length;
+    float d2 = (GEN && P.use_f64) ? distance2(1, pa, pb, length) : L - length;
     float nd = d2 < 0.0f ? d2 : 0.0f;
     if (nd == 0.0f) return out;
     float kn = kns.x;
@@ -126,6 +132,12 @@ __device__ __forceinline__ F3 linear_model(const ScenePar &P, float2 kns, float4
     float Fn = (-nd) * kn;
     float vx = pa.x - pb.x, vy = pa.y - pb.y;
     float nx = vx / L, ny = vy / L;
+    if (GEN && P.damp2 > 0.0f) {
+        const float c = P.damp2 * sqrtf(kn * meff);
+        const float vn = ((da.x - db.x) * nx + (da.y - db.y) * ny) / P.p.dT;
+        Fn = Fn - c * vn;
+        Fn = Fn > 0.0f ? Fn : 0.0f;
+    }
     float tx = -ny, ty = nx;
     float dra = da.z * pa.z;
     float drb = db.z * pb.z;
@@ -1202,13 +1214,20 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             mask &= ~(1u << (BSHIFT + j));
         }
         const float2 kns = __ldg(&w.pair[P.pair_base + (int)meta_mat(m) * P.n_mat + (int)meta_mat(mb)]);
+        float meff = 0.0f;  // effective mass of the pair, for the dashpot (generic form only)
+        if (MAY_F64 && P.damp2 > 0.0f) {
+            const float ma = ((w.mats[P.mat_base + meta_mat(m)].density * 3.14159274101257324219f) * pa.z) * pa.z;
+            const float mbb = ((w.mats[P.mat_base + meta_mat(mb)].density * 3.14159274101257324219f) * pb.z) * pb.z;
+            meff = (ma * mbb) / (ma + mbb);
+        }
         F3 f = {0.0f, 0.0f, 0.0f};
         // L = |pa - pb| in float, taken once per slot where the branch needs
         // it: every float distance of the slot is this value (b - a differs
         // from a - b only in sign, so the squares agree)
         if (bonded < 0 || bonds_model == 0) {
             float tf = tf0;
-            f = linear_model<MAY_F64>(P, kns, pa, da, pb, db, pa.z + pb.z, len2f(pa.x - pb.x, pa.y - pb.y), tf, acc);
+            f = linear_model<MAY_F64>(P, kns, pa, da, pb, db, pa.z + pb.z, len2f(pa.x - pb.x, pa.y - pb.y), tf, acc,
+                                     meff);
             w.s_tf[j * N + i] = tf;
         } else {
             const int bg = P.bond_base + bonded;
@@ -1258,7 +1277,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 acc.d1 = acc.d1 + btf;
                 acc.d2 = acc.d2 + M;
                 float tf = tf0;
-                const F3 lm = linear_model<MAY_F64>(P, kns, pa, da, pb, db, blen, L, tf, acc);
+                const F3 lm = linear_model<MAY_F64>(P, kns, pa, da, pb, db, blen, L, tf, acc, meff);
                 w.s_tf[j * N + i] = tf;
                 f.x = Fx + lm.x;
                 f.y = Fy + lm.y;
@@ -1280,7 +1299,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     fy = 0.0f;
                 }
                 float tf = tf0;
-                const F3 lm = linear_model<MAY_F64>(P, kns, pa, da, pb, db, blen, L, tf, acc);
+                const F3 lm = linear_model<MAY_F64>(P, kns, pa, da, pb, db, blen, L, tf, acc, meff);
                 w.s_tf[j * N + i] = tf;
                 f.x = lm.x + fx;
                 f.y = lm.y + fy;

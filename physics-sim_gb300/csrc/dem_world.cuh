@@ -90,6 +90,7 @@ struct ScenePar {
     int32_t big_base;      // first big-partner record of the scene
     int32_t n_big;         // large particles of the scene at the last layout
     float r_grid;          // largest radius the search cells are sized for
+    float damp2;           // normal dashpot: 2 zeta (0: off; dem_ext.restitution)
 };
 
 // Candidate list of particle i: 32 bytes, 16 int16 {count, b_1 - i, ..., b_15 - i}

@@ -823,6 +823,7 @@ void World::fill_par(SceneHost &h) {
     P.n_mat = h.n_mat;
     P.use_f64 = h.use_f64;
     P.lambda = h.lambda;
+    P.damp2 = h.damp2;
     P.has_strength = h.bond_sn.empty() ? 0 : 1;
     P.active = h.active ? 1 : 0;
     P.step0 = h.step0;
@@ -1120,6 +1121,8 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
         h.params = params[s];
         h.use_f64 = e.use_f64 ? 1 : 0;
         h.lambda = e.bond_lambda;
+        if (!(e.restitution >= 0.0f && e.restitution <= 1.0f)) return fail(DEM_E_INVALID, "restitution not in [0, 1]");
+        h.damp2 = dashpot_factor(e.restitution);
         h.cell_factor = ext.search_cell_factor > 0.0f ? ext.search_cell_factor : 1.0f;
         int rc = compute_layout(h, scenes[s]);
         if (rc) return rc;
@@ -1183,6 +1186,14 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
 // (they cost the FP32 scenes registers), and one bond model built in when
 // every scene uses it (served worlds, whose scenes come and go, do not
 // specialise on the model); a change recaptures the graphs
+// 2 zeta of the normal dashpot for restitution e (0: off; e = 1 gives 0,
+// no damping): zeta = -ln e / sqrt(pi^2 + ln^2 e), in double, rounded once
+float dashpot_factor(float e) {
+    if (!(e > 0.0f) || e >= 1.0f) return 0.0f;
+    const double l = std::log((double)e);
+    return (float)(2.0 * (-l / std::sqrt(M_PI * M_PI + l * l)));
+}
+
 void World::update_kernel_form() {
     unsigned models = 0u;
     bool f64 = false;
@@ -1190,7 +1201,7 @@ void World::update_kernel_form() {
         if ((int)s == free_slot) continue;
         const SceneHost &h = sh[s];
         models |= (h.params.bonds >= 0 && h.params.bonds <= 3) ? 1u << h.params.bonds : 0xFu;
-        f64 |= h.use_f64 != 0;
+        f64 |= h.use_f64 != 0 || h.damp2 > 0.0f;  // the generic kernels carry the F64 paths and the dashpot
     }
     int form = f64 ? -1 : -2;
     if (!f64 && free_slot < 0) form = models == 1u ? 0 : models == 8u ? 3 : -2;
@@ -1286,6 +1297,8 @@ int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e
     h.params = params;
     h.use_f64 = e.use_f64 ? 1 : 0;
     h.lambda = e.bond_lambda;
+    if (!(e.restitution >= 0.0f && e.restitution <= 1.0f)) return fail(DEM_E_INVALID, "restitution not in [0, 1]");
+    h.damp2 = dashpot_factor(e.restitution);
     h.cell_factor = 1.0f;
     int rc = compute_layout(h, sc);
     if (rc) return rc;

@@ -15,6 +15,9 @@
 
 namespace demgb {
 
+// 2 zeta of the normal dashpot for restitution e (dem_ext.restitution)
+float dashpot_factor(float e);
+
 // World limits: the kernels index particles, cells and bonds with 32-bit
 // ints, the slot rows as j * N + i (j < K), and a grid-stride loop's index
 // must not pass 2^31 on its last stride.
@@ -35,6 +38,7 @@ struct SceneHost {
     int big_cap = 0, big_base = 0;     // big-partner records owned by the scene
     int use_f64 = 0;
     float lambda = 0.5f;
+    float damp2 = 0.0f;            // dashpot: 2 zeta (0: off)
     float cell_factor = 1.0f;
     float skin = 0.0f;
     // control words (coll_cont) at step0

@@ -62,7 +62,7 @@ class Ext(C.Structure):
                 ("block_size", C.c_int32), ("search_cell_factor", C.c_float),
                 ("event_capacity", C.c_int32), ("list_skin", C.c_float),
                 ("plain_launches", C.c_int32), ("split_narrow", C.c_int32), ("unfused_lom", C.c_int32),
-                ("host_copies", C.c_int32), ("reorder_every", C.c_int32), ("reserved", C.c_int32)]
+                ("host_copies", C.c_int32), ("reorder_every", C.c_int32), ("restitution", C.c_float)]
 
 
 class Scene(C.Structure):
@@ -259,7 +259,7 @@ def make_params(d):
 def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnostics=True,
              reorder_interval=0, block_size=0, search_cell_factor=0.0, event_capacity=0,
              list_skin=0.0, plain_launches=False, split_narrow=0, unfused_lom=0, host_copies=0, reorder_every=0,
-             keep=None):
+             restitution=0.0, keep=None):
     e = Ext()
     lib().dem_ext_defaults(C.byref(e))
     e.use_f64 = 1 if use_f64 else 0
@@ -275,6 +275,7 @@ def make_ext(use_f64=False, bond_lambda=0.5, bond_sn=None, bond_ss=None, diagnos
     e.unfused_lom = 1 if unfused_lom else 0
     e.host_copies = 1 if host_copies else 0
     e.reorder_every = int(reorder_every)
+    e.restitution = float(restitution)
     for attr, arr in (("bond_normal_strength", bond_sn), ("bond_shear_strength", bond_ss)):
         if arr is not None:
             a = np.ascontiguousarray(arr, dtype=np.float32)

@@ -98,7 +98,7 @@ pub struct dem_ext {
     pub unfused_lom: i32,
     pub host_copies: i32,
     pub reorder_every: i32,
-    pub reserved: i32,
+    pub restitution: f32,
 }
 
 /// One scene in the reference's host layouts.

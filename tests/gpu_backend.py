@@ -75,7 +75,7 @@ def run_both(scene, params, steps, chunk=None, **ext):
     """Advance the same scene on the GPU and on the oracle; return both states
     and both break-event lists (oracle events as dem.BREAK_DTYPE-like tuples)."""
     o = copy_scene(scene)
-    okw = {k: ext[k] for k in ("use_f64",) if k in ext}
+    okw = {k: ext[k] for k in ("use_f64", "restitution") if k in ext}
     if "bond_lambda" in ext:
         okw["bond_lambda"] = ext["bond_lambda"]
     if "bond_sn" in ext:

@@ -256,3 +256,22 @@ def test_record_one_scene_of_a_batch_equals_the_scene_alone():
         ref = ctx.record(60, sel)
     assert none is None
     assert got.shape == (60, 10) and np.array_equal(got, ref)
+
+
+def test_dashpot_scene_in_a_batch_equals_the_oracle():
+    """A scene with the normal dashpot (restitution 0.5) batched with scenes
+    without it: the batch runs the generic kernels and each scene equals the
+    oracle with its own setting."""
+    a = dem_scenes.dense_bed(n=900, seed=23)
+    a = (a[0], a[1], dict(a[2], restitution=0.5))
+    b = dem_scenes.c3_mix_scene(1500, 0.3, 24)
+    c = dem_scenes.dense_bed(n=600, seed=25)
+    items = [a, b, c]
+    with dem.Batch(items) as bt:
+        bt.step(150)
+        got = [bt.download(k) for k in range(3)]
+    for k, (sc, p, ext) in enumerate(items):
+        o = copy_scene(sc)
+        okw = {kk: ext[kk] for kk in ("bond_lambda", "bond_sn", "bond_ss", "restitution") if kk in ext}
+        oracle.step(o, p, 150, **okw)
+        assert_same_state(got[k], o, "scene %d: " % k)

@@ -123,3 +123,41 @@ def test_linear_momentum_is_conserved(workload):
         assert np.abs(pk - p0).max() <= 1e-6 * total, k
     if workload == "bonds":
         assert breaks > 0
+
+
+def _head_on(restitution, steps=3000):
+    """Two equal disks closing at speed 2 (no gravity, walls far away):
+    the ratio of separating to closing speed after the contact."""
+    sc = dem_scenes.empty_scene(2, [1, 1, 1, 1.0, 1e5, 5e4])
+    sc["pos"][:] = [-1.1, 0.0, 1.1, 0.0]
+    sc["radii"][:] = 1.0
+    sc["vel"][:] = [1.0, 0.0, -1.0, 0.0]
+    p = dem_scenes.reference_defaults(2)
+    p.update({"hor_bound": 100.0, "vert_bound": 100.0, "gravity": 0, "planet_mode": 0, "dT": 1e-4,
+              "friction_coefficient": 0.5, "bonds": 0})
+    sc["grid"] = dem_scenes.grid_capacity(100.0, 100.0, sc["radii"], 2)
+    oracle.step(sc, p, steps, restitution=restitution)
+    v = sc["vel"].reshape(2, 2)
+    return float((v[1, 0] - v[0, 0]) / 2.0)
+
+
+def test_dashpot_extension_restitution():
+    """The normal dashpot (an extension; the reference's contacts are pure
+    springs): restitution 0 keeps the reference's elastic contact, and a
+    head-on collision of two disks comes out with about the requested
+    restitution (higher for strong damping, where the no-pull clamp cuts the
+    dashpot's tension off)."""
+    assert abs(_head_on(0.0) - 1.0) < 1e-4
+    assert 0.5 <= _head_on(0.5) <= 0.6
+    assert 0.79 <= _head_on(0.8) <= 0.83
+    assert abs(_head_on(0.95) - 0.95) < 0.01
+
+
+def test_dashpot_off_is_the_reference_arithmetic():
+    """restitution 0 gives the default step byte for byte."""
+    sc, p, ext = dem_scenes.dense_bed(n=400, seed=3)
+    a, b = copy_scene(sc), copy_scene(sc)
+    oracle.step(a, p, 60)
+    oracle.step(b, p, 60, restitution=0.0)
+    for k in ("pos", "vel", "acc", "data", "contacts"):
+        assert np.array_equal(a[k].view(np.int32), b[k].view(np.int32)), k
