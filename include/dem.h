@@ -111,7 +111,8 @@ typedef struct dem_ext {
                                          page tables (Grace), else through a page-locked block; 1: always
                                          through the page-locked block */
     int32_t reorder_every;            /* rebuilds per reorder of the particle arrays into cell order; 0 =
-                                         default 8.  Every rebuild sorts by cell and rebuilds the candidate
+                                         default: 3 in a single-scene context, 8 in batches and servers.
+                                         Every rebuild sorts by cell and rebuilds the candidate
                                          lists; the reorder only restores memory locality, which particles
                                          lose slowly (they move a skin between rebuilds, a cell takes
                                          many); results do not depend on it */

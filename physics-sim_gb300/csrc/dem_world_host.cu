@@ -512,7 +512,10 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
     w.kbuild = dalloc<uint32_t>(owned, N, ok);
     w.rebuild = dalloc<int32_t>(owned, 1, ok);
     w.reorder = dalloc<int32_t>(owned, 1, ok);
-    w.reorder_every = reorder_every;
+    // default: every 3rd rebuild in a single-scene world (a dense scene's
+    // warps gain from fresh grouping by contact count), every 8th in a
+    // batch or server (many sparse scenes: the reorder's bytes dominate)
+    w.reorder_every = reorder_every > 0 ? reorder_every : (S == 1 ? 3 : 8);
     w.tickets = dalloc<uint32_t>(owned, 2, ok);
     w.fix_ref = dalloc<int32_t>(owned, 6 * (size_t)N, ok);
     w.force_ref = dalloc<float>(owned, 6 * (size_t)N, ok);

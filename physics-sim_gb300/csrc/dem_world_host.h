@@ -113,7 +113,7 @@ class World {
     int block = 256;
     int graph_steps = 35;          // steps per captured CUDA graph
     float skin_factor = 0.2f;      // candidate-list skin / r_max
-    int reorder_every = 8;         // rebuilds per reorder into cell order
+    int reorder_every = 0;         // rebuilds per reorder into cell order (0: by world, see alloc)
     bool diagnostics = true;
     long long host_step = 0;
     std::vector<SceneHost> sh;
