@@ -722,13 +722,24 @@ def run_ours_batch(args):
         batch.download_many(down_tab)
     barrier()
     e2e_s = time.perf_counter() - t0
+    # one more cycle, each call waited for, for the breakdown (not in the value)
+    parts = {}
+    for name, fn in (("upload_ms", lambda: batch.upload_many(up_tab)), ("frame_ms", lambda: batch.step(F)),
+                     ("download_ms", lambda: batch.download_many(down_tab))):
+        barrier()
+        t1 = time.perf_counter()
+        fn()
+        barrier()
+        parts[name] = (time.perf_counter() - t1) * 1e3
     del outs, up_tab, down_tab
     e2e = {"value": job_rate(ntot * F * e2e_n, e2e_s * 1e3, ws, dev)[0], "unit": "particle-steps/s",
            "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": h2d,
+           "cycle_ms": e2e_s * 1e3 / e2e_n,
+           "breakdown_ms": parts,
            "note": "dem_batch_upload_many of all scenes + dem_batch_step(frame) + dem_batch_download_many of all "
                    "scenes, from and into the callers' host arrays (scene struct tables built once), from the "
-                   "states at the end of the horizon"}
+                   "states at the end of the horizon; breakdown_ms: one extra cycle with each call waited for"}
 
     # settled states: the mix run on (untimed) to --settle-steps, then frames timed there
     settled = None
