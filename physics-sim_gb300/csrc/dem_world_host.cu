@@ -853,11 +853,14 @@ int World::push_det() {
 }
 
 // the next step rebuilds the cell table, the particle order and the candidate lists
-// (and reorders the particle arrays into cell order: the layout changed)
-int World::force_rebuild() {
+// (reorder: and reorders the particle arrays into cell order -- after
+// uploads, which leave a scene's particles in scene-local order; an admitted
+// or retired scene, moved walls or positions set from outside only need new
+// cell lists, and the regular reorder interval restores the order later)
+int World::force_rebuild(bool reorder) {
     static const int32_t one = 1;
     CK(cudaMemcpyAsync(d.rebuild, &one, 4, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.reorder, &one, 4, cudaMemcpyHostToDevice, stream));
+    if (reorder) CK(cudaMemcpyAsync(d.reorder, &one, 4, cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
     return DEM_OK;
 }
@@ -1358,7 +1361,7 @@ int World::admit(const dem_scene *sc, const dem_params &params, const dem_ext &e
     if (rc == DEM_OK) rc = push_det();
     if (rc == DEM_OK) rc = update_live();
     if (rc == DEM_OK) update_kernel_form();
-    if (rc == DEM_OK) rc = force_rebuild();
+    if (rc == DEM_OK) rc = force_rebuild(false);
     if (rc != DEM_OK) {
         retire(s);
         return rc;
@@ -1390,7 +1393,7 @@ int World::retire(int s) {
     rc = update_live();
     if (rc) return rc;
     update_kernel_form();
-    return force_rebuild();
+    return force_rebuild(false);
 }
 
 // A re-uploaded scene keeps its cell budget and large-particle records and
@@ -1497,7 +1500,7 @@ int World::set_params(int s, const dem_params &p) {
     update_kernel_form();
     // walls moved: the search grid keeps its allocation (it clamps particles
     // to its extent) and the cell lists are rebuilt before the next step
-    return geometry ? force_rebuild() : DEM_OK;
+    return geometry ? force_rebuild(false) : DEM_OK;
 }
 
 int World::set_materials(int s, const float *m, int n) {
@@ -2044,7 +2047,7 @@ int World::set_properties(int s, int32_t *selections, const int32_t *props) {
     if (e != cudaSuccess || e2 != cudaSuccess) return fail(DEM_E_CUDA, "set_properties failed");
     for (int i = 0; i < n; ++i)
         if (selections[i] != 0 && props[9] == 1) h.r_max = std::max(h.r_max, f[23]);
-    if (any && (props[0] == 1 || props[1] == 1 || props[9] == 1)) return force_rebuild();
+    if (any && (props[0] == 1 || props[1] == 1 || props[9] == 1)) return force_rebuild(false);
     return DEM_OK;
 }
 
@@ -2245,7 +2248,7 @@ int World::broad_phase_snapshot(int s, int32_t *keys, int32_t *order, int32_t *c
         cell_start[grid_cells + 1] = cs[h.n_cells] - first;
     }
     // the cell table now describes the current positions, not the last rebuild
-    return force_rebuild();
+    return force_rebuild(false);
 }
 
 int World::stats(dem_stats *out) {

@@ -154,7 +154,7 @@ class World {
     int update_live();
     int stage_many(const int32_t *idx, const dem_scene *const *scs, int count, const SceneHost *probes,
                    const std::function<int()> &layouts);
-    int force_rebuild();
+    int force_rebuild(bool reorder = true);
     void enqueue_plain_step(bool first, bool last, bool next_last);
     void enqueue_rebuild(cudaStream_t st, const int32_t *gate, bool every_step);
     int capture_graph(int R, cudaGraphExec_t *out, int *kernels);
