@@ -334,7 +334,8 @@ const char *dem_tune_last_error(void);
  * of both particles.  pos[2n] and radii[n] are host arrays; writes
  * bonds[3 * nb] {status 1, angle bits, length bits} (nb <= bonds_cap, else
  * DEM_E_CAPACITY with *n_bonds = nb so the caller can size the array) and
- * contacts[84 n] exactly as regen_bonds does.  max_bonds in [1, 14]. */
+ * contacts[84 n] exactly as regen_bonds does.  max_bonds in [1, 14]; n at
+ * most 2^26 (DEM_E_CAPACITY beyond). */
 int dem_generate_bonds(const float *pos, const float *radii, int32_t n, int32_t max_bonds, int32_t device,
                        int32_t *bonds, int64_t bonds_cap, int64_t *n_bonds, int32_t *contacts);
 const char *dem_bondgen_last_error(void);

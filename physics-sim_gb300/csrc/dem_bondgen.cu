@@ -200,6 +200,9 @@ int dem_generate_bonds(const float *pos, const float *radii, int32_t n, int32_t 
                        int32_t *bonds, int64_t bonds_cap, int64_t *n_bonds, int32_t *contacts) {
     g_bondgen_error.clear();
     if (n < 0 || !n_bonds) return bfail(DEM_E_INVALID, "n < 0 or n_bonds is NULL");
+    // at most 14 bonds a particle: bond numbers (and the incoming-bond sort's
+    // sequence) stay below 2^30
+    if (n > (1 << 26)) return bfail(DEM_E_CAPACITY, "n is above 2^26 particles");
     if (max_bonds < 1 || max_bonds > MAXB) return bfail(DEM_E_INVALID, "max_bonds must be in [1, 14]");
     if (n > 0 && (!pos || !radii || !contacts)) return bfail(DEM_E_INVALID, "a required array is NULL");
     *n_bonds = 0;
