@@ -18,6 +18,8 @@ reference at run time.  Outputs:
                Rotation Velocity, Data1..Data4, FPS
   TEXP_1_head.csv  the first 12 lines of data/TEXP_1.csv as text: the
                reference's own CSV formatting of those numbers
+  Default.bin  byte copy of the Default.bin at the root of the reference
+               checkout, a state in neither of its schemas
 """
 import glob
 import os
@@ -48,6 +50,7 @@ def main():
             rows = np.loadtxt(path, delimiter=",", skiprows=1, dtype=np.float64, ndmin=2)
             traces[key] = rows
     np.savez_compressed(os.path.join(HERE, "traces.npz"), **traces)
+    shutil.copyfile(os.path.join(REFERENCE, "Default.bin"), os.path.join(HERE, "Default.bin"))
     with open(os.path.join(src_data, "TEXP_1.csv")) as f:
         head = [next(f) for _ in range(12)]
     with open(os.path.join(HERE, "TEXP_1_head.csv"), "w") as f:

@@ -23,7 +23,11 @@ def _same_scene(a, b):
             assert x.dtype == y.dtype and x.shape == y.shape and x.tobytes() == y.tobytes(), k
 
 
-@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.bin"))), ids=os.path.basename)
+# the experiment states (Default.bin is in neither schema: its own test below)
+EXPERIMENT_STATES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.bin")) if not p.endswith("Default.bin"))
+
+
+@pytest.mark.parametrize("path", EXPERIMENT_STATES, ids=os.path.basename)
 def test_golden_states_round_trip_through_the_writer(path):
     sc, uni, info = state_io.load_state(path)
     out = state_io.save_state(sc, uni, info)
@@ -149,3 +153,41 @@ def test_random_scenes_round_trip_bit_for_bit():
             assert x.dtype == y.dtype and x.shape == y.shape and x.tobytes() == y.tobytes(), k
 
     check()
+
+
+def _root_vectors(buf):
+    """Field count of a FlatBuffers root table and, per field, the length
+    word of the vector it points to (None for an absent field)."""
+    import struct
+    root = struct.unpack_from("<I", buf, 0)[0]
+    vt = root - struct.unpack_from("<i", buf, root)[0]
+    vlen = struct.unpack_from("<H", buf, vt)[0]
+    out = []
+    for k in range((vlen - 4) // 2):
+        o = struct.unpack_from("<H", buf, vt + 4 + 2 * k)[0]
+        if o == 0:
+            out.append(None)
+            continue
+        tgt = root + o + struct.unpack_from("<I", buf, root + o)[0]
+        out.append(struct.unpack_from("<I", buf, tgt)[0] if tgt + 4 <= len(buf) else None)
+    return out
+
+
+def test_default_bin_is_in_neither_schema_and_is_refused(golden_dir):
+    """The Default.bin at the root of the reference checkout is not the scene
+    the reference starts with: its code reads saved states only from files
+    the user or a script picks (State::load_from_file from client.rs:917 and
+    1151).  It follows neither schema in the reference: a 256-particle state
+    whose root table holds 15 fields in an order of neither State table, with
+    a contact vector of 14,336 words -- 4 words a record, where both schemas
+    store 6 (contacts = 14 records x 6 words a particle).  The reader refuses
+    it instead of misreading it."""
+    buf = open(os.path.join(golden_dir, "Default.bin"), "rb").read()
+    lens = _root_vectors(buf)
+    assert len(lens) == 15
+    assert 14336 in lens and 256 * 14 * 4 == 14336 and 256 * 14 * 6 not in lens
+    with pytest.raises(ValueError):
+        state_io.load_state(os.path.join(golden_dir, "Default.bin"))
+    for name in ("TEXPS.bin", "Strings.bin"):   # the experiment states: 6 words a record
+        s, _, _ = state_io.load_state(os.path.join(golden_dir, name))
+        assert s["contacts"].size == 14 * 6 * s["radii"].size
