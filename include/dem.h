@@ -167,7 +167,11 @@ typedef struct dem_stats {
     int64_t events;             /* bond breaks recorded */
     int64_t events_dropped;     /* breaks beyond the event ring */
     int64_t reorders;           /* rebuilds (cell sort, reorder by cell, candidate lists) */
-    int32_t device_error;       /* sticky device error bits, 0 = none */
+    int32_t device_error;       /* sticky device error bits, 0 = none: 1 breaks of one step beyond the
+                                   pending-break capacity; 2 a touching pair whose first shared bucket
+                                   ranks beyond 15 in the scan order, or an AABB 31 or more buckets
+                                   wide (the bucket grid is much finer than the particles); 4 a large
+                                   particle touching more than 2048 particles at once */
     int32_t reserved;
     int64_t kernel_launches;    /* kernels this library launched on the context's stream */
     int64_t list_overflows;     /* particles whose candidates exceeded the list (searched the cells) */

@@ -44,21 +44,47 @@ __device__ __forceinline__ void ref_range(const ScenePar &P, float px, float py,
     y1 = d < P.ref_h - 1 ? d : P.ref_h - 1;
 }
 
-// The range packed in 16-bit fields: an empty side (x0 beyond the grid or x1
-// below it) is stored as w (resp. -1), which intersects no range exactly as
-// the unclamped value does.  Grids are limited to 32766 buckets per side.
-__device__ __forceinline__ int2 pack_range(const ScenePar &P, int x0, int x1, int y0, int y1) {
-    x0 = x0 < P.ref_w ? x0 : P.ref_w;
-    y0 = y0 < P.ref_h ? y0 : P.ref_h;
-    x1 = x1 >= 0 ? x1 : -1;
-    y1 = y1 >= 0 ? y1 : -1;
-    return make_int2((x0 & 0xFFFF) | (x1 << 16), (y0 & 0xFFFF) | (y1 << 16));
+// The range as one 32-bit code, kept in the w word of the particle's
+// position record: the first column and row modulo 2048 (11 bits each), then
+// the width and the height in buckets (5 bits each: 0 for an empty side, as
+// for a particle off the grid; 31 for 31 or more).  Ranges are compared only
+// for pairs that touch, and those ranges overlap or abut: the AABBs overlap,
+// the roundings of their edges and the truncation to buckets are monotone,
+// and intervals that meet pairwise and each meet the grid meet within it.
+// Their first columns (rows) then differ by at most a range's width, so the
+// 11-bit differences are the true ones, for any grid size.
+__device__ __forceinline__ float range_code(int x0, int x1, int y0, int y1) {
+    long long wd = (long long)x1 - x0 + 1, ht = (long long)y1 - y0 + 1;
+    wd = wd < 0 ? 0 : (wd > 31 ? 31 : wd);
+    ht = ht < 0 ? 0 : (ht > 31 ? 31 : ht);
+    return __uint_as_float(((uint32_t)x0 & 2047u) | (((uint32_t)y0 & 2047u) << 11) | ((uint32_t)wd << 22) |
+                           ((uint32_t)ht << 27));
 }
-__device__ __forceinline__ void unpack_range(int2 r, int &x0, int &x1, int &y0, int &y1) {
-    x0 = (int)(short)(r.x & 0xFFFF);
-    x1 = r.x >> 16;
-    y0 = (int)(short)(r.y & 0xFFFF);
-    y1 = r.y >> 16;
+
+// Whether the ranges ca (particle a) and cb share a bucket; if so, rank =
+// the first shared bucket's position in a's scan order (rows top to bottom,
+// columns left to right within a's range), the order in which the reference
+// meets b while scanning a's buckets (2D_Simulation.wgsl:143-170).  A rank
+// beyond 15 (an AABB wider than 4 buckets: the bucket grid is finer than
+// 2 r) or a side of 31 buckets or more sets device error 2.
+__device__ __forceinline__ bool shared_bucket(const DevWorld &w, uint32_t ca, uint32_t cb, unsigned &rank) {
+    const int wa = (int)((ca >> 22) & 31u), ha = (int)(ca >> 27);
+    const int wb = (int)((cb >> 22) & 31u), hb = (int)(cb >> 27);
+    if (wa == 0 || ha == 0 || wb == 0 || hb == 0) return false;
+    const int dx = (int)((cb - ca) << 21) >> 21;                  // bx0 - ax0
+    const int dy = (int)(((cb >> 11) - (ca >> 11)) << 21) >> 21;  // by0 - ay0
+    if (dx > wa - 1 || dx + wb - 1 < 0 || dy > ha - 1 || dy + hb - 1 < 0) return false;
+    rank = (unsigned)((dy > 0 ? dy : 0) * wa + (dx > 0 ? dx : 0));
+    if (rank > 15u || wa == 31 || ha == 31 || wb == 31 || hb == 31) {
+        atomicOr(w.err, 2);
+        rank = rank < 15u ? rank : 15u;
+    }
+    return true;
+}
+
+// the w word of particle b's position record: its range code
+__device__ __forceinline__ uint32_t range_of(const DevWorld &w, int b) {
+    return __float_as_uint(__ldg(reinterpret_cast<const float *>(w.pr + b) + 3));
 }
 
 // search-grid cell of a position (floor, clamped to the grid)
@@ -212,12 +238,13 @@ __device__ __forceinline__ bool last_warp(uint32_t *ticket) {
 // for a rebuild before this step's Simulation pass.
 // 2D_LOM.wgsl:85-152 of one particle from its records (p, v, a, flags m,
 // rebuild position b); `ext`: positions were set externally, so the
-// displacement is the stored dext.  Position, displacement and bucket range
-// go to pr_out/dp_out/rr_out, the velocities to vw, and data[4..6] to d4
-// when keep_d4 (a later LOM pass of the same call would overwrite it).
+// displacement is the stored dext.  Position and bucket range go to pr_out,
+// the displacement to dp_out, the velocities and rotation to vw, and
+// data[4..6] to d4 when keep_d4 (a later LOM pass of the same call would
+// overwrite it).
 __device__ __forceinline__ void lom_core(const DevWorld &w, const ScenePar &P, int i, uint32_t m, float4 p,
                                          float4 v, float4 a, float2 b, bool ext, float4 dext, bool keep_d4,
-                                         float4 *pr_out, float4 *dp_out, int2 *rr_out) {
+                                         float4 *pr_out, float4 *dp_out) {
     const float dT = P.p.dT;
     float ivx = v.x, ivy = v.y, iw = v.z;
     if (m & M_KICK_X) ivx = ivx + (a.x * dT) * 0.5f;               // :88
@@ -271,14 +298,14 @@ __device__ __forceinline__ void lom_core(const DevWorld &w, const ScenePar &P, i
     }
     p.x = p.x + d.x;                                               // :148
     p.y = p.y + d.y;
-    p.w = p.w + d.z;                                               // :149
-    pr_out[i] = p;
+    const float rot = v.w + d.z;                                   // :149
     {
         int x0, x1, y0, y1;                                        // 2D_LOM.wgsl:167-178
         ref_range(P, p.x, p.y, p.z, x0, x1, y0, y1);
-        rr_out[i] = pack_range(P, x0, x1, y0, y1);
+        p.w = range_code(x0, x1, y0, y1);
     }
-    w.vw[i] = make_float4(ivx, ivy, iw, v.w);                      // :151-152
+    pr_out[i] = p;
+    w.vw[i] = make_float4(ivx, ivy, iw, rot);                      // :151-152
     if (!ext) dp_out[i] = d;
     const float ex = p.x - b.x, ey = p.y - b.y;
     if (!(ex * ex + ey * ey <= P.disp_limit2)) atomicOr(w.rebuild, 1);
@@ -296,8 +323,7 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     const ScenePar &P = w.par[s];
     if (p.z == 0.0f) return;                                       // :83
     const bool ext = w.cc3[s] != 0;
-    lom_core(w, P, i, m, p, v, a, b, ext, ext ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f), true, w.pr, w.dp,
-             w.rr);
+    lom_core(w, P, i, m, p, v, a, b, ext, ext ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f), true, w.pr, w.dp);
 }
 
 // With w.ticket the kernel's last warp sets the rebuild conditional; without
@@ -741,7 +767,6 @@ __device__ __forceinline__ void gather_one(const DevWorld &w, const DevWorld &o,
     o.meta[i] = w.meta[src];
     o.orig[i] = w.orig[src];
     o.smask[i] = w.smask[src];
-    o.rr[i] = w.rr[src];
     const int N = w.N;
 #pragma unroll 2
     for (int j = 0; j < K; ++j) {
@@ -779,7 +804,6 @@ __device__ __forceinline__ void copy_back_one(const DevWorld &w, const DevWorld 
     w.meta[i] = o.meta[i];
     w.orig[i] = o.orig[i];
     w.smask[i] = o.smask[i];
-    w.rr[i] = o.rr[i];
     const int N = w.N;
 #pragma unroll 2
     for (int j = 0; j < K; ++j) {
@@ -951,29 +975,21 @@ __device__ __forceinline__ bool touching(float4 pa, float4 pb) {
     return sqrtf(s2) < t;
 }
 
-// b passed the distance test: keep it when its AABB shares a reference
-// bucket with the particle's, keyed by the first shared bucket
-__device__ __forceinline__ void accept_partner(const DevWorld &w, int b, int ax0, int ax1, int ay0, int ay1,
-                                               Narrow &nr) {
-    int bx0, bx1, by0, by1;
-    unpack_range(__ldg(&w.rr[b]), bx0, bx1, by0, by1);
-    if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) return;
-    const int fy = by0 > ay0 ? by0 : ay0;
-    const int fx = bx0 > ax0 ? bx0 : ax0;
-    unsigned rank = (unsigned)((fy - ay0) * (ax1 - ax0 + 1) + (fx - ax0));
-    if (rank > 15u) {           // AABB wider than 4 buckets: the bucket grid is smaller than 2 r
-        atomicOr(w.err, 2);
-        rank = 15u;
-    }
+// b (range code cb) passed the distance test: keep it when its AABB shares a
+// reference bucket with the particle's (range code ca), keyed by the first
+// shared bucket
+__device__ __forceinline__ void accept_partner(const DevWorld &w, int b, uint32_t ca, uint32_t cb, Narrow &nr) {
+    unsigned rank;
+    if (!shared_bucket(w, ca, cb, rank)) return;
     const uint32_t key = (rank << 28) | (uint32_t)__ldg(&w.orig[b]);
     top14_insert(key, b, nr);
 }
 
-__device__ __forceinline__ void narrow_test(const DevWorld &w, int i, int b, float4 pa, int ax0, int ax1,
-                                            int ay0, int ay1, Narrow &nr) {
+__device__ __forceinline__ void narrow_test(const DevWorld &w, int i, int b, float4 pa, Narrow &nr) {
     if (b == i) return;
-    if (!touching(pa, __ldg(&w.pr[b]))) return;
-    accept_partner(w, b, ax0, ax1, ay0, ay1, nr);
+    const float4 pb = __ldg(&w.pr[b]);
+    if (!touching(pa, pb)) return;
+    accept_partner(w, b, __float_as_uint(pa.w), __float_as_uint(pb.w), nr);
 }
 
 // entry k (0..15) of a candidate list held in two int4
@@ -998,7 +1014,7 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // With FUSE the particle's LOM pass of the next step follows at once
 // (2D_LOM.wgsl:85-152 with this step's accelerations and velocities, as the
 // next step's LOM would read them): its position, displacement and bucket
-// range go to the other buffers (pr_n, dp_n, rr_n), because neighbours still
+// range go to the other buffers (pr_n, dp_n), because neighbours still
 // read this step's values.  Particles that do not step on (zero radius, or a
 // served scene at its horizon) copy theirs across.
 // Accelerations and data[0..2] (this pass) and data[4..6] (the LOM pass) are
@@ -1019,10 +1035,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     const uint32_t m = w.meta[i];
     const float4 pa = w.pr[i];
     uint32_t mask = w.smask[i];
-    if (PART != 2) {
-        prefetch_l1(&w.nl[2 * (size_t)i]);
-        prefetch_l1(&w.rr[i]);
-    }
+    if (PART != 2) prefetch_l1(&w.nl[2 * (size_t)i]);
     if (PART != 1) {
         prefetch_l1(&w.dp[i]);
         prefetch_l1(&w.vw[i]);
@@ -1043,7 +1056,6 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         if (FUSE) {
             w.pr_n[i] = pa;
             w.dp_n[i] = w.dp[i];
-            w.rr_n[i] = w.rr[i];
         }
         return;
     }
@@ -1056,7 +1068,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     const bool detect = PART != 2 && P.p.collisions == 1 && w.det[s] != 0;
     if (detect) {                                                  // :126-228
         nr.cnt = 0;
-        int ax0, ax1, ay0, ay1;
+        const uint32_t ca = __float_as_uint(pa.w);  // the particle's bucket range
         bool direct = false;       // accepted partners that own a slot only mark it found
         int n_acc = 0;             // partners accepted in direct mode
         uint32_t found_slots = 0u;
@@ -1083,7 +1095,6 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 if (k > lmax) break;
                 if (k <= lc && touching(pa, __ldg(&w.pr[i + nl_entry(la, lb, k)]))) pass |= 1u << k;
             }
-            if (pass || (h0 & NL_NEAR_BIG)) unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
             // With at most 14 partners touching and no large particle near,
             // the accepted list is never cut at 14, so a partner that already
             // owns a slot needs no key: it only marks the slot found.  The
@@ -1092,9 +1103,8 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             if (direct) {
                 for (; pass; pass &= pass - 1) {
                     const int b = i + nl_entry(la, lb, __ffs(pass) - 1);
-                    int bx0, bx1, by0, by1;
-                    unpack_range(__ldg(&w.rr[b]), bx0, bx1, by0, by1);
-                    if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) continue;
+                    unsigned rank;
+                    if (!shared_bucket(w, ca, range_of(w, b), rank)) continue;
                     ++n_acc;
                     uint32_t hit = 0u;
                     for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
@@ -1105,30 +1115,24 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                         found_slots |= hit;
                         continue;
                     }
-                    const int fy = by0 > ay0 ? by0 : ay0;
-                    const int fx = bx0 > ax0 ? bx0 : ax0;
-                    unsigned rank = (unsigned)((fy - ay0) * (ax1 - ax0 + 1) + (fx - ax0));
-                    if (rank > 15u) {
-                        atomicOr(w.err, 2);
-                        rank = 15u;
-                    }
                     top14_insert((rank << 28) | (uint32_t)__ldg(&w.orig[b]), b, nr);
                 }
             } else {
-                for (; pass; pass &= pass - 1)
-                    accept_partner(w, i + nl_entry(la, lb, __ffs(pass) - 1), ax0, ax1, ay0, ay1, nr);
+                for (; pass; pass &= pass - 1) {
+                    const int b = i + nl_entry(la, lb, __ffs(pass) - 1);
+                    accept_partner(w, b, ca, range_of(w, b), nr);
+                }
             }
             if (h0 & NL_NEAR_BIG) {
                 int bf, bn;
                 big_cell(w, P, bf, bn);
-                for (int k = 0; k < bn; ++k) narrow_test(w, i, w.sorted[bf + k], pa, ax0, ax1, ay0, ay1, nr);
+                for (int k = 0; k < bn; ++k) narrow_test(w, i, w.sorted[bf + k], pa, nr);
             }
         } else {
-            unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
             if (P.n_big > 0) {
                 int bf, bn;
                 big_cell(w, P, bf, bn);
-                for (int k = 0; k < bn; ++k) narrow_test(w, i, w.sorted[bf + k], pa, ax0, ax1, ay0, ay1, nr);
+                for (int k = 0; k < bn; ++k) narrow_test(w, i, w.sorted[bf + k], pa, nr);
             }
             const int local = (int)w.kbuild[i] - P.cell_base;
             const int gx = local % P.g_w, gy = local / P.g_w;
@@ -1137,7 +1141,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
             for (int cy = cy0; cy <= cy1; ++cy) {
                 const int row = P.cell_base + cy * P.g_w;
                 const int beg = w.cell_start[row + cx0], end = w.cell_start[row + cx1 + 1];
-                for (int k = beg; k < end; ++k) narrow_test(w, i, w.sorted[k], pa, ax0, ax1, ay0, ay1, nr);
+                for (int k = beg; k < end; ++k) narrow_test(w, i, w.sorted[k], pa, nr);
             }
         }
         const int cnt = nr.cnt;
@@ -1399,12 +1403,11 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         w.vw[i] = v;
     } else if (steps_on) {
         lom_core(w, P, i, m, pa, v, make_float4(ax, ay, al, 0.0f), w.pbuild[i], false,
-                 make_float4(0.0f, 0.0f, 0.0f, 0.0f), lom_final || rem == 2, w.pr_n, w.dp_n, w.rr_n);
+                 make_float4(0.0f, 0.0f, 0.0f, 0.0f), lom_final || rem == 2, w.pr_n, w.dp_n);
     } else {
         w.vw[i] = v;
         w.pr_n[i] = pa;
         w.dp_n[i] = w.dp[i];
-        w.rr_n[i] = w.rr[i];
     }
     // data[0..2]; a particle without contacts writes +0 every step, which the
     // slot word's DF_ZERO bit (set while the stored value is all +0) lets it skip
@@ -1525,8 +1528,7 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
         if (threadIdx.x == 0) out[15] = 0;
         return;
     }
-    int ax0, ax1, ay0, ay1;
-    unpack_range(w.rr[i], ax0, ax1, ay0, ay1);
+    const uint32_t ca = __float_as_uint(pa.w);
     const float2 p0 = w.pbuild[i];
     const float reach = pa.z + P.r_grid + P.skin;
     int cx0, cy0, cx1, cy1;
@@ -1537,17 +1539,10 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     auto consider = [&](int b) {
         if (b == i) return;
-        if (!touching(pa, __ldg(&w.pr[b]))) return;
-        int bx0, bx1, by0, by1;
-        unpack_range(__ldg(&w.rr[b]), bx0, bx1, by0, by1);
-        if (bx0 > ax1 || bx1 < ax0 || by0 > ay1 || by1 < ay0) return;
-        const int fy = by0 > ay0 ? by0 : ay0;
-        const int fx = bx0 > ax0 ? bx0 : ax0;
-        unsigned rank = (unsigned)((fy - ay0) * (ax1 - ax0 + 1) + (fx - ax0));
-        if (rank > 15u) {
-            atomicOr(w.err, 2);
-            rank = 15u;
-        }
+        const float4 pb = __ldg(&w.pr[b]);
+        if (!touching(pa, pb)) return;
+        unsigned rank;
+        if (!shared_bucket(w, ca, __float_as_uint(pb.w), rank)) return;
         const int q = atomicAdd(&scount, 1);
         if (q < BIG_ACC_MAX) {
             skey[q] = (rank << 28) | (uint32_t)__ldg(&w.orig[b]);
@@ -1777,13 +1772,14 @@ __global__ void __launch_bounds__(ST_THREADS) k_stage_in(DevWorld w, RefArrays r
     const long long t = t0 + p;
     const int g = s_g[p], i = (int)(t - I.off);
     const float radius = r.radii[t];
-    const float4 pr = make_float4(r.pos[2 * t], r.pos[2 * t + 1], radius, r.rot[t]);
+    // the bucket range (w) is written by the LOM pass before any Simulation pass reads it
+    const float4 pr = make_float4(r.pos[2 * t], r.pos[2 * t + 1], radius, 0.0f);
     const float4 dp = make_float4(r.del_pos[2 * t], r.del_pos[2 * t + 1], r.del_rot[t], 0.0f);
     w.pr[g] = pr;
     w.pr_n[g] = pr;   // both buffers: a scene that never steps must read the same from either
     w.dp[g] = dp;
     w.dp_n[g] = dp;
-    w.vw[g] = make_float4(r.vel[2 * t], r.vel[2 * t + 1], r.rot_vel[t], 0.0f);
+    w.vw[g] = make_float4(r.vel[2 * t], r.vel[2 * t + 1], r.rot_vel[t], r.rot[t]);
     w.ac[g] = make_float4(r.acc[2 * t], r.acc[2 * t + 1], r.rot_acc[t], 0.0f);
     const float *f = r.forces + 6 * t;
     w.fx[g] = make_float4(f[0], f[1], f[2], 0.0f);
@@ -1904,7 +1900,7 @@ __global__ void __launch_bounds__(ST_THREADS) k_stage_out(DevWorld w, RefArrays 
     r.pos[2 * o] = pp.x;
     r.pos[2 * o + 1] = pp.y;
     r.radii[o] = pp.z;
-    r.rot[o] = pp.w;
+    r.rot[o] = v.w;
     r.vel[2 * o] = v.x;
     r.vel[2 * o + 1] = v.y;
     r.rot_vel[o] = v.z;
@@ -2023,12 +2019,13 @@ __global__ void k_gather_datum(DevWorld w, int base, const int32_t *__restrict__
     if (t >= count) return;
     const int i = w.o2i[base + idx[t]];
     const float4 p = w.pr[i], d4 = w.d4[i], dF = w.dF[i];
+    const float rot = w.vw[i].w;
     float *o = out + 10 * (size_t)t;
     o[0] = p.x;
     o[1] = p.y;
     o[2] = d4.x;
     o[3] = d4.y;
-    o[4] = p.w;
+    o[4] = rot;
     o[5] = d4.z;
     o[6] = dF.x;
     o[7] = dF.y;
@@ -2059,7 +2056,7 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_set_properties(DevWorld w, i
     bool setpos = false;
     if (in[0] == 1) { d.x = f[14] - p.x; p.x = f[14]; setpos = true; }
     if (in[1] == 1) { d.y = f[15] - p.y; p.y = f[15]; setpos = true; }
-    if (in[2] == 1) { d.z = f[16] - p.w; p.w = f[16]; }
+    if (in[2] == 1) { d.z = f[16] - v.w; v.w = f[16]; }
     if (in[3] == 1) v.x = f[17];
     if (in[4] == 1) v.y = f[18];
     if (in[5] == 1) v.z = f[19];

@@ -7,8 +7,9 @@
 //
 // Per-particle hot state is packed in float4 records so each load is one
 // 16-byte transaction:
-//   pr  {pos.x, pos.y, radius, rot}
-//   vw  {vel.x, vel.y, rot_vel, -}
+//   pr  {pos.x, pos.y, radius, range}   range: the AABB's reference-bucket
+//       range as a 32-bit code (written by the LOM pass; see range_code)
+//   vw  {vel.x, vel.y, rot_vel, rot}
 //   ac  {acc.x, acc.y, rot_acc, -}          ("accelerations" / rot_acc bindings)
 //   dp  {del_pos.x, del_pos.y, del_rot, -}
 //   fx  {forces.x, forces.y, forces.rot, -} (external forces, read when M_FEXT)
@@ -115,7 +116,6 @@ struct DevWorld {
     int32_t N, C, B, S, M, MP;
     float4 *pr, *vw, *ac, *dp, *fx, *d4, *dF;
     float4 *pr_n, *dp_n;        // the other position / displacement buffers (written by fused steps)
-    int2 *rr_n;
     uint32_t *meta;
     int32_t *orig;
     int32_t *o2i;               // [N] particle_base + scene-local index -> internal index (kept by the reorder)
@@ -126,7 +126,6 @@ struct DevWorld {
     int32_t *matp_ref;          // [N] material pointers
     float *data3;               // [N] data[7i+3]
     uint32_t *smask;            // bits 0-13: occupied slots; 16-29: slot's bonded field >= 0; 31: DF_ZERO
-    int2 *rr;                   // reference bucket range of the AABB: {x0 | x1 << 16, y0 | y1 << 16}
     int32_t *s_b, *s_bonded;
     float *s_tf, *s_btf, *s_thb;
     int32_t *b_status;

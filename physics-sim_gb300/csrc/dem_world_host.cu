@@ -470,7 +470,6 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
         x.orig = dalloc<int32_t>(owned, N, ok);
         x.o2i = dalloc<int32_t>(owned, N, ok);
         x.smask = dalloc<uint32_t>(owned, N, ok);
-        x.rr = dalloc<int2>(owned, N, ok);
         x.s_b = dalloc<int32_t>(owned, (size_t)K * N, ok);
         x.s_bonded = dalloc<int32_t>(owned, (size_t)K * N, ok);
         x.s_tf = dalloc<float>(owned, (size_t)K * N, ok);
@@ -480,7 +479,6 @@ int World::alloc(int N, int C, int B, int S, int M, int MP, int TB, uint32_t ev_
     particle_arrays(w);
     w.pr_n = dalloc<float4>(owned, N, ok);
     w.dp_n = dalloc<float4>(owned, N, ok);
-    w.rr_n = dalloc<int2>(owned, N, ok);
     parity = 0;
     w.b_status = dalloc<int32_t>(owned, B, ok);
     w.b_length = dalloc<float>(owned, B, ok);
@@ -746,7 +744,6 @@ int World::compute_layout(SceneHost &h, const dem_scene *sc) {
         if (dem_grid_capacity(&h.params, sc->radii, n, n, &g) != 0)
             return fail(DEM_E_INVALID, "cannot derive the bucket grid");
     }
-    if (g.w > 32766 || g.h > 32766) return fail(DEM_E_UNSUPPORTED, "bucket grid wider than 32766 cells");
     h.grid = g;
     // search grid: centre-binned cells of side >= 2 r_max (1 + pad), covering the
     // walls (or the particles, whichever is smaller in cells)
@@ -1219,7 +1216,7 @@ void World::update_kernel_form() {
 
 long long World::bytes_per_particle() const {
     // live + spare particle records, slots, broad phase and candidate lists
-    const long long rec = 7 * 16 + 3 * 4 + 8 + (long long)K * 5 * 4;
+    const long long rec = 7 * 16 + 3 * 4 + (long long)K * 5 * 4;
     return 2 * rec + 4 * 4 + 4 + 32 + 8 + 4;
 }
 
@@ -1637,12 +1634,11 @@ void World::drop_graph() {
     }
 }
 
-// the current and the other pr/dp/rr buffers trade places (a fused step
+// the current and the other pr/dp buffers trade places (a fused step
 // wrote the next step's values into the other ones)
 void World::flip() {
     std::swap(d.pr, d.pr_n);
     std::swap(d.dp, d.dp_n);
-    std::swap(d.rr, d.rr_n);
     parity ^= 1;
 }
 
