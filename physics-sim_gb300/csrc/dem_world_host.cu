@@ -1187,8 +1187,11 @@ int World::build(const std::vector<const dem_scene *> &scenes, const std::vector
 // the Simulation kernels compiled for what the scenes need (launch_interact):
 // the double-precision paths only while some scene uses the F64 distances
 // (they cost the FP32 scenes registers), and one bond model built in when
-// every scene uses it (served worlds, whose scenes come and go, do not
-// specialise on the model); a change recaptures the graphs
+// every scene with bonds uses it (served worlds, whose scenes come and go,
+// do not specialise on the model); a change recaptures the graphs.  A scene
+// without bond records steps alike under every model: uploads refuse a
+// contact whose bonded field names no bond record (>= n_bonds), so none of
+// its slots is bonded, and the models differ only for bonded slots.
 // 2 zeta of the normal dashpot for restitution e (0: off; e = 1 gives 0,
 // no damping): zeta = -ln e / sqrt(pi^2 + ln^2 e), in double, rounded once
 float dashpot_factor(float e) {
@@ -1203,11 +1206,12 @@ void World::update_kernel_form() {
     for (size_t s = 0; s < sh.size(); ++s) {
         if ((int)s == free_slot) continue;
         const SceneHost &h = sh[s];
-        models |= (h.params.bonds >= 0 && h.params.bonds <= 3) ? 1u << h.params.bonds : 0xFu;
+        if (h.n_bonds > 0)
+            models |= (h.params.bonds >= 0 && h.params.bonds <= 3) ? 1u << h.params.bonds : 0xFu;
         f64 |= h.use_f64 != 0 || h.damp2 > 0.0f;  // the generic kernels carry the F64 paths and the dashpot
     }
     int form = f64 ? -1 : -2;
-    if (!f64 && free_slot < 0) form = models == 1u ? 0 : models == 8u ? 3 : -2;
+    if (!f64 && free_slot < 0) form = (models == 1u || models == 0u) ? 0 : models == 8u ? 3 : -2;
     if (form != kernel_form) {
         kernel_form = form;
         drop_graph();
