@@ -835,6 +835,14 @@ void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStr
 // skin/2.  More than NL candidates, or one farther than an int16 offset can
 // reach: the particle searches the cell table (built in the same rebuild) at
 // every step instead.
+// the list's first word h0 (count and flags) and the slot word's NL_LIVE bit
+__device__ __forceinline__ void list_head(const DevWorld &w, int i, int16_t *h, int h0) {
+    h[0] = (int16_t)h0;
+    const uint32_t sm = w.smask[i];
+    const uint32_t nsm = h0 != 0 ? (sm | NL_LIVE) : (sm & ~NL_LIVE);
+    if (nsm != sm) w.smask[i] = nsm;
+}
+
 __device__ __forceinline__ void list_build_one(const DevWorld &w, int i) {
     if (!chunk_live(w, i)) return;
     const uint32_t m = w.meta[i];
@@ -843,12 +851,12 @@ __device__ __forceinline__ void list_build_one(const DevWorld &w, int i) {
     w.pbuild[i] = make_float2(pa.x, pa.y);
     int16_t *h = reinterpret_cast<int16_t *>(w.nl + 2 * (size_t)i);
     if (!w.act[meta_scene(m)] || pa.z == 0.0f) {
-        h[0] = 0;
+        list_head(w, i, h, 0);
         w.kbuild[i] = (uint32_t)P.dead_cell;
         return;
     }
     if (m & M_BIG) {
-        h[0] = (int16_t)NL_BIG;
+        list_head(w, i, h, NL_BIG);
         w.kbuild[i] = (uint32_t)P.big_cell;
         return;
     }
@@ -890,7 +898,7 @@ __device__ __forceinline__ void list_build_one(const DevWorld &w, int i) {
             }
         }
     }
-    h[0] = (int16_t)((over ? NL_OVERFLOW : cnt) | flags);
+    list_head(w, i, h, (over ? NL_OVERFLOW : cnt) | flags);
     if (over) atomicAdd(&w.stats[5], 1ull);
 }
 
@@ -1035,12 +1043,14 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     const uint32_t m = w.meta[i];
     const float4 pa = w.pr[i];
     uint32_t mask = w.smask[i];
-    if (PART != 2) prefetch_l1(&w.nl[2 * (size_t)i]);
     if (PART != 1) {
-        prefetch_l1(&w.dp[i]);
         prefetch_l1(&w.vw[i]);
         if (FUSE) prefetch_l1(&w.pbuild[i]);
     }
+    // the candidate list only when it is not empty, del_pos only for a
+    // particle with contacts (its force loop reads it)
+    if (PART != 2 && (mask & NL_LIVE)) prefetch_l1(&w.nl[2 * (size_t)i]);
+    if (PART != 1 && (mask & ((1u << K) - 1u))) prefetch_l1(&w.dp[i]);
     const int N = w.N;
     for (uint32_t left = mask & ((1u << K) - 1u); left; left &= left - 1) {
         const int j = __ffs(left) - 1;
@@ -1072,7 +1082,7 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         bool direct = false;       // accepted partners that own a slot only mark it found
         int n_acc = 0;             // partners accepted in direct mode
         uint32_t found_slots = 0u;
-        const int4 la = __ldg(&w.nl[2 * (size_t)i]);
+        const int4 la = (mask & NL_LIVE) ? __ldg(&w.nl[2 * (size_t)i]) : make_int4(0, 0, 0, 0);
         const int h0 = la.x & 0xFFFF;
         const int lc = h0 & 0xFF;
         if (lc == NL_BIG) {

@@ -19,7 +19,9 @@
 // word smask[i] holds the occupancy of the 14 slots in bits 0-13, so empty
 // slots are never read, and in bits 16-29 whether each slot's `bonded` field
 // is >= 0 (kept for empty slots too, whose stale field a new contact
-// inherits), so unbonded slots never read `bonded`.  Bit 31 (DF_ZERO) records
+// inherits), so unbonded slots never read `bonded`.  Bit 14 (NL_LIVE) is set
+// while the particle's candidate list holds a candidate or a flag, so
+// particles with an empty list skip reading it.  Bit 31 (DF_ZERO) records
 // that dF is all +0, so particles without contacts skip rewriting it.
 #pragma once
 #include <cuda_runtime.h>
@@ -32,6 +34,7 @@ namespace demgb {
 constexpr int K = DEM_MAX_CONTACTS;
 constexpr int BSHIFT = 16;  // first bonded-field bit of the slot word
 constexpr uint32_t DF_ZERO = 1u << 31;  // slot-word bit: dF holds +0, +0, +0
+constexpr uint32_t NL_LIVE = 1u << 14;  // slot-word bit: the candidate list is not empty
 
 // meta word: fixity predicates, external-force flag, material, scene
 enum : uint32_t {
@@ -125,7 +128,8 @@ struct DevWorld {
     float *force_ref;           // [6N] external forces
     int32_t *matp_ref;          // [N] material pointers
     float *data3;               // [N] data[7i+3]
-    uint32_t *smask;            // bits 0-13: occupied slots; 16-29: slot's bonded field >= 0; 31: DF_ZERO
+    uint32_t *smask;            // bits 0-13: occupied slots; 14: NL_LIVE; 16-29: slot's bonded field >= 0;
+                                // 31: DF_ZERO
     int32_t *s_b, *s_bonded;
     float *s_tf, *s_btf, *s_thb;
     int32_t *b_status;
