@@ -242,10 +242,12 @@ __device__ __forceinline__ bool last_warp(uint32_t *ticket) {
 // the displacement to dp_out, the velocities and rotation to vw, and
 // data[4..6] to d4 when keep_d4 (a later LOM pass of the same call would
 // overwrite it).
-__device__ __forceinline__ void lom_core(const DevWorld &w, const ScenePar &P, int i, uint32_t m, float4 p,
-                                         float4 v, float4 a, float2 b, bool ext, float4 dext, bool keep_d4,
-                                         float4 *pr_out, float4 *dp_out) {
-    const float dT = P.p.dT;
+// U: the scene's settings (P.p) and model constants, P its geometry; the
+// two are the same record unless the world's scenes share the former.
+__device__ __forceinline__ void lom_core(const DevWorld &w, const ScenePar &P, const ScenePar &U, int i,
+                                         uint32_t m, float4 p, float4 v, float4 a, float2 b, bool ext, float4 dext,
+                                         bool keep_d4, float4 *pr_out, float4 *dp_out) {
+    const float dT = U.p.dT;
     float ivx = v.x, ivy = v.y, iw = v.z;
     if (m & M_KICK_X) ivx = ivx + (a.x * dT) * 0.5f;               // :88
     if (m & M_KICK_Y) ivy = ivy + (a.y * dT) * 0.5f;               // :89
@@ -259,7 +261,7 @@ __device__ __forceinline__ void lom_core(const DevWorld &w, const ScenePar &P, i
     }
     float r = p.z;
     float npx = p.x + d.x, npy = p.y + d.y;                        // :103
-    if (P.p.round_bounds == 0) {                                   // :104-129
+    if (U.p.round_bounds == 0) {                                   // :104-129
         float yH = P.yH, xW = P.xW;
         if (!(m & M_FIX_Y)) {
             if (npy - r < -yH) {
@@ -279,14 +281,14 @@ __device__ __forceinline__ void lom_core(const DevWorld &w, const ScenePar &P, i
                 p.x = p.x - ((npx + r) - xW);
             }
         }
-    } else if (len2f(npx, npy) + r > P.p.bound_radius) {          // :130-145
+    } else if (len2f(npx, npy) + r > U.p.bound_radius) {          // :130-145
         float L = len2f(npx, npy);
         float nx = npx / L, ny = npy / L;
         float dd = d.x * nx + d.y * ny;
         float dcx = dd * nx, dcy = dd * ny;
         float vv = ivx * nx + ivy * ny;
         float cvx = vv * nx, cvy = vv * ny;
-        float Rb = P.p.bound_radius;
+        float Rb = U.p.bound_radius;
         if (!(m & M_FIX_X)) {
             p.x = (nx * (Rb - r)) - dcx;
             ivx = (-cvx) * 0.5f;
@@ -323,7 +325,7 @@ __device__ __forceinline__ void lom_particle(const DevWorld &w, int i) {
     const ScenePar &P = w.par[s];
     if (p.z == 0.0f) return;                                       // :83
     const bool ext = w.cc3[s] != 0;
-    lom_core(w, P, i, m, p, v, a, b, ext, ext ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f), true, w.pr, w.dp);
+    lom_core(w, P, P, i, m, p, v, a, b, ext, ext ? w.dp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f), true, w.pr, w.dp);
 }
 
 // With w.ticket the kernel's last warp sets the rebuild conditional; without
@@ -1034,8 +1036,18 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // rest (and the registers it holds) drops out: 0 or 3, every scene uses that
 // bond model and none the F64 distances; -2, any bond model, no F64
 // distances; -1, anything.  Only -1 carries the double-precision paths.
-template <int PART, bool FUSE, int FORM>
-__device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr, bool lom_final) {
+// PS: where the scene parameters come from.  PS_SCENE: w.par[scene].
+// PS_ONE: the world holds a single scene, whose parameters come with the
+// launch (Pv, in the kernel's parameter space): the instructions then read
+// them where they are used, with no load and no register held for them (on
+// the 4 M-particle impact scene the force kernel's spills disappear and the
+// Simulation kernels take 7.7 % less time).  PS_SHARED: the scenes differ
+// only in geometry and record bases; their common settings and model
+// constants (the fields read through U) come with the launch, the rest from
+// w.par[scene].
+template <int PART, bool FUSE, int FORM, int PS>
+__device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr, bool lom_final,
+                                                  const ScenePar &Pv) {
     // The particle's own records: the ones needed first are loaded now, the
     // rest (read only after the scene, detection and slot checks resolve)
     // are prefetched now, so the DRAM round trips overlap instead of
@@ -1060,7 +1072,8 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     }
     const int s = (int)meta_scene(m);
     if (!w.act[s]) return;
-    const ScenePar &P = w.par[s];
+    const ScenePar &P = PS == PS_ONE ? Pv : w.par[s];
+    const ScenePar &U = PS == PS_SCENE ? P : Pv;
     if (pa.z == 0.0f) {                                            // :113-118
         if (PART != 1) w.dF[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (FUSE) {
@@ -1070,12 +1083,12 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         return;
     }
     const uint32_t before = mask;
-    const int bonds_model = FORM == 0 ? 0 : FORM == 3 ? 3 : P.p.bonds;
+    const int bonds_model = FORM == 0 ? 0 : FORM == 3 ? 3 : U.p.bonds;
     constexpr bool MAY_F64 = FORM == -1;
 
     // Loads that only some particles need (the bucket range, the second half
     // of the candidate list, del_pos) wait until the particle needs them.
-    const bool detect = PART != 2 && P.p.collisions == 1 && w.det[s] != 0;
+    const bool detect = PART != 2 && U.p.collisions == 1 && w.det[s] != 0;
     if (detect) {                                                  // :126-228
         nr.cnt = 0;
         const uint32_t ca = __float_as_uint(pa.w);  // the particle's bucket range
@@ -1221,24 +1234,24 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         }
         const float4 pb = __ldg(&w.pr[b]);
         const float4 db = __ldg(&w.dp[b]);
-        const uint32_t mb = P.n_mat == 1 ? 0u : __ldg(&w.meta[b]);
+        const uint32_t mb = U.n_mat == 1 ? 0u : __ldg(&w.meta[b]);
         int st = 0;
         float blen = 0.0f;
-        float2 str = make_float2(P.p.bond_normal_strength, P.p.bond_shear_strength);
+        float2 str = make_float2(U.p.bond_normal_strength, U.p.bond_shear_strength);
         if (bnn) {
             const int bg = P.bond_base + bonded;
             st = w.b_status[bg];
             blen = w.b_length[bg];
-            if (P.has_strength) str = w.b_str[bg];
+            if (U.has_strength) str = w.b_str[bg];
         }
         if (st < 0) {                                              // :236-239
             w.s_bonded[j * N + i] = st;
             bonded = st;
             mask &= ~(1u << (BSHIFT + j));
         }
-        const float2 kns = __ldg(&w.pair[P.pair_base + (int)meta_mat(m) * P.n_mat + (int)meta_mat(mb)]);
+        const float2 kns = __ldg(&w.pair[P.pair_base + (int)meta_mat(m) * U.n_mat + (int)meta_mat(mb)]);
         float meff = 0.0f;  // effective mass of the pair, for the dashpot (generic form only)
-        if (MAY_F64 && P.damp2 > 0.0f) {
+        if (MAY_F64 && U.damp2 > 0.0f) {
             const float ma = ((w.mats[P.mat_base + meta_mat(m)].density * 3.14159274101257324219f) * pa.z) * pa.z;
             const float mbb = ((w.mats[P.mat_base + meta_mat(mb)].density * 3.14159274101257324219f) * pb.z) * pb.z;
             meff = (ma * mbb) / (ma + mbb);
@@ -1249,19 +1262,19 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
         // from a - b only in sign, so the squares agree)
         if (bonded < 0 || bonds_model == 0) {
             float tf = tf0;
-            f = linear_model<MAY_F64>(P, kns, pa, da, pb, db, pa.z + pb.z, len2f(pa.x - pb.x, pa.y - pb.y), tf, acc,
+            f = linear_model<MAY_F64>(U, kns, pa, da, pb, db, pa.z + pb.z, len2f(pa.x - pb.x, pa.y - pb.y), tf, acc,
                                      meff);
             w.s_tf[j * N + i] = tf;
         } else {
             const int bg = P.bond_base + bonded;
             const float sn = str.x, ss = str.y;
             if (bonds_model == 3) {                                // :286-336
-                const float kn = P.p.bond_normal_stiffness, ks = P.p.bond_shear_stiffness;
-                const float Rr = P.lambda * (pa.z < pb.z ? pa.z : pb.z);
+                const float kn = U.p.bond_normal_stiffness, ks = U.p.bond_shear_stiffness;
+                const float Rr = U.lambda * (pa.z < pb.z ? pa.z : pb.z);
                 const float A = (2.0f * Rr) * 1.0f;
                 const float I = ((2.0f / 3.0f * Rr) * Rr) * Rr;
                 const float L = len2f(pa.x - pb.x, pa.y - pb.y);
-                const float nd = (MAY_F64 && P.use_f64) ? distance2(1, pa, pb, blen) : L - blen;
+                const float nd = (MAY_F64 && U.use_f64) ? distance2(1, pa, pb, blen) : L - blen;
                 float Fn = ((-kn) * nd) * A;
                 const float vx = pa.x - pb.x, vy = pa.y - pb.y;
                 const float nx = vx / L, ny = vy / L;
@@ -1281,8 +1294,8 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 float bend = ((-kn) * I) * thb;
                 bend = bend < 0.0f ? -bend : bend;
                 const float abtf = btf < 0.0f ? -btf : btf;
-                if (P.p.bonds_tear == 1 &&
-                    ((Fn / A) - (P.p.moment_contribution_factor * (bend * Rr)) / I < -sn ||
+                if (U.p.bonds_tear == 1 &&
+                    ((Fn / A) - (U.p.moment_contribution_factor * (bend * Rr)) / I < -sn ||
                      abtf / A > ss)) {
                     const int code = -10 + sign_i32(nd);
                     record_break(w, P, s, *w.step, bg, code, i, b);
@@ -1300,20 +1313,20 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 acc.d1 = acc.d1 + btf;
                 acc.d2 = acc.d2 + M;
                 float tf = tf0;
-                const F3 lm = linear_model<MAY_F64>(P, kns, pa, da, pb, db, blen, L, tf, acc, meff);
+                const F3 lm = linear_model<MAY_F64>(U, kns, pa, da, pb, db, blen, L, tf, acc, meff);
                 w.s_tf[j * N + i] = tf;
                 f.x = Fx + lm.x;
                 f.y = Fy + lm.y;
                 f.z = M + lm.z;
             } else if (bonds_model == 1) {                         // :419-432
                 const float L = len2f(pa.x - pb.x, pa.y - pb.y);
-                const float disp = (MAY_F64 && P.use_f64) ? distance1(1, pa, pb) : L - (pa.z + pb.z);
+                const float disp = (MAY_F64 && U.use_f64) ? distance1(1, pa, pb) : L - (pa.z + pb.z);
                 float fx = 0.0f, fy = 0.0f;
-                const float sf = P.p.bond_normal_stiffness * disp;
+                const float sf = U.p.bond_normal_stiffness * disp;
                 const float vx = pb.x - pa.x, vy = pb.y - pa.y;
                 fx = fx + sf * (vx / L);
                 fy = fy + sf * (vy / L);
-                if (P.p.bonds_tear == 1 && sf >= sn) {
+                if (U.p.bonds_tear == 1 && sf >= sn) {
                     const int code = -10 + sign_i32(disp);
                     record_break(w, P, s, *w.step, bg, code, i, b);
                     w.s_bonded[j * N + i] = code;
@@ -1322,16 +1335,16 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                     fy = 0.0f;
                 }
                 float tf = tf0;
-                const F3 lm = linear_model<MAY_F64>(P, kns, pa, da, pb, db, blen, L, tf, acc, meff);
+                const F3 lm = linear_model<MAY_F64>(U, kns, pa, da, pb, db, blen, L, tf, acc, meff);
                 w.s_tf[j * N + i] = tf;
                 f.x = lm.x + fx;
                 f.y = lm.y + fy;
                 f.z = lm.z + 0.0f;
             } else if (bonds_model == 2) {                         // :375-417
                 const float L = len2f(pa.x - pb.x, pa.y - pb.y);
-                const float nd = (MAY_F64 && P.use_f64) ? distance1(1, pa, pb) : L - (pa.z + pb.z);
-                const float kn = P.kb2;
-                const float ks = P.ksb2;
+                const float nd = (MAY_F64 && U.use_f64) ? distance1(1, pa, pb) : L - (pa.z + pb.z);
+                const float kn = U.kb2;
+                const float ks = U.ksb2;
                 float Fn = (-nd) * kn;
                 const float vx = pa.x - pb.x, vy = pa.y - pb.y;
                 const float nx = vx / L, ny = vy / L;
@@ -1342,12 +1355,12 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
                 const float rt = (rx * tx + ry * ty) + rr;
                 float tf = tf0;
                 tf = tf + rt * ks;
-                const float cd = P.p.contact_damping;
+                const float cd = U.p.contact_damping;
                 float Fx = cd * (nx * Fn + tx * tf);
                 float Fy = cd * (ny * Fn + ty * tf);
                 float M = (-pa.z) * tf;
                 const float atf = tf < 0.0f ? -tf : tf;
-                if (P.p.bonds_tear == 1 && (Fn < -sn || atf > ss)) {
+                if (U.p.bonds_tear == 1 && (Fn < -sn || atf > ss)) {
                     const int code = -10 + sign_i32(nd);
                     record_break(w, P, s, *w.step, bg, code, i, b);
                     w.s_bonded[j * N + i] = code;
@@ -1382,20 +1395,20 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     float fxs = nfx + fe.x;
     float fys = nfy + fe.y;
     float moment = nm + fe.z;
-    if (P.p.gravity == 1 && P.p.planet_mode == 1) {
+    if (U.p.gravity == 1 && U.p.planet_mode == 1) {
         float cx = 0.0f, cy = 0.0f;
-        if (P.p.mouse_gravity == 1) {
-            cx = P.p.gravity_x;
-            cy = P.p.gravity_y;
+        if (U.p.mouse_gravity == 1) {
+            cx = U.p.gravity_x;
+            cy = U.p.gravity_y;
         }
         const float dx = cx - pa.x, dy = cy - pa.y;
         if (dx != 0.0f || dy != 0.0f) {
             const float L = len2f(dx, dy);
-            fxs = fxs + (((dx / L) * 9.81f) * P.p.gravity_acc) * mass;
-            fys = fys + (((dy / L) * 9.81f) * P.p.gravity_acc) * mass;
+            fxs = fxs + (((dx / L) * 9.81f) * U.p.gravity_acc) * mass;
+            fys = fys + (((dy / L) * 9.81f) * U.p.gravity_acc) * mass;
         }
-    } else if (P.p.gravity == 1) {
-        const float ga = 9.81f * P.p.gravity_acc;
+    } else if (U.p.gravity == 1) {
+        const float ga = 9.81f * U.p.gravity_acc;
         fxs = fxs + 0.0f;
         fys = fys + (-ga) * mass;
     }
@@ -1405,14 +1418,14 @@ __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narr
     const bool steps_on = FUSE && rem > 1;  // this scene's next step is in this call
     if (!steps_on) w.ac[i] = make_float4(ax, ay, al, 0.0f);
     float4 v = w.vw[i];
-    const float dT = P.p.dT;
+    const float dT = U.p.dT;
     if (m & M_KICK_X) v.x = v.x + (0.5f * ax) * dT;
     if (m & M_KICK_Y) v.y = v.y + (0.5f * ay) * dT;
     if (m & M_KICK_R) v.z = v.z + (0.5f * al) * dT;
     if (!FUSE) {
         w.vw[i] = v;
     } else if (steps_on) {
-        lom_core(w, P, i, m, pa, v, make_float4(ax, ay, al, 0.0f), w.pbuild[i], false,
+        lom_core(w, P, U, i, m, pa, v, make_float4(ax, ay, al, 0.0f), w.pbuild[i], false,
                  make_float4(0.0f, 0.0f, 0.0f, 0.0f), lom_final || rem == 2, w.pr_n, w.dp_n);
     } else {
         w.vw[i] = v;
@@ -1474,31 +1487,33 @@ __device__ __forceinline__ void interact_tail(const DevWorld &w, bool fused, int
 // Minimum blocks per SM: measured on GB300 (c3 mix, c2 scene).  Occupancy
 // outweighs the few spilled words down to 40 registers for k_interact (12
 // blocks: 7 % faster than 8) and 56 for k_forces (9 blocks).
-template <bool FUSE, int FORM>
+// pv: the parameters of the world's only scene (PS_ONE), or the settings its
+// scenes share (PS_SHARED); unused with PS_SCENE
+template <bool FUSE, int FORM, int PS>
 __global__ void __launch_bounds__(IB, 12) k_interact(DevWorld w, int in_graph, cudaGraphConditionalHandle cond,
-                                                    int lom_final) {
+                                                    int lom_final, const __grid_constant__ ScenePar pv) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N && chunk_live(w, i)) interact_particle<0, FUSE, FORM>(w, i, nr, lom_final != 0);
+    if (i < w.N && chunk_live(w, i)) interact_particle<0, FUSE, FORM, PS>(w, i, nr, lom_final != 0, pv);
     interact_tail(w, FUSE, in_graph, cond);
 }
 
-template <int FORM>
-__global__ void __launch_bounds__(IB, 12) k_narrow(DevWorld w) {
+template <int FORM, int PS>
+__global__ void __launch_bounds__(IB, 12) k_narrow(DevWorld w, const __grid_constant__ ScenePar pv) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N && chunk_live(w, i)) interact_particle<1, false, FORM>(w, i, nr, false);
+    if (i < w.N && chunk_live(w, i)) interact_particle<1, false, FORM, PS>(w, i, nr, false, pv);
 }
 
-template <bool FUSE, int FORM>
+template <bool FUSE, int FORM, int PS>
 __global__ void __launch_bounds__(IB, 9) k_forces(DevWorld w, int in_graph, cudaGraphConditionalHandle cond,
-                                                  int lom_final) {
+                                                  int lom_final, const __grid_constant__ ScenePar pv) {
     Narrow nr;
     nr.cnt = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.N && chunk_live(w, i)) interact_particle<2, FUSE, FORM>(w, i, nr, lom_final != 0);
+    if (i < w.N && chunk_live(w, i)) interact_particle<2, FUSE, FORM, PS>(w, i, nr, lom_final != 0, pv);
     interact_tail(w, FUSE, in_graph, cond);
 }
 
@@ -1616,22 +1631,31 @@ __global__ void __launch_bounds__(BIG_THREADS) k_big_narrow(DevWorld w) {
     if (threadIdx.x == 0) out[15] = keep;
 }
 
-template <int FORM>
-static int launch_sim(const DevWorld &w, int g, cudaStream_t st, bool fuse, int ig, int lf,
-                      cudaGraphConditionalHandle cond) {
+template <int FORM, int PS>
+static int launch_sim_as(const DevWorld &w, int g, cudaStream_t st, bool fuse, int ig, int lf,
+                         cudaGraphConditionalHandle cond, const ScenePar &pv) {
     if (w.split) {
-        k_narrow<FORM><<<g, IB, 0, st>>>(w);
-        if (fuse) k_forces<true, FORM><<<g, IB, 0, st>>>(w, ig, cond, lf);
-        else k_forces<false, FORM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+        k_narrow<FORM, PS><<<g, IB, 0, st>>>(w, pv);
+        if (fuse) k_forces<true, FORM, PS><<<g, IB, 0, st>>>(w, ig, cond, lf, pv);
+        else k_forces<false, FORM, PS><<<g, IB, 0, st>>>(w, ig, cond, lf, pv);
         return 2;
     }
-    if (fuse) k_interact<true, FORM><<<g, IB, 0, st>>>(w, ig, cond, lf);
-    else k_interact<false, FORM><<<g, IB, 0, st>>>(w, ig, cond, lf);
+    if (fuse) k_interact<true, FORM, PS><<<g, IB, 0, st>>>(w, ig, cond, lf, pv);
+    else k_interact<false, FORM, PS><<<g, IB, 0, st>>>(w, ig, cond, lf, pv);
     return 1;
 }
 
+template <int FORM>
+static int launch_sim(const DevWorld &w, int g, cudaStream_t st, bool fuse, int ig, int lf,
+                      cudaGraphConditionalHandle cond, const ScenePar *pv, int ps) {
+    if (ps == PS_ONE) return launch_sim_as<FORM, PS_ONE>(w, g, st, fuse, ig, lf, cond, *pv);
+    if (ps == PS_SHARED) return launch_sim_as<FORM, PS_SHARED>(w, g, st, fuse, ig, lf, cond, *pv);
+    const ScenePar unused{};
+    return launch_sim_as<FORM, PS_SCENE>(w, g, st, fuse, ig, lf, cond, unused);
+}
+
 int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool lom_final,
-                    bool in_graph, cudaGraphConditionalHandle cond, int form) {
+                    bool in_graph, cudaGraphConditionalHandle cond, int form, const ScenePar *pv, int ps) {
     (void)block;
     int k = 0;
     if (bigs && w.n_big_slots > 0) {
@@ -1641,10 +1665,10 @@ int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bo
     const int g = w.N > 0 ? (w.N + IB - 1) / IB : 1;
     const int ig = in_graph ? 1 : 0, lf = lom_final ? 1 : 0;
     switch (form) {
-        case 3: k += launch_sim<3>(w, g, st, fuse, ig, lf, cond); break;
-        case 0: k += launch_sim<0>(w, g, st, fuse, ig, lf, cond); break;
-        case -2: k += launch_sim<-2>(w, g, st, fuse, ig, lf, cond); break;
-        default: k += launch_sim<-1>(w, g, st, fuse, ig, lf, cond); break;
+        case 3: k += launch_sim<3>(w, g, st, fuse, ig, lf, cond, pv, ps); break;
+        case 0: k += launch_sim<0>(w, g, st, fuse, ig, lf, cond, pv, ps); break;
+        case -2: k += launch_sim<-2>(w, g, st, fuse, ig, lf, cond, pv, ps); break;
+        default: k += launch_sim<-1>(w, g, st, fuse, ig, lf, cond, pv, ps); break;
     }
     if (!w.ticket) {
         k_end_step<<<1, END_THREADS, 0, st>>>(w);

@@ -25,6 +25,7 @@
 // that dF is all +0, so particles without contacts skip rewriting it.
 #pragma once
 #include <cuda_runtime.h>
+#include <cstring>
 #include <stdint.h>
 
 #include "dem.h"
@@ -219,8 +220,53 @@ void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int3
 // form selects the Simulation kernels compiled for what the scenes need:
 // 0 or 3 (every scene uses that bond model, none the F64 distances), -2 (any
 // bond model, no F64 distances), -1 (anything)
+// ps, pv: where the Simulation kernels read the scene parameters.  PS_SCENE
+// (pv unused): w.par[scene].  PS_ONE: *pv, equal to w.par[0], the world's
+// only scene.  PS_SHARED: the settings every scene of the world shares
+// (shared_settings) from *pv, the rest from w.par[scene].
+constexpr int PS_SCENE = 0, PS_SHARED = 1, PS_ONE = 2;
 int launch_interact(const DevWorld &w, int block, cudaStream_t st, bool bigs, bool fuse, bool lom_final,
-                    bool in_graph, cudaGraphConditionalHandle cond, int form);
+                    bool in_graph, cudaGraphConditionalHandle cond, int form, const ScenePar *pv, int ps);
+
+// The fields of a scene's parameters that the Simulation kernels read from
+// the launch under PS_SHARED (the settings and model constants), the others
+// zero; with bonds false also the bond model's fields, which a scene without
+// bond records never reads (it has no bonded slot, so it steps alike under
+// any bond settings).  Scenes share their settings when their records agree
+// here, the bond fields compared among the scenes that have bonds.
+inline ScenePar shared_settings(const ScenePar &P, bool bonds) {
+    ScenePar k;
+    std::memset(&k, 0, sizeof k);
+    k.p.collisions = P.p.collisions;
+    k.p.gravity = P.p.gravity;
+    k.p.planet_mode = P.p.planet_mode;
+    k.p.mouse_gravity = P.p.mouse_gravity;
+    k.p.gravity_x = P.p.gravity_x;
+    k.p.gravity_y = P.p.gravity_y;
+    k.p.gravity_acc = P.p.gravity_acc;
+    k.p.dT = P.p.dT;
+    k.p.friction_coefficient = P.p.friction_coefficient;
+    k.p.round_bounds = P.p.round_bounds;
+    k.p.bound_radius = P.p.bound_radius;
+    k.n_mat = P.n_mat;
+    k.damp2 = P.damp2;
+    k.use_f64 = P.use_f64;
+    if (bonds) {
+        k.p.bonds = P.p.bonds;
+        k.p.bond_normal_strength = P.p.bond_normal_strength;
+        k.p.bond_shear_strength = P.p.bond_shear_strength;
+        k.p.bond_normal_stiffness = P.p.bond_normal_stiffness;
+        k.p.bond_shear_stiffness = P.p.bond_shear_stiffness;
+        k.p.bonds_tear = P.p.bonds_tear;
+        k.p.moment_contribution_factor = P.p.moment_contribution_factor;
+        k.p.contact_damping = P.p.contact_damping;
+        k.has_strength = P.has_strength;
+        k.lambda = P.lambda;
+        k.kb2 = P.kb2;
+        k.ksb2 = P.ksb2;
+    }
+    return k;
+}
 void launch_set_properties(const DevWorld &w, int scene, const int32_t *d_sel, int32_t *d_sel_out,
                            const int32_t *d_props, int block, cudaStream_t st);
 int scan_tmp_size(int n);

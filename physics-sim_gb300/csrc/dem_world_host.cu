@@ -1622,7 +1622,8 @@ void World::enqueue_plain_step(bool first, bool last, bool next_last) {
     enqueue_rebuild(stream, d.rebuild, true);
     rec(T_INTERACT, true);
     const bool fuse = fuse_lom && !last;
-    k += launch_interact(d, block, stream, has_bigs, fuse, next_last, false, cudaGraphConditionalHandle{}, kernel_form);
+    k += launch_interact(d, block, stream, has_bigs, fuse, next_last, false, cudaGraphConditionalHandle{}, kernel_form,
+                         &par_pv, par_ps);
     rec(T_INTERACT, false);
     if (fuse) flip();
     launches += k + rebuild_kernels;
@@ -1724,13 +1725,13 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
         if (fuse_lom && k + 1 < R) {
             cudaGraphConditionalHandle hn{};
             CKR(cudaGraphConditionalHandleCreate(&hn, g, 0, cudaGraphCondAssignDefault));
-            kernels += launch_interact(d, block, stream, has_bigs, true, k + 2 == R, true, hn, kernel_form);
+            kernels += launch_interact(d, block, stream, has_bigs, true, k + 2 == R, true, hn, kernel_form, &par_pv, par_ps);
             CKR(cudaGetLastError());
             flip();
             h = hn;
         } else {
             kernels += launch_interact(d, block, stream, has_bigs, false, false, true, cudaGraphConditionalHandle{},
-                                       kernel_form);
+                                       kernel_form, &par_pv, par_ps);
             CKR(cudaGetLastError());
         }
     }
@@ -1748,10 +1749,45 @@ int World::capture_graph(int R, cudaGraphExec_t *out, int *kernels_out) {
     return DEM_OK;
 }
 
+// the scene parameters' source for the Simulation launches of a step() call:
+// the host records equal the device's whenever a call steps
+void World::update_param_source() {
+    if (sh.size() == 1) {
+        par_ps = PS_ONE;
+        std::memcpy(&par_pv, &sh[0].par, sizeof(ScenePar));  // padding too: graph_par is compared bytewise
+        return;
+    }
+    par_ps = PS_SCENE;
+    std::memset(&par_pv, 0, sizeof par_pv);
+    if (sh.empty()) return;
+    const ScenePar k0 = shared_settings(sh[0].par, false);
+    int bonded = -1;  // a scene with bond records: its bond settings are the shared ones
+    for (size_t s = 0; s < sh.size(); ++s) {
+        const ScenePar k = shared_settings(sh[s].par, false);
+        if (std::memcmp(&k, &k0, sizeof k) != 0) return;
+        if (sh[s].n_bonds <= 0) continue;
+        if (bonded < 0) {
+            bonded = (int)s;
+            continue;
+        }
+        const ScenePar a = shared_settings(sh[bonded].par, true), b = shared_settings(sh[s].par, true);
+        if (std::memcmp(&a, &b, sizeof a) != 0) return;
+    }
+    const ScenePar kp = shared_settings(sh[bonded < 0 ? 0 : bonded].par, true);
+    par_ps = PS_SHARED;
+    std::memcpy(&par_pv, &kp, sizeof(ScenePar));
+}
+
 int World::step(int n_steps) {
     if (n_steps < 0) return fail(DEM_E_INVALID, "n_steps < 0");
+    update_param_source();
     int k = 0;
     if (use_graphs && !timing && n_steps > 0) {
+        if (par_ps != graph_ps || std::memcmp(&par_pv, &graph_par, sizeof(ScenePar)) != 0) {
+            drop_graph();
+            graph_ps = par_ps;
+            std::memcpy(&graph_par, &par_pv, sizeof(ScenePar));
+        }
         while (n_steps - k >= graph_steps) {
             const int p = parity;
             if (!graph[p] || graph_R[p] != graph_steps) {

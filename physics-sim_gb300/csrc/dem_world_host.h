@@ -191,6 +191,16 @@ class World {
     int graph_R[2] = {0, 0};
     int graph_kernels[2] = {0, 0};
     int graph1_kernels[2] = {0, 0};
+    // Where the Simulation kernels read the scene parameters (launch_interact,
+    // PS_*): a world of one scene passes them with each launch, a world whose
+    // scenes share their settings passes those.  step() sets both before any
+    // launch; graphs keep the values they were captured with, so step()
+    // captures anew when these change.
+    int par_ps = PS_SCENE;
+    ScenePar par_pv{};
+    void update_param_source();
+    int graph_ps = -1;
+    ScenePar graph_par{};
     int parity = 0;                    // which pr/dp/rr buffers are current
     void flip();
     int rebuild_kernels = 0;
