@@ -47,6 +47,8 @@ static inline double orc_dashpot_2zeta(float e) {
 #define V3 v3_f32
 #define EVBUF evbuf_f32
 #include "dem_oracle_step.inc"
+#undef LEN2
+#undef SQRT_R
 #undef REAL
 #undef REAL_IS_FLOAT
 #undef FN
@@ -68,6 +70,8 @@ static inline double orc_dashpot_2zeta(float e) {
 #define V3 v3_f64
 #define EVBUF evbuf_f64
 #include "dem_oracle_step.inc"
+#undef LEN2
+#undef SQRT_R
 #undef REAL
 #undef REAL_IS_FLOAT
 #undef FN

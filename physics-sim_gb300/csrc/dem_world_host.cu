@@ -1755,25 +1755,40 @@ void World::update_param_source() {
     if (sh.size() == 1) {
         par_ps = PS_ONE;
         std::memcpy(&par_pv, &sh[0].par, sizeof(ScenePar));  // padding too: graph_par is compared bytewise
+        // what the Simulation kernels never read from it: the interval
+        // counter's origin (end_of_step reads w.par) changes with every upload,
+        // and would make each step call after one capture its graphs anew
+        par_pv.step0 = 0;
+        par_pv.cc1_0 = 0;
+        par_pv.active = 0;
         return;
     }
     par_ps = PS_SCENE;
     std::memset(&par_pv, 0, sizeof par_pv);
-    if (sh.empty()) return;
-    const ScenePar k0 = shared_settings(sh[0].par, false);
-    int bonded = -1;  // a scene with bond records: its bond settings are the shared ones
+    // scenes the host has frozen (a server's free slots) read no parameters:
+    // the kernels stop at their act word first
+    int first = -1, bonded = -1;  // an active scene; one with bond records, whose bond settings are shared
+    ScenePar k_first, k_bonded;
     for (size_t s = 0; s < sh.size(); ++s) {
-        const ScenePar k = shared_settings(sh[s].par, false);
-        if (std::memcmp(&k, &k0, sizeof k) != 0) return;
+        if (!sh[s].active) continue;
+        if (first < 0) {
+            first = (int)s;
+            k_first = shared_settings(sh[s].par, false);
+        } else {
+            const ScenePar k = shared_settings(sh[s].par, false);
+            if (std::memcmp(&k, &k_first, sizeof k) != 0) return;
+        }
         if (sh[s].n_bonds <= 0) continue;
         if (bonded < 0) {
             bonded = (int)s;
+            k_bonded = shared_settings(sh[s].par, true);
             continue;
         }
-        const ScenePar a = shared_settings(sh[bonded].par, true), b = shared_settings(sh[s].par, true);
-        if (std::memcmp(&a, &b, sizeof a) != 0) return;
+        const ScenePar k = shared_settings(sh[s].par, true);
+        if (std::memcmp(&k, &k_bonded, sizeof k) != 0) return;
     }
-    const ScenePar kp = shared_settings(sh[bonded < 0 ? 0 : bonded].par, true);
+    if (first < 0) return;
+    const ScenePar kp = shared_settings(sh[bonded < 0 ? first : bonded].par, true);
     par_ps = PS_SHARED;
     std::memcpy(&par_pv, &kp, sizeof(ScenePar));
 }
