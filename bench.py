@@ -731,15 +731,62 @@ def run_ours_batch(args):
         fn()
         barrier()
         parts[name] = (time.perf_counter() - t1) * 1e3
-    del outs, up_tab, down_tab
-    e2e = {"value": job_rate(ntot * F * e2e_n, e2e_s * 1e3, ws, dev)[0], "unit": "particle-steps/s",
+    del up_tab, down_tab
+    single = {"value": job_rate(ntot * F * e2e_n, e2e_s * 1e3, ws, dev)[0], "cycle_ms": e2e_s * 1e3 / e2e_n,
+              "breakdown_ms": parts}
+
+    # The same cycle with the mix held as two batches (alternate scenes), so
+    # that one half's transfers overlap the other half's frame: upload A and
+    # step it, read B's previous frame back, upload B and step it, read A
+    # back.  Every cycle still moves every scene in and out once.  The halves
+    # move their arrays with host threads through page-locked blocks and the
+    # copy engines (dem_ext.host_copies), which leaves the SMs to the other
+    # half's frame (measured on the mix: 121 ms per cycle against 136 ms
+    # with the device's own copy kernels, and 140 ms for one batch).
+    halves = [list(range(0, len(items), 2)), list(range(1, len(items), 2))]
+    hb = [dem.Batch([items[k] for k in idx], device=local, plain_launches=args.plain, host_copies=1, **knobs)
+          for idx in halves]
+    h_up = [dem.SceneTable([(j, states[k]) for j, k in enumerate(idx)]) for idx in halves]
+    h_down = [dem.SceneTable([(j, outs[k]) for j, k in enumerate(idx)]) for idx in halves]
+
+    def pipelined(n):
+        A, B = hb
+        for c in range(n):
+            A.upload_many(h_up[0])
+            A.step(F)
+            if c > 0:
+                B.download_many(h_down[1])
+            B.upload_many(h_up[1])
+            B.step(F)
+            A.download_many(h_down[0])
+        B.download_many(h_down[1])
+
+    pipelined(1)                      # untimed: staging and graphs of both halves
+    for b in hb:
+        b.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    pipelined(e2e_n)
+    for b in hb:
+        b.synchronize()
+    barrier()
+    pipe_s = time.perf_counter() - t0
+    for b in hb:
+        b.close()
+    del outs, hb, h_up, h_down
+    e2e = {"value": job_rate(ntot * F * e2e_n, pipe_s * 1e3, ws, dev)[0], "unit": "particle-steps/s",
            "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": h2d,
-           "cycle_ms": e2e_s * 1e3 / e2e_n,
-           "breakdown_ms": parts,
-           "note": "dem_batch_upload_many of all scenes + dem_batch_step(frame) + dem_batch_download_many of all "
-                   "scenes, from and into the callers' host arrays (scene struct tables built once), from the "
-                   "states at the end of the horizon; breakdown_ms: one extra cycle with each call waited for"}
+           "cycle_ms": pipe_s * 1e3 / e2e_n,
+           "single_batch": single,
+           "note": "per cycle every scene is restored from the caller's host arrays (dem_batch_upload_many), "
+                   "advanced one frame (dem_batch_step) and read back into the caller's arrays "
+                   "(dem_batch_download_many), from the states at the end of the horizon; the mix is held as "
+                   "two batches of alternate scenes so that one half's transfers overlap the other half's "
+                   "frame, each half moving its arrays through page-locked blocks by host threads and the copy "
+                   "engines (dem_ext.host_copies = 1); single_batch: the same cycle on one batch whose copy "
+                   "kernels read and write the callers' arrays, calls in sequence (its breakdown_ms: one extra "
+                   "cycle with each call waited for)"}
 
     # settled states: the mix run on (untimed) to --settle-steps, then frames timed there
     settled = None
