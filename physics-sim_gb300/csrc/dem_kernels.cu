@@ -845,6 +845,10 @@ __device__ __forceinline__ void list_head(const DevWorld &w, int i, int16_t *h, 
     if (nsm != sm) w.smask[i] = nsm;
 }
 
+// Candidate lists one particle a thread in internal order, the cell table's
+// cells read from global memory: the form for sparse worlds (about one
+// particle a search cell or fewer, where a block's particles span too many
+// cells for staging to pay).
 __device__ __forceinline__ void list_build_one(const DevWorld &w, int i) {
     if (!chunk_live(w, i)) return;
     const uint32_t m = w.meta[i];
@@ -909,6 +913,208 @@ __global__ void __launch_bounds__(PK_MAX_THREADS) k_list_build(DevWorld w, const
     FOR_EACH_ITEM(i, w.N) list_build_one(w, i);
 }
 
+// The candidate-list head of a particle that is not in a search cell
+// (frozen scene, zero radius, large particle) and its rebuild records;
+// false for the others, whose lists k_list_tiles builds.
+__device__ __forceinline__ bool list_head_only(const DevWorld &w, int i) {
+    if (!chunk_live(w, i)) return true;
+    const uint32_t m = w.meta[i];
+    const ScenePar &P = w.par[meta_scene(m)];
+    const float4 pa = w.pr[i];
+    int16_t *h = reinterpret_cast<int16_t *>(w.nl + 2 * (size_t)i);
+    if (!w.act[meta_scene(m)] || pa.z == 0.0f) {
+        w.pbuild[i] = make_float2(pa.x, pa.y);
+        list_head(w, i, h, 0);
+        w.kbuild[i] = (uint32_t)P.dead_cell;
+        return true;
+    }
+    if (m & M_BIG) {
+        w.pbuild[i] = make_float2(pa.x, pa.y);
+        list_head(w, i, h, NL_BIG);
+        w.kbuild[i] = (uint32_t)P.big_cell;
+        return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(PK_MAX_THREADS) k_list_heads(DevWorld w, const int32_t *gate) {
+    if (gated_off(gate)) return;
+    FOR_EACH_ITEM(i, w.N) list_head_only(w, i);
+}
+
+// Candidate lists of the particles in search cells, a block per LT_THREADS
+// consecutive entries of the cell list (cell order: each scene's grid row by
+// row), one particle per thread.  When the block's particles lie in at most
+// LT cells [c0, c1) of one scene, the block first stages in shared memory
+// the cell starts and the particles (index and position record) of the cell
+// ranges [c0 + d g_w - st, c1 + d g_w + st), d in [-st, st]: every
+// neighbour cell of those cells, whether or not the run wraps a grid row.
+// Each particle then scans its (2 st + 1)^2 cells there, rows top to bottom
+// and cells and members in cell order -- the order and the test of a scan
+// of the cell table, so the lists are the same.  Rows the staging does not
+// hold (a sparse run of cells, more than LT_CAP particles, another scene's
+// particle) are read from the cell table.
+constexpr int LT = 256;              // cells a block's particles may span for staging
+constexpr int LT_ST = 2;             // largest stencil the staging holds
+constexpr int LT_ROWS = 2 * LT_ST + 1;
+constexpr int LT_CELLS = LT + 2 * LT_ST + 1;  // cell starts per staged row (one more than its cells)
+constexpr int LT_CAP = 512;          // staged particles per block
+constexpr int LT_THREADS = 128;
+
+struct ListScan {
+    int cnt = 0;
+    bool over = false;
+};
+
+__device__ __forceinline__ void list_consider(const ScenePar &P, int i, float4 pa, int b, float4 pb, int16_t *h,
+                                              ListScan &ls) {
+    if (b == i) return;
+    if (pb.z == 0.0f) return;
+    const float dx = pb.x - pa.x, dy = pb.y - pa.y;
+    const float t = (pa.z + pb.z + P.skin) * 1.00001f;
+    if (dx * dx + dy * dy > t * t) return;
+    const int off = b - i;
+    if (ls.cnt < NL && off >= -32768 && off <= 32767) h[1 + ls.cnt] = (int16_t)off;
+    else ls.over = true;
+    ++ls.cnt;
+}
+
+// the search cell of a particle in a search cell (as keys_one files it), or -1
+__device__ __forceinline__ int regular_cell(const DevWorld &w, int b, int &scene) {
+    const uint32_t m = w.meta[b];
+    scene = (int)meta_scene(m);
+    const ScenePar &P = w.par[scene];
+    const float4 p = w.pr[b];
+    if (p.z == 0.0f || (m & M_BIG)) return -1;
+    int cx, cy;
+    search_xy(P, p.x, p.y, cx, cy);
+    return P.cell_base + cy * P.g_w + cx;
+}
+
+__global__ void __launch_bounds__(LT_THREADS) k_list_tiles(DevWorld w, const int32_t *gate) {
+    if (gated_off(gate)) return;
+    __shared__ float4 s_pr[LT_CAP];
+    __shared__ int32_t s_idx[LT_CAP];
+    __shared__ int32_t s_cs[LT_ROWS * LT_CELLS];
+    __shared__ int32_t s_lo[LT_ROWS], s_hi[LT_ROWS], s_off[LT_ROWS];
+    __shared__ int s_scene, s_ca[2], s_sa[2];
+    const int total = w.cell_start[w.C];  // particles in cells
+    const int runs = (total + LT_THREADS - 1) / LT_THREADS;
+    for (int run = blockIdx.x; run < runs; run += gridDim.x) {
+        const int first = run * LT_THREADS, last = min(first + LT_THREADS, total) - 1;
+        __syncthreads();  // the previous run's staging is no longer read
+        // the cells of the run's first and last particles (two threads), then
+        // each staged row's range (one thread a row), then their offsets
+        if (threadIdx.x < 2) s_ca[threadIdx.x] = regular_cell(w, w.sorted[threadIdx.x ? last : first], s_sa[threadIdx.x]);
+        __syncthreads();
+        const int ca = s_ca[0], cb = s_ca[1], sa = s_sa[0];
+        const bool stage = ca >= 0 && cb >= 0 && sa == s_sa[1] && cb - ca < LT && w.par[sa].stencil <= LT_ST;
+        if (stage && threadIdx.x < LT_ROWS) {
+            const int r = threadIdx.x;
+            const ScenePar &P = w.par[sa];
+            const int st = P.stencil, gw = P.g_w;
+            const int glo = P.cell_base, ghi = P.cell_base + P.g_w * P.g_h;  // the scene's search cells
+            const int d = r - LT_ST;
+            const int lo = max(ca + d * gw - st, glo), hi = min(cb + 1 + d * gw + st, ghi);
+            s_lo[r] = lo;
+            s_hi[r] = hi;
+            s_off[r] = (d < -st || d > st || lo >= hi) ? -1 : w.cell_start[hi] - w.cell_start[lo];  // count
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int off = 0;
+            if (stage)
+                for (int r = 0; r < LT_ROWS; ++r) {
+                    const int n = s_off[r];
+                    if (n < 0 || off + n > LT_CAP) {
+                        s_off[r] = -1;  // not staged: read from the cell table
+                        continue;
+                    }
+                    s_off[r] = off;
+                    off += n;
+                }
+            s_scene = stage ? sa : -1;
+        }
+        __syncthreads();
+        const int st_scene = s_scene;
+        if (st_scene >= 0) {
+            for (int r = 0; r < LT_ROWS; ++r) {
+                if (s_off[r] < 0) continue;
+                const int lo = s_lo[r], hi = s_hi[r];
+                for (int k = threadIdx.x; k <= hi - lo; k += LT_THREADS)
+                    s_cs[r * LT_CELLS + k] = w.cell_start[lo + k];
+            }
+            __syncthreads();
+            for (int r = 0; r < LT_ROWS; ++r) {
+                if (s_off[r] < 0) continue;
+                const int base = s_cs[r * LT_CELLS], n = s_cs[r * LT_CELLS + (s_hi[r] - s_lo[r])] - base;
+                for (int k = threadIdx.x; k < n; k += LT_THREADS) {
+                    const int b = w.sorted[base + k];
+                    s_idx[s_off[r] + k] = b;
+                    s_pr[s_off[r] + k] = w.pr[b];
+                }
+            }
+            __syncthreads();
+        }
+        const int q = first + (int)threadIdx.x;
+        if (q > last) continue;
+        const int i = w.sorted[q];
+        if (!chunk_live(w, i)) continue;
+        const uint32_t m = w.meta[i];
+        const int s = (int)meta_scene(m);
+        const ScenePar &P = w.par[s];
+        const float4 pa = w.pr[i];
+        if (!w.act[s] || pa.z == 0.0f || (m & M_BIG)) continue;  // k_list_heads
+        w.pbuild[i] = make_float2(pa.x, pa.y);
+        int16_t *h = reinterpret_cast<int16_t *>(w.nl + 2 * (size_t)i);
+        int gx, gy;
+        search_xy(P, pa.x, pa.y, gx, gy);
+        w.kbuild[i] = (uint32_t)(P.cell_base + gy * P.g_w + gx);
+        const int cy0 = max(gy - P.stencil, 0), cy1 = min(gy + P.stencil, P.g_h - 1);
+        const int cx0 = max(gx - P.stencil, 0), cx1 = min(gx + P.stencil, P.g_w - 1);
+        ListScan ls;
+        for (int cy = cy0; cy <= cy1; ++cy) {
+            const int row = P.cell_base + cy * P.g_w;
+            const int a = row + cx0, z = row + cx1 + 1;  // cells [a, z)
+            int hit = -1;
+            if (s == st_scene)
+                for (int r = 0; r < LT_ROWS; ++r)
+                    if (s_off[r] >= 0 && s_lo[r] <= a && z <= s_hi[r]) {
+                        hit = r;
+                        break;
+                    }
+            if (hit >= 0) {
+                const int *cs = s_cs + hit * LT_CELLS;
+                const int at = s_off[hit] - cs[0];
+                const int beg = cs[a - s_lo[hit]] + at, fin = cs[z - s_lo[hit]] + at;
+                for (int k = beg; k < fin; ++k) list_consider(P, i, pa, s_idx[k], s_pr[k], h, ls);
+            } else {
+                const int beg = w.cell_start[a], fin = w.cell_start[z];
+                for (int k = beg; k < fin; ++k) {
+                    const int b = w.sorted[k];
+                    list_consider(P, i, pa, b, w.pr[b], h, ls);
+                }
+            }
+        }
+        int flags = 0;
+        if (P.n_big > 0) {
+            int bf, bn;
+            big_cell(w, P, bf, bn);
+            for (int k = 0; k < bn; ++k) {
+                const float4 pb = w.pr[w.sorted[bf + k]];
+                const float dx = pb.x - pa.x, dy = pb.y - pa.y;
+                const float t = (pa.z + pb.z + P.skin) * 1.00001f;
+                if (pb.z != 0.0f && dx * dx + dy * dy <= t * t) {
+                    flags = NL_NEAR_BIG;
+                    break;
+                }
+            }
+        }
+        list_head(w, i, h, (ls.over ? NL_OVERFLOW : ls.cnt) | flags);
+        if (ls.over) atomicAdd(&w.stats[5], 1ull);
+    }
+}
+
 __global__ void k_rebuild_done(DevWorld w, const int32_t *gate) {
     if (gated_off(gate)) return;
     *w.rebuild = 0;
@@ -923,11 +1129,22 @@ __global__ void k_rebuild_done(DevWorld w, const int32_t *gate) {
 // conditional graph node) takes one block per chunk instead, since particles
 // differ widely in candidate work and the hardware then balances the blocks
 // (a single 4 M-particle scene rebuilds 0.5 % faster per step that way)
-void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate, bool every_step) {
-    if (w.N == 0) return;
-    const int g = every_step ? capped_grid(k_list_build, w.N, block, block) : (w.N + block - 1) / block;
-    k_list_build<<<g, block, 0, st>>>(w, gate);
+// staged: the dense form (k_list_heads + k_list_tiles), else k_list_build;
+// both build the same lists
+int launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate, bool every_step,
+                      bool staged) {
+    if (w.N == 0) return 0;
+    if (staged) {
+        k_list_heads<<<capped_grid(k_list_heads, w.N, block, block), block, 0, st>>>(w, gate);
+        const long long runs = ((long long)w.N + LT_THREADS - 1) / LT_THREADS;  // particles in cells <= N
+        const int g = every_step ? capped_grid(k_list_tiles, runs, 1, LT_THREADS) : (int)runs;
+        k_list_tiles<<<g, LT_THREADS, 0, st>>>(w, gate);
+    } else {
+        const int g = every_step ? capped_grid(k_list_build, w.N, block, block) : (w.N + block - 1) / block;
+        k_list_build<<<g, block, 0, st>>>(w, gate);
+    }
     k_rebuild_done<<<1, 1, 0, st>>>(w, gate);
+    return staged ? 3 : 2;
 }
 
 // -------------------------------------------------------------- interact

@@ -212,7 +212,8 @@ void launch_keys(const DevWorld &w, int block, cudaStream_t st, const int32_t *g
 int launch_broad_phase(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate);
 void launch_reorder(const DevWorld &w, const DevWorld &spare, int block, cudaStream_t st,
                     const int32_t *gate);
-void launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate, bool every_step);
+int launch_list_build(const DevWorld &w, int block, cudaStream_t st, const int32_t *gate, bool every_step,
+                      bool staged);
 // the Simulation pass of one step; with `fuse` also the next step's LOM pass
 // (into the other pr/dp/rr buffers), whose rebuild condition is set on `cond`
 // when in a graph.  A fused step is never a call's last step; lom_final: the

@@ -1594,9 +1594,25 @@ void World::enqueue_rebuild(cudaStream_t st, const int32_t *gate, bool every_ste
     launch_reorder(d, spare, block, st, gate);
     rec_event(T_REORDER, st);
     rec_event(T_LIST, st);
-    launch_list_build(d, block, st, gate, every_step);
+    const int lk = launch_list_build(d, block, st, gate, every_step, dense_cells());
     rec_event(T_LIST, st);
-    rebuild_kernels = 1 + bp + 3 + 2;
+    rebuild_kernels = 1 + bp + 3 + lk;
+}
+
+// whether the active scenes hold 1.5 particles or more a search cell on
+// average: then a block's particles span few cells and the candidate lists
+// are built from neighbour cells staged in shared memory (k_list_tiles);
+// sparser worlds read the cell table directly (measured: the 4 M-particle
+// impact bed, 5.3 particles a cell, 0.59 -> 0.38 ms per list build staged;
+// the 512-scene mix, 0.74 a cell, 0.21 -> 0.44 ms)
+bool World::dense_cells() const {
+    long long cells = 0, n = 0;
+    for (const auto &h : sh) {
+        if (!h.active) continue;
+        cells += (long long)h.par.g_w * h.par.g_h;
+        n += h.n;
+    }
+    return cells > 0 && 2 * n >= 3 * cells;
 }
 
 void World::rec_event(int kind, cudaStream_t st) {

@@ -159,6 +159,7 @@ class World {
     void enqueue_rebuild(cudaStream_t st, const int32_t *gate, bool every_step);
     int capture_graph(int R, cudaGraphExec_t *out, int *kernels);
     void drop_graph();
+    bool dense_cells() const;
     DevWorld spare{};
     std::vector<void *> owned;
     // device copy of one scene in the reference layouts (uploads, downloads)

@@ -68,3 +68,36 @@ def test_autotune_picks_listed_values_and_keeps_results():
     for k in range(len(items)):
         assert_same_state(got[k], ref[k], "scene %d: " % k)
     assert got_ev == ref_ev
+
+
+def _dense_items():
+    # beds of c2's model (about two particles a search cell at the default
+    # cell size): their candidate lists come from neighbour cells staged in
+    # shared memory, whose runs of 128 cell-list entries here also straddle
+    # scene boundaries and wrap grid rows
+    items = [dem_scenes.c2_impact(cols=40, rows=90, seed=20 + k, projectile_radius=5.0, projectile_speed=250.0)
+             for k in range(3)]
+    items.append(dem_scenes.c2_impact(cols=17, rows=120, seed=30, projectile_radius=5.0, projectile_speed=200.0))
+    return items
+
+
+@pytest.mark.parametrize("knobs", [
+    dict(search_cell_factor=1.36, list_skin=0.2),   # larger cells: staged, 3 x 3
+    dict(search_cell_factor=0.68, list_skin=0.2),   # 5 x 5 search of smaller cells
+    dict(search_cell_factor=1.0, list_skin=0.45, plain_launches=1),
+])
+def test_dense_batch_lists_do_not_depend_on_the_cell_size(knobs):
+    """The staged list build (dense worlds) and the cell-table scan (sparse
+    ones) build the same candidate lists: a batch of dense beds with a fast
+    projectile each (rebuilds every few steps) steps bit for bit alike under
+    cell sizes on both sides of the density threshold and both stencils."""
+    items = _dense_items()
+    sc, p, ext = items[0]
+    with dem.Context(sc, p, **ext) as ctx:  # default cell size: a dense world
+        gw, gh = ctx.search_grid()[3:5]
+    assert 2 * sc["radii"].shape[0] >= 3 * gw * gh
+    ref, ref_ev = _run(items, 280)
+    got, got_ev = _run(items, 280, **knobs)
+    for k in range(len(items)):
+        assert_same_state(got[k], ref[k], "scene %d: " % k)
+    assert got_ev == ref_ev
