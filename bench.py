@@ -943,10 +943,14 @@ def run_serve(args):
     offered = float(sum(int(pool[pick[k]][0]["radii"].shape[0]) * int(horizons[k]) for k in range(len(arrivals))))
     sv = dem.Server(device=local, memory_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
                     max_active_particles=args.serve_active, reorder_interval=35)
+    sampler = ClockSampler(local)
+    sampler.start()
+    sampler.mark()
     t0 = time.perf_counter()
     nxt = 0
     submitted = {}
     done = {}
+    finals = []  # (final state, params, ext) of the first completed requests, for the FP64-twin error
     max_queue = max_running = 0
     series = []
     next_sample = 0.0
@@ -969,13 +973,22 @@ def run_serve(args):
             next_sample = tp + 1.0
         for rid in sv.poll():
             k, work = submitted[rid]
-            sv.finish(rid)
+            if len(finals) < 4:
+                out, _, _ = sv.fetch(rid)
+                finals.append((out, pool[pick[k]][1], pool[pick[k]][2]))
+            else:
+                sv.finish(rid)
             done[rid] = (k, tp - arrivals[k], work)
         if st["running"] == 0 and st["queued"] == 0 and nxt < len(arrivals):
             time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
     elapsed = time.perf_counter() - t0
+    sampler.mark()
+    sampler.stop()
     st = sv.stats()
     sv.close()
+    fp64 = fp64_twin_error(finals, local) if finals else None
+    if fp64 is not None:
+        fp64["state"] = "the final states of the first %d completed requests" % len(finals)
     lat = np.array([v[1] for v in done.values()]) if done else np.zeros(1)
     in_window = [v[1] for v in done.values() if arrivals[v[0]] < window]
     value = st["particle_steps"] / elapsed
@@ -1002,7 +1015,10 @@ def run_serve(args):
                        "drained": bool(len(done) == len(arrivals))},
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
                           "p99": float(np.percentile(lat, 99)), "max": float(lat.max()),
-                          "of": "arrival to completion, every completed request (%d)" % len(in_window)}}
+                          "of": "arrival to completion, every completed request (%d)" % len(in_window)},
+            "clocks": sampler.summary()}
+    if fp64 is not None:
+        line["fp64_error"] = fp64
     print(json.dumps(line), flush=True)
 
 
