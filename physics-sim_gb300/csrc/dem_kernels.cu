@@ -1261,7 +1261,8 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // Simulation kernels take 7.7 % less time).  PS_SHARED: the scenes differ
 // only in geometry and record bases; their common settings and model
 // constants (the fields read through U) come with the launch, the rest from
-// w.par[scene].
+// w.par[scene].  Every field read through U is one that shared_settings
+// (dem_world.cuh) copies (tests/test_param_source.py checks this source).
 template <int PART, bool FUSE, int FORM, int PS>
 __device__ __forceinline__ void interact_particle(const DevWorld &w, int i, Narrow &nr, bool lom_final,
                                                   const ScenePar &Pv) {
